@@ -1,0 +1,388 @@
+"""ctypes binding of the C ABI (include/ann_gpu.h) with numpy in and out.
+
+``Context`` mirrors the reference's NNP usage (src/nnp/nnpce.cpp:273-287): load a potential
+(NNP::read), then compute energies / forces of structures (NeighborList + NNP::symm +
+NNP::compute / PotNNPE::compute). Errors raise AnnError with the library's message, the way the
+reference raises std::invalid_argument / std::runtime_error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+FP64 = 0
+MIXED = 1
+NEWTON_ALL_IMAGES = 0
+NEWTON_UNTRANSLATED = 1
+
+_HERE = Path(__file__).resolve().parent
+_LIB = None
+
+
+class AnnError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[ann error {code}] {msg}")
+        self.code = code
+
+
+class Options(C.Structure):
+    _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("newton", C.c_int32), ("max_neighbors", C.c_int32),
+                ("use_graphs", C.c_int32), ("mlp_backend", C.c_int32)]
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("ANN_GPU_LIB", _HERE / "libann_gpu.so"))
+
+
+def build_library(verbose_ptxas: bool = False) -> Path:
+    from .build import build
+    return build(verbose_ptxas=verbose_ptxas)
+
+
+_D = C.POINTER(C.c_double)
+_I32 = C.POINTER(C.c_int32)
+_I64 = C.POINTER(C.c_int64)
+_V = C.c_void_p
+
+_SIGS = {
+    "ann_default_options": (None, [C.POINTER(Options)]),
+    "ann_create": (C.c_int, [C.POINTER(_V), C.POINTER(Options)]),
+    "ann_destroy": (C.c_int, [_V]),
+    "ann_last_error": (C.c_char_p, [_V]),
+    "ann_abi_version": (C.c_int, []),
+    "ann_load_potential": (C.c_int, [_V, C.c_char_p]),
+    "ann_load_potential_text": (C.c_int, [_V, C.c_char_p]),
+    "ann_write_potential": (C.c_int, [_V, C.c_char_p]),
+    "ann_num_types": (C.c_int, [_V, _I32]),
+    "ann_type_index": (C.c_int, [_V, C.c_char_p, _I32]),
+    "ann_type_name": (C.c_int, [_V, C.c_int32, C.c_char_p, C.c_int32]),
+    "ann_cutoff": (C.c_int, [_V, _D]),
+    "ann_num_inputs": (C.c_int, [_V, C.c_int32, _I32]),
+    "ann_num_params": (C.c_int, [_V, _I64]),
+    "ann_get_params": (C.c_int, [_V, _D, C.c_int64]),
+    "ann_set_params": (C.c_int, [_V, _D, C.c_int64]),
+    "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
+    "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
+    "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_batch_upload": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D]),
+    "ann_batch_set_device": (C.c_int, [_V, C.c_int32, _I64, _V, _V, _V]),
+    "ann_batch_compute": (C.c_int, [_V, C.c_int32, C.c_int32]),
+    "ann_batch_download": (C.c_int, [_V, _D, _D, _D]),
+    "ann_batch_results_device": (C.c_int, [_V, _V, _V, _V]),
+    "ann_synchronize": (C.c_int, [_V]),
+    "ann_kernel_count": (C.c_int, [_V, _I64]),
+    "ann_profile_phases": (C.c_int, [_V, C.c_int32]),
+    "ann_phase_times": (C.c_int, [_V, _D, C.c_int32]),
+    "ann_stream": (_V, [_V]),
+    "ann_symm_width": (C.c_int, [_V, _I32]),
+    "ann_get_symm": (C.c_int, [_V, _D]),
+    "ann_get_dedg": (C.c_int, [_V, _D]),
+    "ann_get_atom_energies": (C.c_int, [_V, _D]),
+    "ann_num_neighbors": (C.c_int, [_V, _I64]),
+    "ann_get_neighbors": (C.c_int, [_V, _I32, _I32, _I32, _D, C.c_int64]),
+    "ann_train_forward": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, C.c_double, C.c_double, C.c_int32, _D]),
+    "ann_train_backward": (C.c_int, [_V, C.c_double, _D, C.c_int64]),
+    "ann_md_init": (C.c_int, [_V, C.c_int64, _D, _D, _I32, _D, _D, C.c_double, C.c_double, C.c_int32]),
+    "ann_md_run": (C.c_int, [_V, C.c_int32, _D, _D, _I32]),
+    "ann_md_get_state": (C.c_int, [_V, _D, _D, _D]),
+}
+
+ABI_SYMBOLS = tuple(_SIGS)
+
+
+def peaks() -> dict:
+    """Roofline denominators: the measured copy bandwidth / bf16 GEMM rate of the GB300s
+    (MEASURED_PEAKS.json at the repository root), else the stated fallback."""
+    import json
+    p = _HERE.parent / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "bf16_tflops_sustained": float(d.get("bf16_tflops_sustained", d["bf16_tflops"])),
+                "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0)), "source": "measured (MEASURED_PEAKS.json)"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "sm_max_mhz": 2070.0,
+            "source": "fallback (6.8 TB/s, 1.9 PFLOP/s)"}
+
+
+def load_library(path: str | Path | None = None):
+    """Load libann_gpu.so (raises AnnError if it is missing: there is no fallback)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else library_path()
+    if not p.exists():
+        raise AnnError(-1, f"{p} not built: run `python -m ann_gb300.build` (the GPU path has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _i32(a):
+    return None if a is None else a.ctypes.data_as(_I32)
+
+
+def _i64(a):
+    return None if a is None else a.ctypes.data_as(_I64)
+
+
+def pack_batch(structures):
+    """Pack a list of (posn[N,3], type[N], cell[3,3] with lattice vectors as columns) into the
+    flat arrays of the C ABI: offsets[S+1] int64, posn[3N] f64, type[N] i32, cell[9S] f64
+    (column-major: cell[9s + 3c + r] = R[r, c])."""
+    offs = np.zeros(len(structures) + 1, dtype=np.int64)
+    for s, (x, t, R) in enumerate(structures):
+        offs[s + 1] = offs[s] + len(t)
+    posn = np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=np.float64).reshape(-1, 3) for x, _, _ in structures])
+                                if structures else np.zeros((0, 3)), dtype=np.float64)
+    types = np.ascontiguousarray(np.concatenate([np.asarray(t, dtype=np.int32) for _, t, _ in structures])
+                                 if structures else np.zeros(0, dtype=np.int32), dtype=np.int32)
+    cell = np.ascontiguousarray(np.stack([np.asarray(R, dtype=np.float64).T.reshape(9) for _, _, R in structures])
+                                if structures else np.zeros((0, 9)), dtype=np.float64)
+    return offs, posn, types, cell
+
+
+class Context:
+    """One device context: a loaded potential plus device buffers (one per host thread)."""
+
+    def __init__(self, device: int = 0, precision: int = MIXED, newton: int = NEWTON_ALL_IMAGES, max_neighbors: int = 0,
+                 use_graphs: bool = True, mlp_backend: int = 0):
+        self.lib = load_library()
+        o = Options()
+        self.lib.ann_default_options(C.byref(o))
+        o.device, o.precision, o.newton, o.max_neighbors = device, precision, newton, max_neighbors
+        o.use_graphs, o.mlp_backend = int(use_graphs), mlp_backend
+        h = _V()
+        rc = self.lib.ann_create(C.byref(h), C.byref(o))
+        if rc != 0:
+            raise AnnError(rc, self.lib.ann_last_error(None).decode())
+        self.h = h
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ann_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise AnnError(rc, self.lib.ann_last_error(self.h).decode())
+
+    # ---- potential
+    def load(self, path):
+        self._ck(self.lib.ann_load_potential(self.h, str(path).encode()))
+        return self
+
+    def load_text(self, text: str):
+        self._ck(self.lib.ann_load_potential_text(self.h, text.encode()))
+        return self
+
+    def write(self, path):
+        self._ck(self.lib.ann_write_potential(self.h, str(path).encode()))
+
+    @property
+    def ntypes(self) -> int:
+        n = C.c_int32()
+        self._ck(self.lib.ann_num_types(self.h, C.byref(n)))
+        return n.value
+
+    def type_index(self, name: str) -> int:
+        n = C.c_int32()
+        self._ck(self.lib.ann_type_index(self.h, name.encode(), C.byref(n)))
+        return n.value
+
+    def type_name(self, i: int) -> str:
+        buf = C.create_string_buffer(256)
+        self._ck(self.lib.ann_type_name(self.h, i, buf, 256))
+        return buf.value.decode()
+
+    @property
+    def rc(self) -> float:
+        v = C.c_double()
+        self._ck(self.lib.ann_cutoff(self.h, C.byref(v)))
+        return v.value
+
+    def num_inputs(self, t: int) -> int:
+        n = C.c_int32()
+        self._ck(self.lib.ann_num_inputs(self.h, t, C.byref(n)))
+        return n.value
+
+    @property
+    def nparams(self) -> int:
+        n = C.c_int64()
+        self._ck(self.lib.ann_num_params(self.h, C.byref(n)))
+        return n.value
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.nparams)
+        self._ck(self.lib.ann_get_params(self.h, _d(p), len(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        self._ck(self.lib.ann_set_params(self.h, _d(p), len(p)))
+
+    def set_input_scaling(self, t: int, inpw, inpb):
+        w = np.ascontiguousarray(inpw, dtype=np.float64)
+        b = np.ascontiguousarray(inpb, dtype=np.float64)
+        self._ck(self.lib.ann_set_input_scaling(self.h, t, _d(w), _d(b), len(w)))
+
+    def init_network(self, t: int, seed: int, dist: int = 0, init: int = 4, sigma_b: float = 0.001, sigma_w: float = 1.0):
+        self._ck(self.lib.ann_init_network(self.h, t, seed, dist, init, sigma_b, sigma_w))
+
+    # ---- compute
+    def compute(self, offs, posn, types, cell, forces=True, virial=True, precision=None):
+        """E (+F, virial) of a packed batch; returns (energy[S], forces[N,3] or None, virial[S,3,3] or None)."""
+        prec = self.precision if precision is None else precision
+        S = len(offs) - 1
+        N = int(offs[-1])
+        e = np.zeros(S)
+        f = np.zeros((N, 3)) if forces else None
+        w = np.zeros((S, 3, 3)) if virial else None
+        self._ck(self.lib.ann_compute(self.h, S, _i64(np.ascontiguousarray(offs, np.int64)), _d(np.ascontiguousarray(posn, np.float64)),
+                                      _i32(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
+                                      _d(e), _d(f), _d(w), prec))
+        return e, f, w
+
+    def upload(self, offs, posn, types, cell):
+        self._keep = [np.ascontiguousarray(offs, np.int64), np.ascontiguousarray(posn, np.float64),
+                      np.ascontiguousarray(types, np.int32), np.ascontiguousarray(cell, np.float64)]
+        o, x, t, c = self._keep
+        self._S, self._N = len(o) - 1, int(o[-1])
+        self._ck(self.lib.ann_batch_upload(self.h, self._S, _i64(o), _d(x), _i32(t), _d(c)))
+
+    def compute_resident(self, precision=None, forces=True):
+        self._ck(self.lib.ann_batch_compute(self.h, self.precision if precision is None else precision, int(forces)))
+
+    def download(self, forces=True, virial=True):
+        e = np.zeros(self._S)
+        f = np.zeros((self._N, 3)) if forces else None
+        w = np.zeros((self._S, 3, 3)) if virial else None
+        self._ck(self.lib.ann_batch_download(self.h, _d(e), _d(f), _d(w)))
+        return e, f, w
+
+    def synchronize(self):
+        self._ck(self.lib.ann_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return self.lib.ann_stream(self.h) or 0
+
+    # ---- instrumentation
+    def kernel_count(self) -> int:
+        n = C.c_int64()
+        self._ck(self.lib.ann_kernel_count(self.h, C.byref(n)))
+        return n.value
+
+    def kernels_per_batch(self, precision=None) -> int:
+        """Kernels one resident-batch evaluation launches (graph replays count their nodes)."""
+        k0 = self.kernel_count()
+        self.compute_resident(precision)
+        self.synchronize()
+        return self.kernel_count() - k0
+
+    def profile_phases(self, enable: bool):
+        self._ck(self.lib.ann_profile_phases(self.h, int(enable)))
+
+    def phase_times(self) -> np.ndarray:
+        ms = np.zeros(6)
+        self._ck(self.lib.ann_phase_times(self.h, _d(ms), 6))
+        return ms
+
+    # ---- inspection
+    def symm_width(self) -> int:
+        n = C.c_int32()
+        self._ck(self.lib.ann_symm_width(self.h, C.byref(n)))
+        return n.value
+
+    def symm(self) -> np.ndarray:
+        G = np.zeros((self._last_natoms(), self.symm_width()))
+        self._ck(self.lib.ann_get_symm(self.h, _d(G)))
+        return G
+
+    def dedg(self) -> np.ndarray:
+        G = np.zeros((self._last_natoms(), self.symm_width()))
+        self._ck(self.lib.ann_get_dedg(self.h, _d(G)))
+        return G
+
+    def atom_energies(self) -> np.ndarray:
+        e = np.zeros(self._last_natoms())
+        self._ck(self.lib.ann_get_atom_energies(self.h, _d(e)))
+        return e
+
+    def _last_natoms(self) -> int:
+        return getattr(self, "_N", 0)
+
+    def neighbors(self, with_vectors=False):
+        n = C.c_int64()
+        self._ck(self.lib.ann_num_neighbors(self.h, C.byref(n)))
+        k = n.value
+        i = np.zeros(k, np.int32)
+        j = np.zeros(k, np.int32)
+        img = np.zeros((k, 3), np.int32)
+        r = np.zeros((k, 3)) if with_vectors else None
+        self._ck(self.lib.ann_get_neighbors(self.h, _i32(i), _i32(j), _i32(img), _d(r), k))
+        return i, j, img, r
+
+    # ---- training
+    def train_forward(self, offs, posn, types, cell, e_ref, f_ref, w_energy=1.0, w_force=0.1, precision=None):
+        prec = self.precision if precision is None else precision
+        self._S, self._N = len(offs) - 1, int(offs[-1])
+        loss = np.zeros(3)
+        self._ck(self.lib.ann_train_forward(self.h, self._S, _i64(np.ascontiguousarray(offs, np.int64)),
+                                            _d(np.ascontiguousarray(posn, np.float64)), _i32(np.ascontiguousarray(types, np.int32)),
+                                            _d(np.ascontiguousarray(cell, np.float64)), _d(np.ascontiguousarray(e_ref, np.float64)),
+                                            _d(np.ascontiguousarray(f_ref, np.float64)), w_energy, w_force, prec, _d(loss)))
+        return loss
+
+    def train_backward(self, scale=1.0) -> np.ndarray:
+        g = np.zeros(self.nparams)
+        self._ck(self.lib.ann_train_backward(self.h, scale, _d(g), len(g)))
+        return g
+
+    # ---- MD
+    def md_init(self, posn, vel, types, cell, masses, dt_fs=2.0, skin=0.5, precision=None):
+        prec = self.precision if precision is None else precision
+        self._N = len(types)
+        self._S = 1
+        x = np.ascontiguousarray(posn, np.float64)
+        v = np.ascontiguousarray(vel, np.float64)
+        t = np.ascontiguousarray(types, np.int32)
+        c = np.ascontiguousarray(np.asarray(cell, np.float64).T.reshape(9))
+        m = np.ascontiguousarray(masses, np.float64)
+        self._ck(self.lib.ann_md_init(self.h, len(t), _d(x), _d(v), _i32(t), _d(c), _d(m), dt_fs, skin, prec))
+
+    def md_run(self, nsteps):
+        pe, ke, rb = C.c_double(), C.c_double(), C.c_int32()
+        self._ck(self.lib.ann_md_run(self.h, nsteps, C.byref(pe), C.byref(ke), C.byref(rb)))
+        return pe.value, ke.value, rb.value
+
+    def md_state(self):
+        x = np.zeros((self._N, 3))
+        v = np.zeros((self._N, 3))
+        f = np.zeros((self._N, 3))
+        self._ck(self.lib.ann_md_get_state(self.h, _d(x), _d(v), _d(f)))
+        return x, v, f

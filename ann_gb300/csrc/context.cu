@@ -1,0 +1,870 @@
+// ann_ctx: device buffers, the per-batch kernel sequence, CUDA-graph capture, and the extern "C"
+// entry points of include/ann_gpu.h. No C++ exception crosses the C boundary.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/ann_gpu.h"
+#include "kernels.hpp"
+#include "plan_build.hpp"
+#include "potential.hpp"
+
+namespace ann {
+// training loss / adjoint seeds (train.cu)
+void launch_train_loss(int nstruc, int natoms, const int32_t* off, const int32_t* sid, const double* Es, const double* Fout,
+                       const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* ce, void* lam,
+                       bool fp64, cudaStream_t st);
+void launch_md_kick_drift(int natoms, double* pos, double* vel, const void* F, bool fp64, const double* minv, const int32_t* type,
+                          double dt, const double* R, const double* Ri, double* disp_ref, int32_t* maxdisp_flag, double half_skin2,
+                          int stage, cudaStream_t st);
+void launch_md_ke(int natoms, const double* vel, const double* mass, const int32_t* type, double* ke, cudaStream_t st);
+void configure_kernels();
+}
+
+using namespace ann;
+
+static std::mutex g_err_mu;
+static std::string g_err;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t b) {
+        if (b <= bytes && p) return;
+        if (p) cudaFree(p);
+        p = nullptr; bytes = 0;
+        const size_t want = std::max<size_t>(b, 256);
+        const cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) { p = nullptr; throw ann_error(ANN_ERR_CUDA, std::string("cudaMalloc(") + std::to_string(want) + "): " + cudaGetErrorString(e)); }
+        bytes = want;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+    template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+template <typename real>
+struct ParamSet {
+    DevBuf rs, reta, aeta, zeta, alam, agrp, slot2ref, w, wt, b, inpw, inpb;
+    DevParams<real> view() const {
+        DevParams<real> d;
+        d.rs = rs.as<real>(); d.reta = reta.as<real>(); d.aeta = aeta.as<real>(); d.zeta = zeta.as<real>(); d.alam = alam.as<real>();
+        d.agrp = agrp.as<int32_t>(); d.slot2ref = slot2ref.as<int32_t>();
+        d.w = w.as<real>(); d.wt = wt.as<real>(); d.b = b.as<real>(); d.inpw = inpw.as<real>(); d.inpb = inpb.as<real>();
+        return d;
+    }
+    void release() { for (DevBuf* x : {&rs, &reta, &aeta, &zeta, &alam, &agrp, &slot2ref, &w, &wt, &b, &inpw, &inpb}) x->release(); }
+};
+
+template <typename real> static DevParams<real> params_of(ParamSet<float>& f, ParamSet<double>& d);
+template <> DevParams<float> params_of<float>(ParamSet<float>& f, ParamSet<double>&) { return f.view(); }
+template <> DevParams<double> params_of<double>(ParamSet<float>&, ParamSet<double>& d) { return d.view(); }
+
+static void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw ann_error(ANN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename real>
+static void upload_vec(DevBuf& b, const std::vector<double>& v, cudaStream_t st) {
+    std::vector<real> h(v.begin(), v.end());
+    b.ensure(h.size() * sizeof(real));
+    ck(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(real), cudaMemcpyHostToDevice, st), "upload params");
+    ck(cudaStreamSynchronize(st), "upload params");
+}
+static void upload_ints(DevBuf& b, const std::vector<int>& v, cudaStream_t st) {
+    b.ensure(v.size() * sizeof(int32_t));
+    ck(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st), "upload params");
+    ck(cudaStreamSynchronize(st), "upload params");
+}
+
+struct GraphKey {
+    int S, N, cap, prec, forces, nbins;
+    bool operator==(const GraphKey& o) const { return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins; }
+};
+
+struct ann_ctx {
+    ann_options opt;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool have_pot = false;
+    Potential pot;
+    PlanHost plan;
+    ParamSet<float> pf;
+    ParamSet<double> pd;
+    DevBuf poff;
+    // batch
+    int S = 0, N = 0;
+    bool have_batch = false;
+    std::vector<int32_t> off_h, sid_h;
+    DevBuf off, cell, pos, type, sid;
+    // neighbour list
+    int cap = 0, nbins_cap = 0;
+    DevBuf geo, pos4, abin, abc, am, aslot, bcount, bstart, bidx, bm, bpos4, bposd, nbins_total, nn, ntc, nj, nimg, nr, scan_tmp, counter, status;
+    // per atom / structure
+    DevBuf G, dEdG, Eatom, F, W, Es, Ws, Fout, tcount, tstart, tlist;
+    int last_prec = -1;
+    bool have_results = false, have_forces = false;
+    // graphs
+    cudaGraphExec_t gexec = nullptr;
+    GraphKey gkey{-1, -1, -1, -1, -1, -1};
+    // training
+    DevBuf Eref, Fref, loss3, ce, lam, U, grad;
+    bool have_train = false;
+    int train_prec = 0;
+    double train_wE = 0, train_wF = 0;
+    // MD
+    bool md_ready = false;
+    int md_prec = 0;
+    double md_dt = 0, md_skin = 0;
+    DevBuf vel, minv, mass, disp_ref, mdflag, ke;
+    std::vector<double> md_mass_t;
+    double md_R[9], md_Ri[9];
+    DevBuf md_R_d, md_Ri_d;
+    int md_rebuilds = 0;
+    // instrumentation
+    int64_t kernels = 0;            // kernels launched (graph replays add graph_kernels)
+    int64_t graph_kernels = 0;
+    bool profile = false;
+    cudaEvent_t ev[16] = {};
+};
+
+namespace ann { extern thread_local int64_t g_launch_counter; }
+
+static int fail(ann_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    std::lock_guard<std::mutex> g(g_err_mu);
+    g_err = m;
+    return code;
+}
+#define ANN_TRY(ctx, ...)                                                                 \
+    try { __VA_ARGS__; return ANN_OK; }                                                   \
+    catch (ann_error& e) { return fail(ctx, e.code, e.what()); }                          \
+    catch (std::exception& e) { return fail(ctx, ANN_ERR_ARG, e.what()); }
+
+static void set_device(ann_ctx* c) { ck(cudaSetDevice(c->opt.device), "cudaSetDevice"); }
+
+// ---------------------------------------------------------------- potential upload
+template <typename real>
+static void upload_params(ann_ctx* c, ParamSet<real>& P) {
+    const PlanHost& h = c->plan;
+    upload_vec<real>(P.rs, h.rs, c->stream); upload_vec<real>(P.reta, h.reta, c->stream);
+    upload_vec<real>(P.aeta, h.aeta, c->stream); upload_vec<real>(P.zeta, h.zeta, c->stream); upload_vec<real>(P.alam, h.alam, c->stream);
+    upload_ints(P.agrp, h.agrp, c->stream); upload_ints(P.slot2ref, h.slot2ref, c->stream);
+    upload_vec<real>(P.w, h.w, c->stream); upload_vec<real>(P.wt, h.wt, c->stream); upload_vec<real>(P.b, h.b, c->stream);
+    upload_vec<real>(P.inpw, h.inpw, c->stream); upload_vec<real>(P.inpb, h.inpb, c->stream);
+}
+static void reset_graph(ann_ctx* c) {
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    c->gkey = GraphKey{-1, -1, -1, -1, -1, -1};
+}
+static void rebuild_plan(ann_ctx* c) {
+    build_plan(c->pot, c->plan);
+    upload_params<float>(c, c->pf);
+    upload_params<double>(c, c->pd);
+    std::vector<int> po;
+    int64_t acc = 0;
+    for (auto& s : c->pot.sp) { po.push_back((int)acc); acc += s.nn.size(); }
+    upload_ints(c->poff, po, c->stream);
+    c->have_pot = true;
+    c->have_results = false;
+    c->have_train = false;
+    reset_graph(c);
+}
+
+// ---------------------------------------------------------------- batch buffers
+static int estimate_cap(ann_ctx* c, const double* cell) {
+    if (c->opt.max_neighbors > 0) return ((c->opt.max_neighbors + 31) / 32) * 32;
+    double rho_max = 0.0;
+    if (cell) {
+        for (int s = 0; s < c->S; ++s) {
+            const double* R = cell + 9 * s;
+            const double det = R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]);
+            const int n = c->off_h[s + 1] - c->off_h[s];
+            if (std::fabs(det) > 0) rho_max = std::max(rho_max, n / std::fabs(det));
+        }
+    }
+    if (rho_max <= 0) rho_max = 0.1;
+    const double rc = c->pot.rc + (c->md_ready ? c->md_skin : 0.0);
+    const double est = rho_max * 4.18879 * rc * rc * rc;
+    int cap = (int)(est * 1.5 + 32);
+    return std::min(((cap + 31) / 32) * 32, 4096);
+}
+static void ensure_batch_buffers(ann_ctx* c) {
+    const int S = c->S, N = std::max(c->N, 1), T = c->pot.ntypes(), imax = c->pot.max_input();
+    const size_t rb = sizeof(double);  // sized for the widest precision
+    c->off.ensure(sizeof(int32_t) * (S + 1)); c->cell.ensure(sizeof(double) * 9 * std::max(S, 1));
+    c->pos.ensure(sizeof(double) * 3 * N); c->type.ensure(sizeof(int32_t) * N); c->sid.ensure(sizeof(int32_t) * N);
+    c->geo.ensure(sizeof(StrucGeo) * std::max(S, 1));
+    c->nbins_cap = 2 * N + S + 2;
+    c->pos4.ensure(sizeof(float4) * N); c->abin.ensure(4 * N); c->abc.ensure(4 * N); c->am.ensure(4 * N); c->aslot.ensure(4 * N);
+    c->bcount.ensure(4 * (size_t)(c->nbins_cap + 1)); c->bstart.ensure(4 * (size_t)(c->nbins_cap + 1));
+    c->bidx.ensure(4 * N); c->bm.ensure(4 * N); c->bpos4.ensure(sizeof(float4) * N); c->bposd.ensure(sizeof(double) * 3 * N);
+    c->nbins_total.ensure(4); c->nn.ensure(4 * N); c->ntc.ensure(4 * (size_t)N * T);
+    c->nj.ensure(4 * (size_t)N * c->cap); c->nimg.ensure(4 * (size_t)N * c->cap); c->nr.ensure(sizeof(Vec4d) * (size_t)N * c->cap);
+    c->scan_tmp.ensure(4 * scan_tmp_ints(c->nbins_cap + 1)); c->counter.ensure(16); c->status.ensure(4 * 8);
+    c->G.ensure(rb * (size_t)N * std::max(imax, 1)); c->dEdG.ensure(rb * (size_t)N * std::max(imax, 1));
+    c->Eatom.ensure(sizeof(double) * N); c->F.ensure(rb * 3 * (size_t)N); c->W.ensure(rb * 9 * (size_t)N);
+    c->Es.ensure(sizeof(double) * std::max(S, 1)); c->Ws.ensure(sizeof(double) * 9 * std::max(S, 1)); c->Fout.ensure(sizeof(double) * 3 * (size_t)N);
+    c->tcount.ensure(4 * ((size_t)T + 1 + N)); c->tstart.ensure(4 * ((size_t)T + 1)); c->tlist.ensure(4 * (size_t)N);
+}
+
+static void stage_offsets(ann_ctx* c, int nstruc, const int64_t* atom_offsets) {
+    if (nstruc < 0) throw ann_error(ANN_ERR_ARG, "nstruc must be >= 0");
+    if (!atom_offsets) throw ann_error(ANN_ERR_ARG, "atom_offsets is NULL");
+    if (atom_offsets[0] != 0) throw ann_error(ANN_ERR_ARG, "atom_offsets[0] must be 0");
+    for (int s = 0; s < nstruc; ++s)
+        if (atom_offsets[s + 1] < atom_offsets[s]) throw ann_error(ANN_ERR_ARG, "atom_offsets must be non-decreasing");
+    if (atom_offsets[nstruc] > (int64_t)1 << 30) throw ann_error(ANN_ERR_ARG, "too many atoms in one batch (max 2^30)");
+    c->S = nstruc;
+    c->N = (int)atom_offsets[nstruc];
+    c->off_h.assign(nstruc + 1, 0);
+    c->sid_h.assign(c->N, 0);
+    for (int s = 0; s <= nstruc; ++s) c->off_h[s] = (int32_t)atom_offsets[s];
+    for (int s = 0; s < nstruc; ++s) for (int i = c->off_h[s]; i < c->off_h[s + 1]; ++i) c->sid_h[i] = s;
+}
+
+static void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell, bool device_src) {
+    if (!c->have_pot) throw ann_error(ANN_ERR_STATE, "no potential loaded");
+    stage_offsets(c, nstruc, offs);
+    if (c->N > 0 && (!posn || !type)) throw ann_error(ANN_ERR_ARG, "posn/type is NULL");
+    if (nstruc > 0 && !cell) throw ann_error(ANN_ERR_ARG, "cell is NULL");
+    if (!device_src) {
+        for (int i = 0; i < c->N; ++i) if (type[i] < 0 || type[i] >= c->pot.ntypes()) throw ann_error(ANN_ERR_ARG, "type index out of range at atom " + std::to_string(i));
+        for (int64_t k = 0; k < 3 * (int64_t)c->N; ++k) if (!std::isfinite(posn[k])) throw ann_error(ANN_ERR_NUMERIC, "non-finite position");
+        for (int64_t k = 0; k < 9 * (int64_t)nstruc; ++k) if (!std::isfinite(cell[k])) throw ann_error(ANN_ERR_NUMERIC, "non-finite cell");
+        for (int s = 0; s < nstruc; ++s) {
+            const double* R = cell + 9 * s;
+            const double det = R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]);
+            if (!(std::fabs(det) > 0)) throw ann_error(ANN_ERR_ARG, "singular cell of structure " + std::to_string(s));
+        }
+    }
+    if (c->cap == 0) c->cap = estimate_cap(c, device_src ? nullptr : cell);
+    ensure_batch_buffers(c);
+    const cudaMemcpyKind k = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    ck(cudaMemcpyAsync(c->off.p, c->off_h.data(), 4 * (c->S + 1), cudaMemcpyHostToDevice, c->stream), "H2D offsets");
+    if (c->N > 0) {
+        ck(cudaMemcpyAsync(c->sid.p, c->sid_h.data(), 4 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D sid");
+        ck(cudaMemcpyAsync(c->pos.p, posn, sizeof(double) * 3 * (size_t)c->N, k, c->stream), "copy positions");
+        ck(cudaMemcpyAsync(c->type.p, type, sizeof(int32_t) * (size_t)c->N, k, c->stream), "copy types");
+    }
+    if (c->S > 0) ck(cudaMemcpyAsync(c->cell.p, cell, sizeof(double) * 9 * (size_t)c->S, k, c->stream), "copy cells");
+    c->have_batch = true;
+    c->have_results = false;
+}
+
+// ---------------------------------------------------------------- the E+F kernel sequence
+template <typename real>
+static BpArgs<real> bp_args(ann_ctx* c) {
+    BpArgs<real> b{};
+    b.natoms = c->N; b.ntypes = c->pot.ntypes(); b.cap = c->cap; b.newton_untranslated = (c->opt.newton == ANN_NEWTON_UNTRANSLATED);
+    b.type = c->type.as<int32_t>(); b.nn = c->nn.as<int32_t>(); b.ntc = c->ntc.as<int32_t>(); b.nj = c->nj.as<int32_t>(); b.nimg = c->nimg.as<int32_t>();
+    b.nr = c->nr.p; b.G = c->G.as<real>(); b.dEdG = c->dEdG.as<real>(); b.F = c->F.as<real>(); b.W = c->W.as<real>();
+    b.lam = c->lam.as<real>(); b.U = c->U.as<real>();
+    b.counter = c->counter.as<uint32_t>(); b.status = c->status.as<int32_t>();
+    return b;
+}
+static NbrArgs nbr_args(ann_ctx* c, double rc) {
+    NbrArgs a{};
+    a.nstruc = c->S; a.natoms = c->N; a.ntypes = c->pot.ntypes(); a.cap = c->cap; a.rc = rc;
+    a.off = c->off.as<int32_t>(); a.cell = c->cell.as<double>(); a.pos = c->pos.as<double>(); a.type = c->type.as<int32_t>(); a.sid = c->sid.as<int32_t>();
+    a.geo = c->geo.as<StrucGeo>(); a.pos4 = c->pos4.as<float4>(); a.abin = c->abin.as<int32_t>(); a.abc = c->abc.as<int32_t>(); a.am = c->am.as<int32_t>();
+    a.aslot = c->aslot.as<int32_t>(); a.bcount = c->bcount.as<int32_t>(); a.bstart = c->bstart.as<int32_t>(); a.bidx = c->bidx.as<int32_t>();
+    a.bm = c->bm.as<int32_t>(); a.bpos4 = c->bpos4.as<float4>(); a.bposd = c->bposd.as<double>(); a.nbins_cap = c->nbins_cap;
+    a.nbins_total = c->nbins_total.as<int32_t>(); a.nn = c->nn.as<int32_t>(); a.ntc = c->ntc.as<int32_t>(); a.nj = c->nj.as<int32_t>();
+    a.nimg = c->nimg.as<int32_t>(); a.nr = c->nr.p; a.scan_tmp = c->scan_tmp.as<int32_t>(); a.counter = c->counter.as<uint32_t>();
+    a.status = c->status.as<int32_t>();
+    return a;
+}
+
+static void mark(ann_ctx* c, int k) {
+    if (!c->profile) return;
+    if (!c->ev[k]) cudaEventCreate(&c->ev[k]);
+    cudaEventRecord(c->ev[k], c->stream);
+}
+
+template <typename real>
+static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
+    cudaStream_t st = c->stream;
+    const bool fp64 = std::is_same<real, double>::value;
+    const DevPot& pot = c->plan.pot;
+    mark(c, 0);
+    if (build_list) launch_neighbors(nbr_args(c, c->pot.rc + (c->md_ready ? c->md_skin : 0.0)), fp64, st);
+    else launch_refresh_geometry(nbr_args(c, c->pot.rc + c->md_skin), fp64, st);
+    mark(c, 1);
+    launch_type_lists(c->N, c->pot.ntypes(), c->type.as<int32_t>(), c->tcount.as<int32_t>(), c->tstart.as<int32_t>(), c->tlist.as<int32_t>(),
+                      c->status.as<int32_t>(), st);
+    mark(c, 2);
+    BpArgs<real> b = bp_args<real>(c);
+    b.prm = params_of<real>(c->pf, c->pd);
+    launch_symm<real>(pot, b, st);
+    mark(c, 3);
+    MlpArgs<real> m{};
+    m.natoms = c->N; m.ntypes = c->pot.ntypes(); m.imax = pot.imax;
+    m.tstart = c->tstart.as<int32_t>(); m.tlist = c->tlist.as<int32_t>();
+    m.G = c->G.as<real>(); m.dEdG = c->dEdG.as<real>(); m.Eatom = c->Eatom.as<double>();
+    m.prm = b.prm;
+    launch_mlp_forward_backward<real>(pot, m, st);
+    mark(c, 4);
+    if (forces) {
+        cudaMemsetAsync(c->F.p, 0, sizeof(real) * 3 * (size_t)std::max(c->N, 1), st);
+        launch_force<real>(pot, b, st);
+    }
+    mark(c, 5);
+    launch_reduce_structures<real>(c->S, c->off.as<int32_t>(), c->Eatom.as<double>(), forces ? c->W.as<real>() : nullptr,
+                                   c->F.as<real>(), c->Es.as<double>(), c->Ws.as<double>(), forces ? c->Fout.as<double>() : nullptr, st);
+    mark(c, 6);
+}
+
+static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true) {
+    if (!c->have_batch) throw ann_error(ANN_ERR_STATE, "no batch staged");
+    if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
+    ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
+    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap};
+    const bool graphs = c->opt.use_graphs && build_list && c->N > 0 && !c->profile;
+    if (graphs) {
+        if (!(c->gexec && c->gkey == key)) {
+            reset_graph(c);
+            cudaGraph_t g = nullptr;
+            const int64_t before = g_launch_counter;
+            ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+            if (prec == ANN_FP64) enqueue_ef<double>(c, forces, true); else enqueue_ef<float>(c, forces, true);
+            ck(cudaStreamEndCapture(c->stream, &g), "end capture");
+            c->graph_kernels = g_launch_counter - before;
+            ck(cudaGraphInstantiate(&c->gexec, g, 0), "graph instantiate");
+            cudaGraphDestroy(g);
+            c->gkey = key;
+        }
+        ck(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+        c->kernels += c->graph_kernels;
+    } else {
+        const int64_t before = g_launch_counter;
+        if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
+        c->kernels += g_launch_counter - before;
+    }
+    ck(cudaGetLastError(), "kernel launch");
+    c->last_prec = prec;
+    c->have_results = true;
+    c->have_forces = forces;
+}
+
+// wait for the batch; on neighbour overflow grow the capacity and recompute
+static void finish_batch(ann_ctx* c) {
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        int32_t st[8];
+        ck(cudaMemcpyAsync(st, c->status.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream), "D2H status");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+        if (st[0] == 0) return;
+        if (st[0] & ST_BAD_TYPE) throw ann_error(ANN_ERR_ARG, "type index out of range");
+        if (st[0] & ST_NONFINITE) throw ann_error(ANN_ERR_NUMERIC, "non-finite position or singular cell");
+        if (st[0] & ST_IMAGE_RANGE) throw ann_error(ANN_ERR_ARG, "an atom lies more than 500 cell lengths outside its cell");
+        if (st[0] & ST_TIMEOUT) throw ann_error(ANN_ERR_TIMEOUT, "a bounded device wait gave up");
+        if (st[0] & ST_NBR_OVERFLOW) {
+            const int need = std::max(st[1], c->cap + 1);
+            const int ncap = ((int)(need * 1.25) + 31) / 32 * 32;
+            if (ncap > 8192) throw ann_error(ANN_ERR_CAPACITY, "more than 8192 neighbours per atom");
+            c->cap = ncap;
+            ensure_batch_buffers(c);
+            reset_graph(c);
+            run_batch(c, c->last_prec, c->have_forces);
+            continue;
+        }
+        throw ann_error(ANN_ERR_CUDA, "unknown device status " + std::to_string(st[0]));
+    }
+    throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity could not be grown");
+}
+
+// ---------------------------------------------------------------- extern "C"
+extern "C" {
+
+void ann_default_options(ann_options* o) {
+    if (!o) return;
+    o->device = 0; o->precision = ANN_MIXED; o->newton = ANN_NEWTON_ALL_IMAGES; o->max_neighbors = 0; o->use_graphs = 1; o->mlp_backend = 0;
+}
+int ann_abi_version(void) { return ANN_GPU_ABI_VERSION; }
+
+int ann_create(ann_ctx** out, const ann_options* opt) {
+    if (!out) return fail(nullptr, ANN_ERR_ARG, "ctx pointer is NULL");
+    *out = nullptr;
+    ann_ctx* c = new ann_ctx();
+    ann_default_options(&c->opt);
+    if (opt) c->opt = *opt;
+    try {
+        int n = 0;
+        ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        if (c->opt.device < 0 || c->opt.device >= n) throw ann_error(ANN_ERR_CUDA, "CUDA device " + std::to_string(c->opt.device) + " not available");
+        set_device(c);
+        ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream create");
+        configure_kernels();
+    } catch (ann_error& e) {
+        delete c;
+        return fail(nullptr, e.code, e.what());
+    }
+    *out = c;
+    return ANN_OK;
+}
+
+int ann_destroy(ann_ctx* c) {
+    if (!c) return ANN_OK;
+    cudaSetDevice(c->opt.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    reset_graph(c);
+    c->pf.release(); c->pd.release();
+    for (DevBuf* b : {&c->poff, &c->off, &c->cell, &c->pos, &c->type, &c->sid, &c->geo, &c->pos4, &c->abin, &c->abc, &c->am, &c->aslot,
+                      &c->bcount, &c->bstart, &c->bidx, &c->bm, &c->bpos4, &c->bposd, &c->nbins_total, &c->nn, &c->ntc, &c->nj, &c->nimg,
+                      &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
+                      &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
+                      &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d})
+        b->release();
+    for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return ANN_OK;
+}
+
+const char* ann_last_error(const ann_ctx* c) {
+    if (c) return c->err.c_str();
+    std::lock_guard<std::mutex> g(g_err_mu);
+    return g_err.c_str();
+}
+
+int ann_load_potential_text(ann_ctx* c, const char* text) {
+    if (!c || !text) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        Potential p;
+        p.read_text(text);
+        p.validate();
+        c->pot = p;
+        rebuild_plan(c);
+    })
+}
+int ann_load_potential(ann_ctx* c, const char* path) {
+    if (!c || !path) return fail(c, ANN_ERR_ARG, "NULL argument");
+    std::ifstream f(path);
+    if (!f) return fail(c, ANN_ERR_IO, std::string("could not open potential file: \"") + path + "\"");
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ann_load_potential_text(c, ss.str().c_str());
+}
+int ann_write_potential(ann_ctx* c, const char* path) {
+    if (!c || !path) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    std::ofstream f(path);
+    if (!f) return fail(c, ANN_ERR_IO, std::string("could not write potential file: \"") + path + "\"");
+    f << c->pot.write_text();
+    return f.good() ? ANN_OK : fail(c, ANN_ERR_IO, "write failed");
+}
+int ann_num_types(ann_ctx* c, int32_t* n) {
+    if (!c || !n) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    *n = c->pot.ntypes();
+    return ANN_OK;
+}
+int ann_type_index(ann_ctx* c, const char* name, int32_t* idx) {
+    if (!c || !name || !idx) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    auto it = c->pot.index.find(name);
+    if (it == c->pot.index.end()) return fail(c, ANN_ERR_ARG, std::string("unknown type name: ") + name);
+    *idx = it->second;
+    return ANN_OK;
+}
+int ann_type_name(ann_ctx* c, int32_t i, char* buf, int32_t len) {
+    if (!c || !buf || len <= 0) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (i < 0 || i >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    std::snprintf(buf, len, "%s", c->pot.sp[i].name.c_str());
+    return ANN_OK;
+}
+int ann_cutoff(ann_ctx* c, double* rc) {
+    if (!c || !rc) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    *rc = c->pot.rc;
+    return ANN_OK;
+}
+int ann_num_inputs(ann_ctx* c, int32_t t, int32_t* n) {
+    if (!c || !n) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    *n = c->pot.sp[t].nInput;
+    return ANN_OK;
+}
+int ann_num_params(ann_ctx* c, int64_t* n) {
+    if (!c || !n) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    *n = c->pot.nparams();
+    return ANN_OK;
+}
+int ann_get_params(ann_ctx* c, double* p, int64_t n) {
+    if (!c || !p) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (n != c->pot.nparams()) return fail(c, ANN_ERR_ARG, "parameter count mismatch");
+    c->pot.get_params(p);
+    return ANN_OK;
+}
+int ann_set_params(ann_ctx* c, const double* p, int64_t n) {
+    if (!c || !p) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (n != c->pot.nparams()) return fail(c, ANN_ERR_ARG, "Invalid size: vector and network mismatch.");  // nn.cpp:869
+    ANN_TRY(c, { set_device(c); c->pot.set_params(p); rebuild_plan(c); })
+}
+int ann_set_input_scaling(ann_ctx* c, int32_t t, const double* w, const double* b, int32_t n) {
+    if (!c || !w || !b) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    if (n != c->pot.sp[t].nInput) return fail(c, ANN_ERR_ARG, "input count mismatch");
+    ANN_TRY(c, {
+        set_device(c);
+        c->pot.sp[t].nn.inpw.assign(w, w + n);
+        c->pot.sp[t].nn.inpb.assign(b, b + n);
+        rebuild_plan(c);
+    })
+}
+int ann_init_network(ann_ctx* c, int32_t t, int32_t seed, int32_t dist, int32_t init, double sb, double sw) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    ANN_TRY(c, { set_device(c); init_network(c->pot.sp[t].nn, seed, dist, init, sb, sw); rebuild_plan(c); })
+}
+
+int ann_batch_upload(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, { set_device(c); upload_batch(c, nstruc, offs, posn, type, cell, false); })
+}
+int ann_batch_set_device(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* d_posn, const int32_t* d_type, const double* d_cell) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, { set_device(c); upload_batch(c, nstruc, offs, d_posn, d_type, d_cell, true); })
+}
+int ann_batch_compute(ann_ctx* c, int32_t prec, int32_t want_forces) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, { set_device(c); run_batch(c, prec, want_forces != 0); })
+}
+int ann_batch_download(ann_ctx* c, double* energy, double* forces, double* virial) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        if ((forces || virial) && !c->have_forces) throw ann_error(ANN_ERR_STATE, "forces were not computed for this batch");
+        if (energy && c->S > 0) ck(cudaMemcpyAsync(energy, c->Es.p, sizeof(double) * c->S, cudaMemcpyDeviceToHost, c->stream), "D2H energy");
+        if (forces && c->N > 0) ck(cudaMemcpyAsync(forces, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream), "D2H forces");
+        if (virial && c->S > 0) ck(cudaMemcpyAsync(virial, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, cudaMemcpyDeviceToHost, c->stream), "D2H virial");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+    })
+}
+int ann_batch_results_device(ann_ctx* c, double* e, double* f, double* w) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        if (e && c->S > 0) ck(cudaMemcpyAsync(e, c->Es.p, sizeof(double) * c->S, cudaMemcpyDeviceToDevice, c->stream), "D2D energy");
+        if (f && c->N > 0) ck(cudaMemcpyAsync(f, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToDevice, c->stream), "D2D forces");
+        if (w && c->S > 0) ck(cudaMemcpyAsync(w, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, cudaMemcpyDeviceToDevice, c->stream), "D2D virial");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+    })
+}
+int ann_kernel_count(ann_ctx* c, int64_t* n) {
+    if (!c || !n) return fail(c, ANN_ERR_ARG, "NULL argument");
+    *n = c->kernels;
+    return ANN_OK;
+}
+int ann_profile_phases(ann_ctx* c, int32_t enable) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    c->profile = enable != 0;
+    return ANN_OK;
+}
+int ann_phase_times(ann_ctx* c, double* ms, int32_t n) {
+    if (!c || !ms) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->profile || !c->ev[6]) throw ann_error(ANN_ERR_STATE, "enable ann_profile_phases and run a batch first");
+        ck(cudaEventSynchronize(c->ev[6]), "event sync");
+        for (int k = 0; k < n && k < 6; ++k) {
+            float t = 0.f;
+            ck(cudaEventElapsedTime(&t, c->ev[k], c->ev[k + 1]), "event elapsed");
+            ms[k] = t;
+        }
+    })
+}
+int ann_synchronize(ann_ctx* c) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, { set_device(c); ck(cudaStreamSynchronize(c->stream), "synchronize"); })
+}
+void* ann_stream(ann_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int ann_compute(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell,
+                double* energy, double* forces, double* virial, int32_t prec) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (!energy) return fail(c, ANN_ERR_ARG, "energy is NULL");
+    ANN_TRY(c, {
+        set_device(c);
+        upload_batch(c, nstruc, offs, posn, type, cell, false);
+        run_batch(c, prec, forces != nullptr || virial != nullptr);
+        finish_batch(c);
+        if (c->S > 0) ck(cudaMemcpyAsync(energy, c->Es.p, sizeof(double) * c->S, cudaMemcpyDeviceToHost, c->stream), "D2H energy");
+        if (forces && c->N > 0) ck(cudaMemcpyAsync(forces, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream), "D2H forces");
+        if (virial && c->S > 0) ck(cudaMemcpyAsync(virial, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, cudaMemcpyDeviceToHost, c->stream), "D2H virial");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+    })
+}
+
+// ---- inspection
+int ann_symm_width(ann_ctx* c, int32_t* w) {
+    if (!c || !w) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    *w = c->pot.max_input();
+    return ANN_OK;
+}
+static void download_real_rows(ann_ctx* c, DevBuf& b, double* out, size_t n) {
+    if (c->last_prec == ANN_FP64) {
+        ck(cudaMemcpyAsync(out, b.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream), "D2H");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+    } else {
+        std::vector<float> h(n);
+        ck(cudaMemcpyAsync(h.data(), b.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream), "D2H");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+        for (size_t k = 0; k < n; ++k) out[k] = h[k];
+    }
+}
+int ann_get_symm(ann_ctx* c, double* G) {
+    if (!c || !G) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        download_real_rows(c, c->G, G, (size_t)c->N * c->pot.max_input());
+    })
+}
+int ann_get_dedg(ann_ctx* c, double* d) {
+    if (!c || !d) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        download_real_rows(c, c->dEdG, d, (size_t)c->N * c->pot.max_input());
+    })
+}
+int ann_get_atom_energies(ann_ctx* c, double* e) {
+    if (!c || !e) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        if (c->N > 0) ck(cudaMemcpy(e, c->Eatom.p, sizeof(double) * c->N, cudaMemcpyDeviceToHost), "D2H");
+    })
+}
+int ann_num_neighbors(ann_ctx* c, int64_t* total) {
+    if (!c || !total) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        std::vector<int32_t> nn(c->N);
+        if (c->N > 0) ck(cudaMemcpy(nn.data(), c->nn.p, 4 * (size_t)c->N, cudaMemcpyDeviceToHost), "D2H");
+        int64_t t = 0;
+        for (int v : nn) t += v;
+        *total = t;
+    })
+}
+int ann_get_neighbors(ann_ctx* c, int32_t* iout, int32_t* jout, int32_t* img, double* r, int64_t capn) {
+    if (!c || !iout || !jout || !img) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);
+        const size_t N = c->N, cap = c->cap;
+        std::vector<int32_t> nn(N), nj(N * cap), ni(N * cap);
+        if (N > 0) {
+            ck(cudaMemcpy(nn.data(), c->nn.p, 4 * N, cudaMemcpyDeviceToHost), "D2H");
+            ck(cudaMemcpy(nj.data(), c->nj.p, 4 * N * cap, cudaMemcpyDeviceToHost), "D2H");
+            ck(cudaMemcpy(ni.data(), c->nimg.p, 4 * N * cap, cudaMemcpyDeviceToHost), "D2H");
+        }
+        std::vector<Vec4d> rr;
+        if (r) {
+            if (c->last_prec != ANN_FP64) throw ann_error(ANN_ERR_STATE, "pair vectors are only kept in FP64 for FP64 batches");
+            rr.resize(N * cap);
+            if (N > 0) ck(cudaMemcpy(rr.data(), c->nr.p, sizeof(Vec4d) * N * cap, cudaMemcpyDeviceToHost), "D2H");
+        }
+        int64_t k = 0;
+        for (size_t i = 0; i < N; ++i)
+            for (int e = 0; e < nn[i]; ++e) {
+                if (k >= capn) throw ann_error(ANN_ERR_CAPACITY, "output arrays too small");
+                const int32_t p = ni[i * cap + e];
+                iout[k] = (int32_t)i; jout[k] = nj[i * cap + e];
+                img[3 * k] = ((int32_t)((uint32_t)p << 22)) >> 22;
+                img[3 * k + 1] = ((int32_t)((uint32_t)p << 12)) >> 22;
+                img[3 * k + 2] = ((int32_t)((uint32_t)p << 2)) >> 22;
+                if (r) { const Vec4d& v = rr[i * cap + e]; r[3 * k] = v.x; r[3 * k + 1] = v.y; r[3 * k + 2] = v.z; }
+                ++k;
+            }
+    })
+}
+
+// ---- training
+int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell,
+                      const double* Eref, const double* Fref, double wE, double wF, int32_t prec, double* loss3) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (!Eref || !Fref || !loss3) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        upload_batch(c, nstruc, offs, posn, type, cell, false);
+        run_batch(c, prec, true);
+        finish_batch(c);
+        const size_t N = std::max(c->N, 1), S = std::max(c->S, 1), rb = (prec == ANN_FP64) ? 8 : 4;
+        c->Eref.ensure(8 * S); c->Fref.ensure(8 * 3 * N); c->loss3.ensure(8 * 4); c->ce.ensure(8 * N);
+        c->lam.ensure(rb * 3 * N); c->U.ensure(rb * N * std::max(c->pot.max_input(), 1));
+        if (c->S > 0) ck(cudaMemcpyAsync(c->Eref.p, Eref, 8 * (size_t)c->S, cudaMemcpyHostToDevice, c->stream), "H2D Eref");
+        if (c->N > 0) ck(cudaMemcpyAsync(c->Fref.p, Fref, 8 * 3 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D Fref");
+        ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
+        launch_train_loss(c->S, c->N, c->off.as<int32_t>(), c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
+                          c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->loss3.as<double>(), c->ce.as<double>(), c->lam.p,
+                          prec == ANN_FP64, c->stream);
+        ck(cudaGetLastError(), "loss kernel");
+        ck(cudaMemcpyAsync(loss3, c->loss3.p, 8 * 3, cudaMemcpyDeviceToHost, c->stream), "D2H loss");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+        c->have_train = true; c->train_prec = prec; c->train_wE = wE; c->train_wF = wF;
+    })
+}
+int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
+    if (!c || !grad) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_train || !c->have_results) throw ann_error(ANN_ERR_STATE, "ann_train_backward needs a preceding ann_train_forward");
+        if (n != c->pot.nparams()) throw ann_error(ANN_ERR_ARG, "parameter count mismatch");
+        c->grad.ensure(8 * (size_t)std::max<int64_t>(n, 1));
+        ck(cudaMemsetAsync(c->grad.p, 0, 8 * (size_t)std::max<int64_t>(n, 1), c->stream), "memset grad");
+        const DevPot& pot = c->plan.pot;
+        auto go = [&](auto tag) {
+            using real = decltype(tag);
+            BpArgs<real> b = bp_args<real>(c);
+            b.prm = params_of<real>(c->pf, c->pd);
+            launch_jvp<real>(pot, b, c->stream);
+            MlpArgs<real> m{};
+            m.natoms = c->N; m.ntypes = c->pot.ntypes(); m.imax = pot.imax; m.tstart = c->tstart.as<int32_t>(); m.tlist = c->tlist.as<int32_t>();
+            m.G = c->G.as<real>(); m.U = c->U.as<real>(); m.ce = c->ce.as<double>(); m.ct = -1.0; m.grad = c->grad.as<double>();
+            m.poff = c->poff.as<int32_t>(); m.prm = b.prm;
+            launch_mlp_train_grad<real>(pot, m, c->stream);
+        };
+        if (c->train_prec == ANN_FP64) go(double()); else go(float());
+        ck(cudaGetLastError(), "backward kernels");
+        ck(cudaMemcpyAsync(grad, c->grad.p, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "D2H grad");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+        int32_t st[8];
+        ck(cudaMemcpy(st, c->status.p, sizeof(st), cudaMemcpyDeviceToHost), "D2H status");
+        if (st[0] != 0) throw ann_error(ANN_ERR_CUDA, "device status " + std::to_string(st[0]) + " in backward pass");
+        for (int64_t k = 0; k < n; ++k) grad[k] *= scale;
+    })
+}
+
+// ---- molecular dynamics
+static void inv3(const double* R, double* Ri) {
+    auto at = [&](int r, int c) { return R[3 * c + r]; };
+    const double det = at(0, 0) * (at(1, 1) * at(2, 2) - at(1, 2) * at(2, 1)) - at(0, 1) * (at(1, 0) * at(2, 2) - at(1, 2) * at(2, 0)) + at(0, 2) * (at(1, 0) * at(2, 1) - at(1, 1) * at(2, 0));
+    if (!(std::fabs(det) > 0)) throw ann_error(ANN_ERR_ARG, "singular cell");
+    const double id = 1.0 / det;
+    double m[3][3];
+    m[0][0] = (at(1, 1) * at(2, 2) - at(1, 2) * at(2, 1)) * id; m[0][1] = (at(0, 2) * at(2, 1) - at(0, 1) * at(2, 2)) * id; m[0][2] = (at(0, 1) * at(1, 2) - at(0, 2) * at(1, 1)) * id;
+    m[1][0] = (at(1, 2) * at(2, 0) - at(1, 0) * at(2, 2)) * id; m[1][1] = (at(0, 0) * at(2, 2) - at(0, 2) * at(2, 0)) * id; m[1][2] = (at(0, 2) * at(1, 0) - at(0, 0) * at(1, 2)) * id;
+    m[2][0] = (at(1, 0) * at(2, 1) - at(1, 1) * at(2, 0)) * id; m[2][1] = (at(0, 1) * at(2, 0) - at(0, 0) * at(2, 1)) * id; m[2][2] = (at(0, 0) * at(1, 1) - at(0, 1) * at(1, 0)) * id;
+    for (int r = 0; r < 3; ++r) for (int cc = 0; cc < 3; ++cc) Ri[3 * cc + r] = m[r][cc];
+}
+
+int ann_md_init(ann_ctx* c, int64_t natoms, const double* posn, const double* vel, const int32_t* type, const double* cell,
+                const double* mass_t, double dt, double skin, int32_t prec) {
+    if (!c || !posn || !vel || !type || !cell || !mass_t) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (dt <= 0 || skin < 0) throw ann_error(ANN_ERR_ARG, "invalid time step or skin");
+        c->md_ready = false;
+        const int64_t offs[2] = {0, natoms};
+        c->md_skin = skin; c->md_dt = dt; c->md_prec = prec;
+        c->md_ready = true;  // list cutoff rc + skin from here on
+        c->cap = 0;
+        upload_batch(c, 1, offs, posn, type, cell, false);
+        std::memcpy(c->md_R, cell, sizeof(c->md_R));
+        inv3(c->md_R, c->md_Ri);
+        c->md_R_d.ensure(72); c->md_Ri_d.ensure(72);
+        ck(cudaMemcpy(c->md_R_d.p, c->md_R, 72, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(c->md_Ri_d.p, c->md_Ri, 72, cudaMemcpyHostToDevice), "H2D");
+        const int T = c->pot.ntypes();
+        c->md_mass_t.assign(mass_t, mass_t + T);
+        std::vector<double> minv(T);
+        for (int t = 0; t < T; ++t) { if (!(mass_t[t] > 0)) throw ann_error(ANN_ERR_ARG, "masses must be positive"); minv[t] = 1.0 / (mass_t[t] * 103.642696526805); }
+        c->minv.ensure(8 * T); c->mass.ensure(8 * T);
+        ck(cudaMemcpy(c->minv.p, minv.data(), 8 * T, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(c->mass.p, mass_t, 8 * T, cudaMemcpyHostToDevice), "H2D");
+        c->vel.ensure(8 * 3 * (size_t)std::max<int64_t>(natoms, 1)); c->disp_ref.ensure(8 * 3 * (size_t)std::max<int64_t>(natoms, 1));
+        c->mdflag.ensure(16); c->ke.ensure(16);
+        ck(cudaMemcpy(c->vel.p, vel, 8 * 3 * (size_t)natoms, cudaMemcpyHostToDevice), "H2D");
+        // initial list + forces
+        run_batch(c, prec, true, true);
+        finish_batch(c);
+        ck(cudaMemcpy(c->disp_ref.p, c->pos.p, 8 * 3 * (size_t)natoms, cudaMemcpyDeviceToDevice), "D2D");
+        c->md_rebuilds = 0;
+    })
+}
+
+int ann_md_run(ann_ctx* c, int32_t nsteps, double* pe, double* ke, int32_t* rebuilds) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->md_ready) throw ann_error(ANN_ERR_STATE, "ann_md_init first");
+        const bool fp64 = c->md_prec == ANN_FP64;
+        const double half_skin2 = 0.25 * c->md_skin * c->md_skin;
+        int reb = 0;
+        for (int step = 0; step < nsteps; ++step) {
+            // first half kick + drift + wrap; flags an atom that moved more than skin/2 since the last build
+            ck(cudaMemsetAsync(c->mdflag.p, 0, 4, c->stream), "memset");
+            launch_md_kick_drift(c->N, c->pos.as<double>(), c->vel.as<double>(), c->F.p, fp64, c->minv.as<double>(), c->type.as<int32_t>(),
+                                 c->md_dt, c->md_R_d.as<double>(), c->md_Ri_d.as<double>(), c->disp_ref.as<double>(), c->mdflag.as<int32_t>(),
+                                 half_skin2, 0, c->stream);
+            int32_t flag = 0;
+            ck(cudaMemcpyAsync(&flag, c->mdflag.p, 4, cudaMemcpyDeviceToHost, c->stream), "D2H flag");
+            ck(cudaStreamSynchronize(c->stream), "synchronize");
+            const bool rebuild = flag != 0;
+            if (rebuild) {  // wrap into the cell (Cell::returnToCell) only when the list is rebuilt
+                ++reb;
+                launch_md_kick_drift(c->N, c->pos.as<double>(), c->vel.as<double>(), c->F.p, fp64, c->minv.as<double>(), c->type.as<int32_t>(),
+                                     c->md_dt, c->md_R_d.as<double>(), c->md_Ri_d.as<double>(), c->disp_ref.as<double>(), c->mdflag.as<int32_t>(),
+                                     half_skin2, 2, c->stream);
+                ck(cudaMemcpyAsync(c->disp_ref.p, c->pos.p, 8 * 3 * (size_t)c->N, cudaMemcpyDeviceToDevice, c->stream), "D2D");
+            }
+            run_batch(c, c->md_prec, true, rebuild);
+            if (rebuild) finish_batch(c);
+            // second half kick
+            launch_md_kick_drift(c->N, c->pos.as<double>(), c->vel.as<double>(), c->F.p, fp64, c->minv.as<double>(), c->type.as<int32_t>(),
+                                 c->md_dt, c->md_R_d.as<double>(), c->md_Ri_d.as<double>(), c->disp_ref.as<double>(), c->mdflag.as<int32_t>(),
+                                 half_skin2, 1, c->stream);
+        }
+        finish_batch(c);
+        c->md_rebuilds += reb;
+        if (rebuilds) *rebuilds = reb;
+        if (pe) ck(cudaMemcpy(pe, c->Es.p, 8, cudaMemcpyDeviceToHost), "D2H pe");
+        if (ke) {
+            launch_md_ke(c->N, c->vel.as<double>(), c->mass.as<double>(), c->type.as<int32_t>(), c->ke.as<double>(), c->stream);
+            ck(cudaMemcpyAsync(ke, c->ke.p, 8, cudaMemcpyDeviceToHost, c->stream), "D2H ke");
+            ck(cudaStreamSynchronize(c->stream), "synchronize");
+        }
+    })
+}
+int ann_md_get_state(ann_ctx* c, double* posn, double* vel, double* forces) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->md_ready) throw ann_error(ANN_ERR_STATE, "ann_md_init first");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+        if (posn) ck(cudaMemcpy(posn, c->pos.p, 8 * 3 * (size_t)c->N, cudaMemcpyDeviceToHost), "D2H");
+        if (vel) ck(cudaMemcpy(vel, c->vel.p, 8 * 3 * (size_t)c->N, cudaMemcpyDeviceToHost), "D2H");
+        if (forces) ck(cudaMemcpy(forces, c->Fout.p, 8 * 3 * (size_t)c->N, cudaMemcpyDeviceToHost), "D2H");
+    })
+}
+
+}  // extern "C"

@@ -1,0 +1,118 @@
+// Kernel argument blocks and host-side launch wrappers of libann_gpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "plan.hpp"
+
+namespace ann {
+
+// kernels launched by this thread (instrumentation; graph captures count their kernel nodes)
+extern thread_local int64_t g_launch_counter;
+
+struct StrucGeo {          // per structure (FP64), filled on the device by k_struc_setup
+    double R[9];           // lattice matrix, column-major (R[3*c + r])
+    double Ri[9];          // inverse, column-major
+    int32_t nb[3];         // bins along each lattice direction
+    int32_t sten[3];       // stencil half-width in bins
+    int32_t bin0;          // first global bin of the structure
+    int32_t atom0, natoms;
+    int32_t pad;
+};
+
+// ---- neighbour list (neighbor.cu) ----------------------------------------------------------
+struct NbrArgs {
+    int32_t nstruc, natoms, ntypes, cap;
+    double rc;                       // list cutoff
+    const int32_t* off;              // [S+1]
+    const double* cell;              // [9S]
+    const double* pos;               // [3N] FP64 positions
+    const int32_t* type;             // [N]
+    const int32_t* sid;              // [N] structure of each atom
+    StrucGeo* geo;                   // [S]
+    float4* pos4;                    // [N] FP32 positions + type bits
+    int32_t* abin;                   // [N] global bin
+    int32_t* abc;                    // [N] packed bin coordinates
+    int32_t* am;                     // [N] packed wrap shift m (s = frac + m)
+    int32_t* aslot;                  // [N] slot inside the bin
+    int32_t* bcount;                 // [nbins_cap+1]
+    int32_t* bstart;                 // [nbins_cap+1]
+    int32_t* bidx;                   // [N] atoms in bin order
+    int32_t* bm;                     // [N] packed m in bin order
+    float4* bpos4;                   // [N] positions in bin order
+    double* bposd;                   // [3N] FP64 positions in bin order
+    int32_t nbins_cap;
+    int32_t* nbins_total;            // [1]
+    int32_t* nn;                     // [N] entries per atom
+    int32_t* ntc;                    // [N*T] entries per atom and neighbour type (type-sorted rows)
+    int32_t* nj;                     // [N*cap]
+    int32_t* nimg;                   // [N*cap] packed image n
+    void* nr;                        // [N*cap] real4 (rx, ry, rz, d)
+    int32_t* scan_tmp;               // scratch for the bin scan
+    uint32_t* counter;               // [1] work counter
+    int32_t* status;                 // [8]
+};
+void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st);
+// recompute nr from positions and stored images (Verlet-list refresh between rebuilds)
+void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st);
+
+// ---- symmetry functions / forces / tangents (bp.cu) ---------------------------------------
+template <typename real>
+struct BpArgs {
+    int32_t natoms, ntypes, cap, newton_untranslated;
+    const int32_t* type;
+    const int32_t* nn;
+    const int32_t* ntc;
+    const int32_t* nj;
+    const int32_t* nimg;
+    const void* nr;                  // real4 rows
+    real* G;                         // [N*imax] symmetry functions (symm pass)
+    const real* dEdG;                // [N*imax] (force pass)
+    real* F;                         // [3N] force accumulator (force pass)
+    real* W;                         // [9N] per-atom virial (force pass)
+    const real* lam;                 // [3N] tangent field (jvp pass)
+    real* U;                         // [N*imax] tangent of G (jvp pass)
+    DevParams<real> prm;
+    uint32_t* counter;
+    int32_t* status;
+};
+template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
+template <typename real> void launch_force(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
+template <typename real> void launch_jvp(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
+
+// ---- networks (mlp.cu) -----------------------------------------------------------------------
+template <typename real>
+struct MlpArgs {
+    int32_t natoms, ntypes, imax;
+    const int32_t* tstart;           // [T+1] start of each type in tlist
+    const int32_t* tlist;            // [N] atoms grouped by type
+    const real* G;                   // [N*imax]
+    real* dEdG;                      // [N*imax]
+    double* Eatom;                   // [N] network output + vacuum energy
+    // training (double backward)
+    const real* U;                   // [N*imax] tangent of G
+    const double* ce;                // [N] energy-loss weight per atom
+    double ct;                       // tangent-loss weight
+    double* grad;                    // [P] parameter gradient accumulator (FP64 in both precisions)
+    const int32_t* poff;             // [T] parameter offset of each type
+    DevParams<real> prm;
+};
+template <typename real> void launch_mlp_forward_backward(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st);
+template <typename real> void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st);
+
+// ---- small kernels (misc.cu) ---------------------------------------------------------------
+void launch_type_lists(int natoms, int ntypes, const int32_t* type, int32_t* tcount, int32_t* tstart, int32_t* tlist,
+                       int32_t* status, cudaStream_t st);
+template <typename real>
+void launch_reduce_structures(int nstruc, const int32_t* off, const double* Eatom, const real* W, const real* F,
+                              double* Es, double* Ws, double* Fout, cudaStream_t st);
+void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st);
+size_t scan_tmp_ints(int n);
+
+// raise the dynamic shared-memory limit of every kernel once (outside any graph capture)
+void configure_bp(int maxsmem);
+void configure_mlp(int maxsmem);
+void configure_nbr(int maxsmem);
+size_t bp_smem_bytes(const DevPot& pot, int cap, bool fp64);
+size_t mlp_smem_bytes(const DevPot& pot, bool fp64, bool train);
+
+}  // namespace ann

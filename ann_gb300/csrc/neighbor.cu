@@ -1,0 +1,318 @@
+// K1: periodic-image neighbour list, cell-binned, one warp per centre atom with warp-ballot
+// compaction. Replaces the reference's NeighborList(struc, rc) (src/struc/, missing from the
+// snapshot; contract from the call sites src/nnp/nnp.cpp:343-348, 478-486): every image
+// j + R n with |x_i - x_j - R n| < rc except (j == i, n == 0), r = x_i - x_j - R n.
+//
+// Binning: fractional coordinates s = R^-1 x are wrapped (s = frac + m) and binned along each
+// lattice direction (bins ~rc/2 wide). A centre atom in bin b visits the unwrapped bins
+// u = b + e, |e_d| <= sten_d = ceil(rc |g_d| nb_d) (g_d = row d of R^-1), which covers every
+// image of every atom within rc once, for any cell shape and for cells smaller than rc
+// (u_d outside [0,nb_d) selects the image k_d = floor(u_d / nb_d)).
+// The accepted entries are written grouped by neighbour type (a stable partition) so that the
+// symmetry-function kernels iterate type blocks without branching.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+#include "kernels.hpp"
+
+namespace ann {
+
+static __device__ __forceinline__ int32_t pack3(int a, int b, int c) {
+    return (int32_t)(((uint32_t)a & 1023u) | (((uint32_t)b & 1023u) << 10) | (((uint32_t)c & 1023u) << 20));
+}
+static __device__ __forceinline__ void unpack3(int32_t p, int& a, int& b, int& c) {
+    a = ((int32_t)((uint32_t)p << 22)) >> 22;
+    b = ((int32_t)((uint32_t)p << 12)) >> 22;
+    c = ((int32_t)((uint32_t)p << 2)) >> 22;
+}
+static __device__ __forceinline__ int floordiv(int a, int b) { int q = a / b; if ((a % b != 0) && ((a < 0) != (b < 0))) --q; return q; }
+
+// ---------------------------------------------------------------- per-structure geometry
+// one block; thread t handles structures t, t+blockDim...; bins per structure bounded by
+// 2*natoms+1 so that the bin arrays can be sized from the atom count alone.
+__global__ void k_struc_setup(NbrArgs a) {
+    __shared__ int32_t part[1024];
+    const int S = a.nstruc;
+    const int per = (S + blockDim.x - 1) / blockDim.x;
+    const int lo = threadIdx.x * per, hi = min(S, lo + per);
+    int32_t local = 0;
+    for (int s = lo; s < hi; ++s) {
+        StrucGeo g;
+        const double* R = a.cell + 9 * s;
+        for (int k = 0; k < 9; ++k) g.R[k] = R[k];
+        auto at = [&](int r, int c) { return R[3 * c + r]; };
+        const double det = at(0, 0) * (at(1, 1) * at(2, 2) - at(1, 2) * at(2, 1)) - at(0, 1) * (at(1, 0) * at(2, 2) - at(1, 2) * at(2, 0)) +
+                           at(0, 2) * (at(1, 0) * at(2, 1) - at(1, 1) * at(2, 0));
+        const double id = 1.0 / det;
+        double m[3][3];
+        m[0][0] = (at(1, 1) * at(2, 2) - at(1, 2) * at(2, 1)) * id; m[0][1] = (at(0, 2) * at(2, 1) - at(0, 1) * at(2, 2)) * id; m[0][2] = (at(0, 1) * at(1, 2) - at(0, 2) * at(1, 1)) * id;
+        m[1][0] = (at(1, 2) * at(2, 0) - at(1, 0) * at(2, 2)) * id; m[1][1] = (at(0, 0) * at(2, 2) - at(0, 2) * at(2, 0)) * id; m[1][2] = (at(0, 2) * at(1, 0) - at(0, 0) * at(1, 2)) * id;
+        m[2][0] = (at(1, 0) * at(2, 1) - at(1, 1) * at(2, 0)) * id; m[2][1] = (at(0, 1) * at(2, 0) - at(0, 0) * at(2, 1)) * id; m[2][2] = (at(0, 0) * at(1, 1) - at(0, 1) * at(1, 0)) * id;
+        for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) g.Ri[3 * c + r] = m[r][c];
+        const int nat = a.off[s + 1] - a.off[s];
+        const int maxbins = 2 * max(nat, 1) + 1;
+        double gn[3];
+        for (int d = 0; d < 3; ++d) gn[d] = sqrt(m[d][0] * m[d][0] + m[d][1] * m[d][1] + m[d][2] * m[d][2]);
+        const bool ok = isfinite(det) && det != 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const double h = ok ? 1.0 / gn[d] : 1.0;             // distance between lattice planes
+            int nb = (int)floor(h / (0.5 * a.rc));
+            g.nb[d] = max(1, min(nb, 1024));
+        }
+        while ((long long)g.nb[0] * g.nb[1] * g.nb[2] > maxbins) {
+            int dm = 0;
+            if (g.nb[1] > g.nb[dm]) dm = 1;
+            if (g.nb[2] > g.nb[dm]) dm = 2;
+            g.nb[dm] = max(1, g.nb[dm] / 2);
+        }
+        for (int d = 0; d < 3; ++d) g.sten[d] = ok ? (int)ceil(a.rc * gn[d] * g.nb[d] + 1e-9) : 0;
+        g.atom0 = a.off[s]; g.natoms = nat; g.bin0 = 0; g.pad = ok ? 0 : 1;
+        a.geo[s] = g;
+        local += g.nb[0] * g.nb[1] * g.nb[2];
+    }
+    part[threadIdx.x] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // serial prefix over <=1024 partials
+        int32_t run = 0;
+        for (int t = 0; t < (int)blockDim.x; ++t) { const int32_t v = part[t]; part[t] = run; run += v; }
+        *a.nbins_total = run;
+        if (run > a.nbins_cap) atomicOr(a.status, (int)ST_NBR_OVERFLOW);
+    }
+    __syncthreads();
+    int32_t run = part[threadIdx.x];
+    for (int s = lo; s < hi; ++s) { a.geo[s].bin0 = run; run += a.geo[s].nb[0] * a.geo[s].nb[1] * a.geo[s].nb[2]; }
+}
+
+// ---------------------------------------------------------------- atom -> bin
+__global__ void k_atom_bin(NbrArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.natoms) return;
+    const int s = a.sid[i];
+    const StrucGeo& g = a.geo[s];
+    const double x = a.pos[3 * i], y = a.pos[3 * i + 1], z = a.pos[3 * i + 2];
+    const int t = a.type[i];
+    if (t < 0 || t >= a.ntypes) atomicOr(a.status, (int)ST_BAD_TYPE);
+    a.pos4[i] = make_float4((float)x, (float)y, (float)z, __int_as_float(t));
+    int b[3] = {0, 0, 0}, m[3] = {0, 0, 0};
+    if (!(isfinite(x) && isfinite(y) && isfinite(z)) || g.pad) {
+        atomicOr(a.status, (int)ST_NONFINITE);
+    } else {
+        for (int d = 0; d < 3; ++d) {
+            const double sd = g.Ri[d] * x + g.Ri[3 + d] * y + g.Ri[6 + d] * z;
+            const double fl = floor(sd);
+            if (fabs(fl) > 500.0) { atomicOr(a.status, (int)ST_IMAGE_RANGE); continue; }
+            m[d] = (int)fl;
+            int bb = (int)floor((sd - fl) * g.nb[d]);
+            b[d] = min(max(bb, 0), g.nb[d] - 1);
+        }
+    }
+    const int bin = g.bin0 + (b[2] * g.nb[1] + b[1]) * g.nb[0] + b[0];
+    const int safe_bin = min(bin, a.nbins_cap - 1);
+    a.abin[i] = safe_bin;
+    a.abc[i] = pack3(b[0], b[1], b[2]);
+    a.am[i] = pack3(m[0], m[1], m[2]);
+    a.aslot[i] = atomicAdd(&a.bcount[safe_bin], 1);
+}
+
+__global__ void k_bin_scatter(NbrArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.natoms) return;
+    a.bidx[a.bstart[a.abin[i]] + a.aslot[i]] = i;
+}
+
+// deterministic order inside each bin (atom index), then the bin-ordered copies
+__global__ void k_bin_sort(NbrArgs a, int nbins) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    const int st = a.bstart[b], en = a.bstart[b + 1];
+    for (int p = st + 1; p < en; ++p) {
+        const int v = a.bidx[p];
+        int q = p - 1;
+        while (q >= st && a.bidx[q] > v) { a.bidx[q + 1] = a.bidx[q]; --q; }
+        a.bidx[q + 1] = v;
+    }
+    for (int p = st; p < en; ++p) {
+        const int i = a.bidx[p];
+        a.bm[p] = a.am[i];
+        a.bpos4[p] = a.pos4[i];
+        a.bposd[3 * p] = a.pos[3 * i]; a.bposd[3 * p + 1] = a.pos[3 * i + 1]; a.bposd[3 * p + 2] = a.pos[3 * i + 2];
+    }
+}
+
+// canonical FP64 pair vector, identical association to the oracle: no contraction
+static __device__ __forceinline__ void pair_vec_d(const double* xi, const double* xj, const double* R, int n0, int n1, int n2,
+                                                  double r[3], double& d2) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double dx = __dsub_rn(xi[c], xj[c]);
+        const double s = __dadd_rn(__dadd_rn(__dmul_rn((double)n0, R[c]), __dmul_rn((double)n1, R[3 + c])), __dmul_rn((double)n2, R[6 + c]));
+        r[c] = __dsub_rn(dx, s);
+    }
+    d2 = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(256) k_neighbors(NbrArgs a) {
+    extern __shared__ int32_t nsm[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int cap = a.cap;
+    int32_t* sj = nsm + wid * 3 * cap;
+    int32_t* simg = sj + cap;
+    int32_t* styp = simg + cap;
+    const unsigned lt = (1u << lane) - 1u;
+    const float rcf = (float)a.rc;
+    const float rc2f = FP64 ? (rcf + 0.05f) * (rcf + 0.05f) : rcf * rcf;
+    const double rc2 = a.rc * a.rc;
+    for (;;) {
+        int i = 0;
+        if (lane == 0) i = (int)atomicAdd(a.counter, 1u);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= a.natoms) break;
+        const StrucGeo& g = a.geo[a.sid[i]];
+        int b0, b1, b2, mi0, mi1, mi2;
+        unpack3(a.abc[i], b0, b1, b2);
+        unpack3(a.am[i], mi0, mi1, mi2);
+        const float4 xi4 = a.pos4[i];
+        const double xid[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
+        float Rf[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Rf[k] = (float)g.R[k];
+        int cursor = 0;
+        for (int e2 = -g.sten[2]; e2 <= g.sten[2]; ++e2) {
+            const int u2 = b2 + e2, k2 = floordiv(u2, g.nb[2]), q2 = u2 - k2 * g.nb[2];
+            for (int e1 = -g.sten[1]; e1 <= g.sten[1]; ++e1) {
+                const int u1 = b1 + e1, k1 = floordiv(u1, g.nb[1]), q1 = u1 - k1 * g.nb[1];
+                for (int e0 = -g.sten[0]; e0 <= g.sten[0]; ++e0) {
+                    const int u0 = b0 + e0, k0 = floordiv(u0, g.nb[0]), q0 = u0 - k0 * g.nb[0];
+                    const int bin = g.bin0 + (q2 * g.nb[1] + q1) * g.nb[0] + q0;
+                    const int st = a.bstart[bin], en = a.bstart[bin + 1];
+                    for (int c0 = st; c0 < en; c0 += 32) {
+                        const int c = c0 + lane;
+                        bool acc = false;
+                        int j = 0, n0 = 0, n1 = 0, n2 = 0, tj = 0;
+                        if (c < en) {
+                            j = a.bidx[c];
+                            int mj0, mj1, mj2;
+                            unpack3(a.bm[c], mj0, mj1, mj2);
+                            n0 = k0 + mi0 - mj0; n1 = k1 + mi1 - mj1; n2 = k2 + mi2 - mj2;
+                            const float4 pj = a.bpos4[c];
+                            tj = __float_as_int(pj.w);
+                            const float fn0 = (float)n0, fn1 = (float)n1, fn2 = (float)n2;
+                            const float rx = (xi4.x - pj.x) - (fn0 * Rf[0] + fn1 * Rf[3] + fn2 * Rf[6]);
+                            const float ry = (xi4.y - pj.y) - (fn0 * Rf[1] + fn1 * Rf[4] + fn2 * Rf[7]);
+                            const float rz = (xi4.z - pj.z) - (fn0 * Rf[2] + fn1 * Rf[5] + fn2 * Rf[8]);
+                            const float d2f = rx * rx + ry * ry + rz * rz;
+                            acc = d2f < rc2f;
+                            if (FP64 && acc) {
+                                double r[3], d2;
+                                pair_vec_d(xid, a.bposd + 3 * c, g.R, n0, n1, n2, r, d2);
+                                acc = d2 < rc2;
+                            }
+                            if (j == i && n0 == 0 && n1 == 0 && n2 == 0) acc = false;
+                        }
+                        const unsigned msk = __ballot_sync(0xffffffffu, acc);
+                        const int pos = cursor + __popc(msk & lt);
+                        if (acc && pos < cap) { sj[pos] = j; simg[pos] = pack3(n0, n1, n2); styp[pos] = tj; }
+                        cursor += __popc(msk);
+                    }
+                }
+            }
+        }
+        int cnt = cursor;
+        if (cnt > cap) {
+            if (lane == 0) { atomicOr(a.status, (int)ST_NBR_OVERFLOW); atomicMax(a.status + 1, cnt); }
+            cnt = cap;
+        }
+        __syncwarp();
+        // stable partition by neighbour type into the output row, with the pair geometry
+        const size_t row = (size_t)i * cap;
+        int base = 0;
+        for (int t = 0; t < a.ntypes; ++t) {
+            int ct = 0;
+            for (int e0 = 0; e0 < cnt; e0 += 32) {
+                const int e = e0 + lane;
+                const bool f = (e < cnt) && (styp[e] == t);
+                const unsigned msk = __ballot_sync(0xffffffffu, f);
+                if (f) {
+                    const int o = base + ct + __popc(msk & lt);
+                    const int j = sj[e];
+                    int n0, n1, n2;
+                    unpack3(simg[e], n0, n1, n2);
+                    a.nj[row + o] = j;
+                    a.nimg[row + o] = simg[e];
+                    if (FP64) {
+                        double r[3], d2;
+                        pair_vec_d(xid, a.pos + 3 * (size_t)j, g.R, n0, n1, n2, r, d2);
+                        reinterpret_cast<Vec4d*>(a.nr)[row + o] = Vec4d{r[0], r[1], r[2], sqrt(d2)};
+                    } else {
+                        const float4 pj = a.pos4[j];
+                        const float fn0 = (float)n0, fn1 = (float)n1, fn2 = (float)n2;
+                        const float rx = (xi4.x - pj.x) - (fn0 * Rf[0] + fn1 * Rf[3] + fn2 * Rf[6]);
+                        const float ry = (xi4.y - pj.y) - (fn0 * Rf[1] + fn1 * Rf[4] + fn2 * Rf[7]);
+                        const float rz = (xi4.z - pj.z) - (fn0 * Rf[2] + fn1 * Rf[5] + fn2 * Rf[8]);
+                        reinterpret_cast<Vec4f*>(a.nr)[row + o] = Vec4f{rx, ry, rz, sqrtf(rx * rx + ry * ry + rz * rz)};
+                    }
+                }
+                ct += __popc(msk);
+            }
+            if (lane == 0) a.ntc[(size_t)i * a.ntypes + t] = ct;
+            base += ct;
+        }
+        if (lane == 0) a.nn[i] = cnt;
+        __syncwarp();
+    }
+}
+
+// Verlet-list refresh: r from current positions and the stored images
+template <bool FP64>
+__global__ void k_refresh(NbrArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.natoms) return;
+    const StrucGeo& g = a.geo[a.sid[i]];
+    const int cnt = a.nn[i];
+    const size_t row = (size_t)i * a.cap;
+    const double xid[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
+    for (int e = lane; e < cnt; e += 32) {
+        const int j = a.nj[row + e];
+        int n0, n1, n2;
+        unpack3(a.nimg[row + e], n0, n1, n2);
+        double r[3], d2;
+        pair_vec_d(xid, a.pos + 3 * (size_t)j, g.R, n0, n1, n2, r, d2);
+        if (FP64) reinterpret_cast<Vec4d*>(a.nr)[row + e] = Vec4d{r[0], r[1], r[2], sqrt(d2)};
+        else reinterpret_cast<Vec4f*>(a.nr)[row + e] = Vec4f{(float)r[0], (float)r[1], (float)r[2], (float)sqrt(d2)};
+    }
+}
+
+void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st) {
+    ++::ann::g_launch_counter, k_struc_setup<<<1, 1024, 0, st>>>(a);
+    cudaMemsetAsync(a.bcount, 0, sizeof(int32_t) * (a.nbins_cap + 1), st);
+    const int nb = (a.natoms + 255) / 256;
+    if (a.natoms > 0) ++::ann::g_launch_counter, k_atom_bin<<<nb, 256, 0, st>>>(a);
+    launch_exclusive_scan(a.bcount, a.bstart, a.nbins_cap + 1, a.scan_tmp, st);
+    if (a.natoms > 0) ++::ann::g_launch_counter, k_bin_scatter<<<nb, 256, 0, st>>>(a);
+    ++::ann::g_launch_counter, k_bin_sort<<<(a.nbins_cap + 255) / 256, 256, 0, st>>>(a, a.nbins_cap);
+    cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), st);
+    const int warps = 8;
+    const size_t smem = (size_t)warps * 3 * a.cap * sizeof(int32_t);
+    int grid = (a.natoms + warps - 1) / warps;
+    grid = std::min(grid, 152 * 8);
+    if (grid < 1) grid = 1;
+    if (fp64) ++::ann::g_launch_counter, k_neighbors<true><<<grid, warps * 32, smem, st>>>(a);
+    else ++::ann::g_launch_counter, k_neighbors<false><<<grid, warps * 32, smem, st>>>(a);
+}
+
+void configure_nbr(int maxsmem) {
+    cudaFuncSetAttribute(k_neighbors<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+    cudaFuncSetAttribute(k_neighbors<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+}
+
+void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st) {
+    const int threads = 256;
+    const int grid = (int)(((long long)a.natoms * 32 + threads - 1) / threads);
+    if (grid < 1) return;
+    if (fp64) ++::ann::g_launch_counter, k_refresh<true><<<grid, threads, 0, st>>>(a);
+    else ++::ann::g_launch_counter, k_refresh<false><<<grid, threads, 0, st>>>(a);
+}
+
+}  // namespace ann

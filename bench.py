@@ -1,0 +1,338 @@
+"""Benchmark: NNP energy+force atom-evaluations per second on one GB300 (and N replicas).
+
+Workload: 256 binary A/B structures, N ~ U{32..512} atoms each (~69.6k atoms), number density
+0.05 /A^3, rc = 6.5 A, 72 symmetry functions per atom (12 radial per species + 16 angular per
+species pair), 72-64-64-1 softplus networks; one packed batch per step (neighbour list,
+symmetry functions, networks, forces, virials, per-structure energies).
+
+  value  : atom-evaluations/s with the batch resident in HBM (device-timed with CUDA events on
+           the library's stream, L2 flushed by a 256 MiB write between steps, outside the timed
+           events), mixed precision (FP32 geometry/basis/forces, FP32 networks, FP64 sums).
+  e2e    : the same through ann_compute with host buffers (H2D of positions/types/cells/offsets and
+           D2H of energies/forces/virials inside the timed region), wall-clock.
+  fp64   : the plain FP64 GPU form on the same batch (the 5x target's denominator).
+  --impl reference : the CPU path (the FP64 oracle that restates the reference's code) on all host
+           cores, on a bounded sample of the same workload.
+Multi-GPU: structures are independent, so each rank runs its own full batch (weak scaling);
+no collective on the data path, a barrier and a max over ranks around the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "NNP E+F atom-evals/s: batched BF16/FP32 vs plain FP64 on GB300 at <=10 meV/A force err"
+WORKLOAD = ("256 binary A/B structures, N~U{32..512} (seeded), rho=0.05/A^3, 1.8 A min distance, rc=6.5 A, "
+            "72 symmetry functions (12 radial/species + 16 angular/pair), 72-64-64-1 softplus nets, one packed batch")
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_work(ctx, offs, posn, types, cell):
+    """Exact pair / triplet counts of the batch (within rc, per type block) from an FP64 pass, and the
+    algorithmic work of the force kernel by the counting conventions: per pair 15 flop + cos/sin
+    pair, radial function F = 8 flop + 1 exp; per triplet 20 flop + 1 exp per damping group,
+    angular function F = 10 flop + 1 pow (2 MUFU). Bytes: neighbour row (16 B geometry + 4 B index
+    read, 12 B Newton-3rd write) per pair, dE/dG row and 48 B force/virial per atom."""
+    from ann_gb300 import FP64
+    ctx.compute(offs, posn, types, cell, precision=FP64)
+    i, j, img, r = ctx.neighbors(with_vectors=True)
+    d = np.linalg.norm(r, axis=1)
+    keep = d < ctx.rc
+    i, j = i[keep], j[keep]
+    T = ctx.ntypes
+    N = len(types)
+    cnt = np.zeros((N, T), np.int64)
+    np.add.at(cnt, (i, types[j]), 1)
+    nR = {}
+    nA = {}
+    ng = 2  # angular damping groups of this potential (eta_B in {0.003, 0.01})
+    nin = {t: ctx.num_inputs(t) for t in range(T)}
+    # the workload's potential has the same basis sizes for every block
+    nr_block = 12
+    na_block = 16
+    pairs = cnt.sum()
+    trip = 0
+    for a in range(T):
+        for b in range(a, T):
+            if a == b:
+                trip += int((cnt[:, a] * (cnt[:, a] - 1) // 2).sum())
+            else:
+                trip += int((cnt[:, a] * cnt[:, b]).sum())
+    flops = pairs * (15 + 8 * nr_block) + trip * (20 + 10 * na_block)
+    mufu = pairs * (2 + nr_block) + trip * (2 * na_block + ng)
+    imax = max(nin.values())
+    bytes_ = pairs * (16 + 4 + 12) + N * (imax * 4 + 48)
+    return dict(pairs=int(pairs), triplets=int(trip), natoms=N, force_flops=float(flops), force_mufu=float(mufu),
+                force_bytes=float(bytes_), symm_flops=float(pairs * (15 + 6 * nr_block) + trip * (20 + 4 * na_block)),
+                symm_mufu=float(pairs * (2 + nr_block) + trip * (2 * na_block + ng)))
+
+
+def cpu_reference(offs, posn, types, cell, pot_text, budget_s=12.0, steps=1, warmup=0, threads=None):
+    """The oracle (CPU restatement of the reference's path, FP64) on all host cores over a bounded
+    sample of the workload's structures; returns atom-evals/s and the sample description."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import Oracle
+    orc = Oracle()
+    pot = orc.load_text(pot_text)
+    threads = threads or os.cpu_count() or 1
+    S = len(offs) - 1
+
+    def run(k):
+        o = offs[: k + 1]
+        n = int(o[-1])
+        t0 = time.perf_counter()
+        pot.compute(o, posn[:n], types[:n], cell[:k], forces=True, nthreads=threads)
+        return time.perf_counter() - t0, n
+
+    # size the sample: time a first chunk of `threads` structures, then scale to the budget
+    k = min(S, threads)
+    dt, n = run(k)
+    per_struct = dt / max(k, 1) * threads
+    k = int(min(S, max(threads, budget_s / max(per_struct, 1e-6) * threads / 1.0)))
+    k = max(1, min(S, (k // threads) * threads or k))
+    for _ in range(warmup):
+        run(k)
+    rates = []
+    for _ in range(max(1, steps)):
+        dt, n = run(k)
+        rates.append(n / dt)
+    return dict(value=float(np.median(rates)), unit="atom-evals/s", cores=threads, kind="port",
+                sample=f"first {k} of {S} structures ({n} atoms) of the workload, FP64 oracle, {threads} threads, "
+                       f"structures block-distributed over threads (thread::Dist rule)")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nstruc", type=int, default=256)
+    args = ap.parse_args()
+    rank, world, local = _env_rank()
+    W_ = max(args.warmup, 3)
+
+    from ann_gb300 import workloads as WL
+    from ann_gb300.api import pack_batch
+
+    structs = WL.config2(nstruc=args.nstruc)
+    offs, posn, types, cell = pack_batch(structs)
+    N = int(offs[-1])
+
+    if args.impl == "reference":
+        if world > 1 and rank != 0:
+            return
+        # same basis and networks as the GPU arm (host-only construction; the input scaling does
+        # not change the CPU cost)
+        pot_text = WL.config_potential_text(2)
+        cb = cpu_reference(offs, posn, types, cell, pot_text, steps=args.steps, warmup=args.warmup)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "atom-evals/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": WORKLOAD, "natoms": N, "nstruc": len(structs), "sample": cb["sample"]},
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from ann_gb300 import FP64, MIXED, Context
+
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    ctx = Context(device=dev, precision=MIXED, use_graphs=True)
+    ctx.load_text(WL.config_potential_text(2))
+    WL.precondition(ctx, offs, posn, types, cell)
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        p = Path(td) / "pot.ann"
+        ctx.write(p)
+        pot_text = p.read_text()
+    ctx.load_text(pot_text)
+
+    # ---- accuracy of the mixed path vs the FP64 path on the same batch
+    E64, F64, _ = ctx.compute(offs, posn, types, cell, precision=FP64)
+    Emx, Fmx, _ = ctx.compute(offs, posn, types, cell, precision=MIXED)
+    nat = np.diff(offs)
+    acc = {"e_mev_atom_max": float(np.max(np.abs(Emx - E64) / nat) * 1e3),
+           "f_mev_A_max": float(np.max(np.abs(Fmx - F64)) * 1e3),
+           "f_mev_A_rms": float(np.sqrt(np.mean((Fmx - F64) ** 2)) * 1e3),
+           "reference": "plain FP64 GPU form on the same batch"}
+    work = algorithmic_work(ctx, offs, posn, types, cell)
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def timed_device(prec, steps, warm):
+        ctx.upload(offs, posn, types, cell)
+        for _ in range(warm):
+            ctx.compute_resident(prec)
+        ctx.download(forces=False, virial=False)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize(dev)
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+            ctx.compute_resident(prec)
+            ev[k][1].record(stream)
+        ctx.download(forces=False, virial=False)
+        torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in ev]
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    t_wall = time.perf_counter()
+    ms = timed_device(MIXED, args.steps, W_)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    ms_step = float(np.sum(ms) / len(ms))
+    tmax = ms_step
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms_step], device=f"cuda:{dev}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tmax = float(tt.item())
+    value = N * world / (tmax * 1e-3)
+    launches_per_step = ctx.kernels_per_batch()
+
+    # ---- plain FP64 form on the same batch
+    ms64 = timed_device(FP64, max(3, args.steps // 4), 2)
+    fp64_value = N / (float(np.mean(ms64)) * 1e-3)
+
+    # ---- per-phase kernel durations (CUDA events around each phase on the library stream)
+    ctx.profile_phases(True)
+    ctx.upload(offs, posn, types, cell)
+    phases = []
+    for k in range(W_ + args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ctx.compute_resident(MIXED)
+        ctx.synchronize()
+        if k >= W_:
+            phases.append(ctx.phase_times())
+    ctx.profile_phases(False)
+    ph = np.mean(np.array(phases), axis=0)
+    names = ["neighbour_list", "type_lists", "symmetry_functions", "networks", "forces", "reductions"]
+    phase_ms = {n: float(v) for n, v in zip(names, ph)}
+    dom = int(np.argmax(ph))
+    from ann_gb300.api import peaks
+    pk = peaks()
+    t_force = ph[4] * 1e-3
+    sm_mhz = clk.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12           # TFLOP/s (FMA = 2 flop) at the sampled clock
+    mufu_peak = 152 * 16 * sm_mhz * 1e6 / 1e12                 # T ops/s
+    roofline = {"kernel": "k_bp force pass (" + names[4] + ")", "bound": "hbm",
+                "achieved": work["force_bytes"] / t_force / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": work["force_bytes"] / t_force / 1e9 / pk["hbm_gbs"], "traffic": None,
+                "peak_source": pk["source"], "dominant_phase": names[dom]}
+    roofline_compute = {"kernel": roofline["kernel"], "bound": "fp32+mufu",
+                        "fp32_tflops": work["force_flops"] / t_force / 1e12, "fp32_peak_tflops": fp32_peak,
+                        "frac_fp32": work["force_flops"] / t_force / 1e12 / fp32_peak,
+                        "mufu_tops": work["force_mufu"] / t_force / 1e12, "mufu_peak_tops": mufu_peak,
+                        "frac_mufu": work["force_mufu"] / t_force / 1e12 / mufu_peak,
+                        "note": "peaks = 152 SMs x (128 FP32 lanes x 2 | 16 MUFU) x sampled SM clock; algorithmic counts "
+                                "(angular pow = 2 MUFU) though the kernel replaces pow by squaring chains"}
+
+    # ---- end to end through the C ABI with host buffers
+    e = np.zeros(len(structs))
+    f = np.zeros((N, 3))
+    w = np.zeros((len(structs), 3, 3))
+    for _ in range(W_):
+        ctx.compute(offs, posn, types, cell, precision=MIXED)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e, f, w = ctx.compute(offs, posn, types, cell, precision=MIXED)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    h2d = int(posn.nbytes + types.nbytes + cell.nbytes + 4 * len(offs) + 4 * N)
+    d2h = int(8 * len(structs) + 24 * N + 72 * len(structs) + 32)
+
+    line = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps, "warmup": W_,
+            "ms_per_step": tmax, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "natoms": N, "nstruc": len(structs), "precision": "mixed (FP32 basis/forces/networks, FP64 energy sums)",
+                       "l2": "flushed between steps (256 MiB write outside the timed events)", "graphs": True,
+                       "parallelism": f"replicas x{world} (structures sharded, no collective)"},
+            "fp64_value": fp64_value, "speedup_vs_fp64": value / world / fp64_value,
+            "accuracy": acc, "phase_ms": phase_ms, "work": work,
+            "roofline": roofline, "roofline_compute": roofline_compute,
+            "e2e": {"value": N / t_e2e, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches_per_step * args.steps),
+            "clocks": clk, "wall_s_timed_region": t_wall}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference(offs, posn, types, cell, pot_text)
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+/*
+ * ann_gpu.h -- C ABI of the GB300 Behler-Parrinello energy/force library (libann_gpu.so).
+ *
+ * Drop-in boundary for the compute call of markdellostritto/ann ("AtomicNN"): it replaces
+ *   NNP::read / NNP::write                     src/nnp/nnp.cpp:181-307 (+ ANN text IO src/ml/nn.cpp:1436-1578)
+ *   NNP::init + NNP::symm + NNP::energy        src/nnp/nnp.cpp:316-447
+ *   NNP::force / NNP::compute                  src/nnp/nnp.cpp:461-736
+ *   ptnl::PotNNPE::compute (energy incl. E_vac) src/torch/pot_nnpe.cpp:169-288
+ *   NeighborList(struc, rc) build               src/struc/ (missing; contract from src/nnp/nnp.cpp:343-348)
+ *   ANN::operator>> / operator<< param packing src/ml/nn.cpp:846-880
+ *   NNPTEFR::error_cost_o1 energy gradient      src/nnp/nnptefr2.cpp:1321-1374, 984-995
+ *   NNPTE::error force-term gradient            src/nnp/nnptef.cpp:1560-1936
+ *   Verlet::compute MD step                      src/torch/integrator.cpp:177-200
+ *
+ * Conventions (metal units: eV, Angstrom, fs, Dalton):
+ *  - every function returns 0 (ANN_OK) or an ANN_ERR_* code; ann_last_error() gives the text.
+ *    No C++ exception crosses this boundary (the reference throws std::invalid_argument /
+ *    std::runtime_error for the same conditions).
+ *  - the caller owns all host arrays; the context owns its device buffers, one CUDA stream and
+ *    captured CUDA graphs. A context is not reentrant (like the reference's NNP, which keeps
+ *    per-call scratch): use one context per host thread.
+ *  - a batch is nstruc structures packed back to back: atom_offsets[nstruc+1] (atom_offsets[0]=0),
+ *    posn[3*N] (x,y,z per atom), type[N] (index into the potential's types, see
+ *    ann_type_index), cell[9*nstruc] (per structure the 3x3 lattice matrix R column-major:
+ *    cell[9*s + 3*c + r] = R[r][c], lattice vectors are the columns, as Structure::R()).
+ *  - neighbours: every periodic image j + R n with |x_i - x_j - R n| < rc, except j==i, n==0.
+ *  - forces: F = -dE/dx (3N); energies per structure include the per-type vacuum energies
+ *    (NNH::energy src/nnp/nnh.cpp:118-121). virial per structure W[a*3+b] = sum over centre atoms
+ *    i and neighbours j of r_ij[a] * v_ij[b], v_ij = -dE_i/dr_ij (so dE/d(strain)_ab = -W_ba).
+ */
+#ifndef ANN_GPU_H
+#define ANN_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ANN_GPU_ABI_VERSION 1
+
+enum ann_status {
+    ANN_OK = 0,
+    ANN_ERR_ARG = 1,          /* invalid argument (null pointer, bad size, bad type index)          */
+    ANN_ERR_IO = 2,           /* file could not be opened / written                                  */
+    ANN_ERR_FORMAT = 3,       /* malformed potential file                                            */
+    ANN_ERR_CUDA = 4,         /* CUDA runtime error (no device, launch failure, out of memory)       */
+    ANN_ERR_CAPACITY = 5,     /* a device capacity was exceeded and could not be grown               */
+    ANN_ERR_STATE = 6,        /* call out of order (no potential loaded, no batch, no forward pass)  */
+    ANN_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up                                  */
+    ANN_ERR_UNSUPPORTED = 8,  /* valid input the GPU path does not implement (named in the message)  */
+    ANN_ERR_NUMERIC = 9       /* non-finite positions / cell, or non-finite results                  */
+};
+
+enum ann_precision {
+    ANN_FP64 = 0,   /* plain form: FP64 geometry, basis, network and forces                          */
+    ANN_MIXED = 1   /* FP32 geometry/basis/forces, FP32-accumulated network, FP64 energy sums       */
+};
+
+enum ann_newton {
+    ANN_NEWTON_ALL_IMAGES = 0,    /* Newton-3rd force on every neighbour entry (exact -dE/dx)        */
+    ANN_NEWTON_UNTRANSLATED = 1   /* only for image n==0: the verlet::List rule of nnp.cpp:550       */
+};
+
+typedef struct ann_options {
+    int32_t device;              /* CUDA device ordinal                                               */
+    int32_t precision;           /* default precision for calls that do not name one (ann_precision)  */
+    int32_t newton;              /* ann_newton                                                         */
+    int32_t max_neighbors;       /* initial neighbour capacity per atom (0 = estimate from density)   */
+    int32_t use_graphs;          /* capture the per-batch kernel sequence in a CUDA graph (1 = yes)   */
+    int32_t mlp_backend;         /* 0 = auto, 1 = SIMT kernels, 2 = tcgen05 tensor-core kernels (MIXED) */
+} ann_options;
+
+typedef struct ann_ctx ann_ctx;
+
+/* ---- lifetime ------------------------------------------------------------------------------ */
+void ann_default_options(ann_options* opt);
+int ann_create(ann_ctx** ctx, const ann_options* opt);   /* opt may be NULL (defaults)             */
+int ann_destroy(ann_ctx* ctx);
+const char* ann_last_error(const ann_ctx* ctx);          /* ctx may be NULL: last global error      */
+int ann_abi_version(void);
+
+/* ---- potential: NNP::read / NNP::write (nnp.cpp:181-307), params (nn.cpp:846-880) ----------- */
+int ann_load_potential(ann_ctx* ctx, const char* path);
+int ann_load_potential_text(ann_ctx* ctx, const char* text);
+int ann_write_potential(ann_ctx* ctx, const char* path);
+int ann_num_types(ann_ctx* ctx, int32_t* ntypes);
+int ann_type_index(ann_ctx* ctx, const char* name, int32_t* index);   /* NNP::index (nnp.hpp)      */
+int ann_type_name(ann_ctx* ctx, int32_t index, char* buf, int32_t buflen);
+int ann_cutoff(ann_ctx* ctx, double* rc);
+int ann_num_inputs(ann_ctx* ctx, int32_t type, int32_t* ninput);       /* NNH::nInput               */
+int ann_num_params(ann_ctx* ctx, int64_t* nparams);                     /* NNP::size (nnp.cpp:47-53) */
+int ann_get_params(ann_ctx* ctx, double* params, int64_t nparams);      /* types in NNP order        */
+int ann_set_params(ann_ctx* ctx, const double* params, int64_t nparams);
+/* input pre-conditioning ins = inpw*(G+inpb) of one type's network (nn.cpp:1343-1346)            */
+int ann_set_input_scaling(ann_ctx* ctx, int32_t type, const double* inpw, const double* inpb, int32_t ninput);
+/* Xavier/He/LeCun/random initialisation of one type's network exactly as ANN::resize
+ * (nn.cpp:1071-1190: std::mt19937(seed), biases then weights, column-major; dist 0 = NORMAL,
+ * 1 = UNIFORM; init 1 RAND, 2 LECUN, 3 HE, 4 XAVIER)                                              */
+int ann_init_network(ann_ctx* ctx, int32_t type, int32_t seed, int32_t dist, int32_t init,
+                     double sigma_b, double sigma_w);
+
+/* ---- compute: nnpce loop / NNP::compute / PotNNPE::compute over a batch (host buffers) ------ */
+int ann_compute(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets, const double* posn,
+                const int32_t* type, const double* cell, double* energy /* nstruc */,
+                double* forces /* 3N or NULL */, double* virial /* 9*nstruc or NULL */,
+                int32_t precision);
+
+/* ---- compute with device-resident batches -------------------------------------------------- */
+/* Stage a batch (host pointers; copied to the context's device buffers).                        */
+int ann_batch_upload(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets, const double* posn,
+                     const int32_t* type, const double* cell);
+/* Stage a batch from device pointers already on the context's device (copied device-to-device
+ * on the context stream; atom_offsets is a HOST array here, posn/type/cell are device pointers).  */
+int ann_batch_set_device(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets,
+                         const double* d_posn, const int32_t* d_type, const double* d_cell);
+/* Run the E+F pipeline on the staged batch; asynchronous on the context stream.                  */
+int ann_batch_compute(ann_ctx* ctx, int32_t precision, int32_t want_forces);
+/* Wait for the batch and copy results to host buffers (NULL = skip); grows capacities and
+ * recomputes transparently if a neighbour list overflowed.                                       */
+int ann_batch_download(ann_ctx* ctx, double* energy, double* forces, double* virial);
+/* Same results into device pointers (double) on the context's device; synchronises.              */
+int ann_batch_results_device(ann_ctx* ctx, double* d_energy, double* d_forces, double* d_virial);
+int ann_synchronize(ann_ctx* ctx);
+/* Raw CUDA stream of the context (cudaStream_t), for callers timing or ordering around it.      */
+void* ann_stream(ann_ctx* ctx);
+
+/* ---- instrumentation (no counterpart in the reference, which prints wall-clock phase timers,
+ *      nnptefr2.cpp:3374-3400) ------------------------------------------------------------------- */
+/* Total kernels this context has launched (graph replays count their kernel nodes).             */
+int ann_kernel_count(ann_ctx* ctx, int64_t* launches);
+/* enable = 1: subsequent batches run without graph capture and record CUDA events around each
+ * phase on the context stream; ann_phase_times returns the last batch's phase durations in ms:
+ * [0] neighbour list, [1] type lists, [2] symmetry functions, [3] networks, [4] forces,
+ * [5] per-structure reductions.                                                                  */
+int ann_profile_phases(ann_ctx* ctx, int32_t enable);
+int ann_phase_times(ann_ctx* ctx, double* ms, int32_t n);
+
+/* ---- inspection (parity tests) -------------------------------------------------------------- */
+/* Max inputs over types: rows of ann_get_symm / ann_get_dedg are padded to this width.           */
+int ann_symm_width(ann_ctx* ctx, int32_t* width);
+int ann_get_symm(ann_ctx* ctx, double* symm /* N*width */);       /* NNP::symm of last batch     */
+int ann_get_dedg(ann_ctx* ctx, double* dedg /* N*width */);       /* dE_i/dG_i (DODZ::dodi row 0) */
+int ann_get_atom_energies(ann_ctx* ctx, double* e /* N */);
+/* neighbour list of the last batch: total entries, then (i, j, image n0,n1,n2) per entry.        */
+int ann_num_neighbors(ann_ctx* ctx, int64_t* total);
+int ann_get_neighbors(ann_ctx* ctx, int32_t* i_out, int32_t* j_out, int32_t* img_out /* 3 per */,
+                      double* r_out /* 3 per, FP64 pipelines only else NULL */, int64_t cap);
+
+/* ---- training: forward/backward pair (the contract of a torch.autograd.Function) ------------ */
+/* L = wE/S sum_s 1/2 ((E_s-Eref_s)/N_s)^2 + wF/(3N) sum_a 1/2 |F_a-Fref_a|^2
+ * (energy term = NNPTEFR::error_cost_o1 MSE/LINEAR, nnptefr2.cpp:1321-1374 + 984-995;
+ *  force term = the intent of NNPTE::error, nnptef.cpp:1715-1825, with all neighbour terms).
+ * loss3 = {L, L_E, L_F}. Saves the state the backward pass needs on the device.                 */
+int ann_train_forward(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets, const double* posn,
+                      const int32_t* type, const double* cell, const double* energy_ref,
+                      const double* forces_ref, double w_energy, double w_force, int32_t precision,
+                      double* loss3);
+/* dL/dp (reference packing, types in NNP order) scaled by dl_scale. Requires ann_train_forward.  */
+int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t nparams);
+
+/* ---- molecular dynamics: velocity Verlet (integrator.cpp:177-200) --------------------------- */
+/* One structure; masses per type in Dalton. list_skin adds to rc for the Verlet list; the list is
+ * rebuilt when an atom has moved more than skin/2 since the last build.                          */
+int ann_md_init(ann_ctx* ctx, int64_t natoms, const double* posn, const double* vel,
+                const int32_t* type, const double* cell, const double* mass_per_type,
+                double dt_fs, double list_skin, int32_t precision);
+/* nsteps velocity-Verlet steps, captured as one CUDA graph per step. pe/ke (eV) after the last
+ * step; rebuilds = number of neighbour-list rebuilds during the call.                            */
+int ann_md_run(ann_ctx* ctx, int32_t nsteps, double* pe, double* ke, int32_t* rebuilds);
+int ann_md_get_state(ann_ctx* ctx, double* posn, double* vel, double* forces);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ANN_GPU_H */

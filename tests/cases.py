@@ -1,0 +1,142 @@
+"""Seeded structure / potential cases shared by the GPU parity tests."""
+from __future__ import annotations
+
+import numpy as np
+
+from ann_gb300 import workloads as W
+from ann_gb300.api import pack_batch
+
+GENERIC_POTENTIAL = """ann
+ntypes 2
+name X mass 12.000000 energy -0.250000
+name Y mass 16.000000 energy 0.125000
+rc 5.000000
+basis X
+basis_radial X
+BasisR TANH 5.000000 SECH 3
+\t0.500000 1.200000
+\t1.500000 0.800000
+\t2.500000 1.500000
+basis_radial Y
+BasisR TANH 5.000000 LOGISTIC 2
+\t1.000000 1.000000
+\t2.000000 0.700000
+basis_angular X X
+BasisA TANH 5.000000 GAUSS2 3
+\t3.000000 1.000000 1 0
+\t3.000000 2.500000 -1 0
+\t4.000000 3.000000 1 0
+basis_angular X Y
+BasisA TANH 5.000000 SECH 2
+\t2.500000 1.500000 1 0
+\t3.500000 2.000000 -1 0
+basis_angular Y Y
+BasisA TANH 5.000000 STUDENT3 2
+\t2.000000 1.000000 1 0
+\t2.000000 4.000000 -1 0
+basis Y
+basis_radial X
+BasisR POLY3 5.000000 LOGCOSH 2
+\t1.000000 1.100000
+\t2.000000 0.900000
+basis_radial Y
+BasisR POLY3 5.000000 TANH 2
+\t1.500000 1.300000
+\t3.000000 0.600000
+basis_angular X X
+BasisA POLY3 5.000000 STUDENT4 2
+\t2.500000 1.000000 1 0
+\t3.000000 2.000000 -1 0
+basis_angular X Y
+BasisA POLY3 5.000000 STUDENT5 1
+\t3.000000 1.700000 1 0
+basis_angular Y Y
+BasisA POLY3 5.000000 GAUSS 3
+\t4.000000 1.300000 1 0
+\t4.000000 2.000000 -1 0
+\t5.000000 1.000000 1 0
+nn X
+nn 12 7 5 1
+neuron SIGMOID 1.300000
+inpw {inpw12}
+outw 0.700000000000000
+inpb {inpb12}
+outb 0.300000000000000
+bias[1] {b1}
+bias[2] {b2}
+bias[3] {b3}
+weight[0,1] {w1}
+weight[1,2] {w2}
+weight[2,3] {w3}
+nn Y
+nn 10 6 1
+neuron TANH 0.800000
+inpw {inpw10}
+outw 1.100000000000000
+inpb {inpb10}
+outb -0.200000000000000
+bias[1] {c1}
+bias[2] {c2}
+weight[0,1] {v1}
+weight[1,2] {v2}
+"""
+
+
+def _fmt(v):
+    return " ".join(f"{x:.15f}" for x in v) + " "
+
+
+def generic_potential_text(seed=7) -> str:
+    """Every non-GAUSS angular variant, all radial variants but GAUSSIAN, TANH/POLY3 cutoffs,
+    non-integer zeta, SIGMOID/TANH networks and vacuum energies (the reference's generic path)."""
+    rng = np.random.default_rng(seed)
+    return GENERIC_POTENTIAL.format(
+        inpw12=_fmt(rng.uniform(0.5, 1.5, 12)), inpb12=_fmt(rng.uniform(-0.5, 0.5, 12)),
+        b1=_fmt(rng.normal(0, 0.1, 7)), b2=_fmt(rng.normal(0, 0.1, 5)), b3=_fmt(rng.normal(0, 0.1, 1)),
+        w1=_fmt(rng.normal(0, 0.5, 7 * 12)), w2=_fmt(rng.normal(0, 0.5, 5 * 7)), w3=_fmt(rng.normal(0, 0.5, 5)),
+        inpw10=_fmt(rng.uniform(0.5, 1.5, 10)), inpb10=_fmt(rng.uniform(-0.5, 0.5, 10)),
+        c1=_fmt(rng.normal(0, 0.1, 6)), c2=_fmt(rng.normal(0, 0.1, 1)),
+        v1=_fmt(rng.normal(0, 0.5, 6 * 10)), v2=_fmt(rng.normal(0, 0.5, 6)))
+
+
+def config_potential(ctx, cfg, tmp_path, precondition_batch=None):
+    """Initialise the configuration potential in ctx, round-trip it through the 'ann' text format
+    (what both sides read) and return that text."""
+    W.make_potential(ctx, cfg)
+    if precondition_batch is not None:
+        W.precondition(ctx, *precondition_batch)
+    p = tmp_path / f"pot{cfg}.ann"
+    ctx.write(p)
+    text = p.read_text()
+    ctx.load_text(text)
+    return text
+
+
+def small_binary(n_struc=6, seed=11):
+    s = W.random_binary(n_struc, 32, 160, seed=seed)
+    return s
+
+
+def ternary_box(dims=(10, 10, 6), seed=5):
+    return W.config4(seed=seed, dims=dims)
+
+
+def tiny_cells():
+    """Cells smaller than the cutoff (many images), a triclinic cell, a lone atom (only self
+    images) and unwrapped coordinates."""
+    rng = np.random.default_rng(3)
+    out = []
+    out.append((np.array([[0.1, 0.2, 0.3], [1.6, 1.5, 1.4]]), np.array([0, 1], np.int32), np.eye(3) * 3.1))
+    R = np.array([[4.0, 1.0, 0.5], [0.0, 3.8, 0.7], [0.0, 0.0, 4.2]])
+    x = rng.uniform(0, 1, (5, 3)) @ R.T
+    out.append((x, np.array([0, 1, 0, 1, 1], np.int32), R))
+    out.append((np.array([[0.3, 0.2, 0.1]]), np.array([0], np.int32), np.eye(3) * 3.7))
+    x = rng.uniform(0, 6, (6, 3))
+    x[0] += np.array([6.0, 0, 0]) * 2
+    x[1] -= np.array([0, 6.0, 0]) * 3
+    out.append((x, np.array([0, 1, 1, 0, 0, 1], np.int32), np.eye(3) * 6.0))
+    return out
+
+
+def batch(structs):
+    return pack_batch(structs)

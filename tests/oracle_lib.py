@@ -1,0 +1,222 @@
+"""ctypes access to the test-only CPU checkers under oracle/ (never used by the product).
+
+- ``Oracle``: the FP64 restatement of the reference path (oracle/ann_oracle.cpp).
+- ``RefBasis``: the reference's own cutoff / basis / special-function code compiled from its
+  sources (oracle/_ref/libref_basis.so), present only where the reference sources are.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[1]
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_SO = ORACLE_DIR / "_build" / "libann_oracle.so"
+REF_SO = ORACLE_DIR / "_ref" / "libref_basis.so"
+REF_SRC = Path(os.environ.get("ANN_REFERENCE_SRC", "/root/reference/src"))
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_L = C.POINTER(C.c_longlong)
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_I)
+
+
+def _l(a):
+    return None if a is None else a.ctypes.data_as(_L)
+
+
+def build_oracle(ref: bool = False) -> None:
+    target = ["oracle"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), *target, f"REF={REF_SRC}"], check=True)
+
+
+class Oracle:
+    def __init__(self):
+        if not ORACLE_SO.exists() or ORACLE_SO.stat().st_mtime < (ORACLE_DIR / "ann_oracle.cpp").stat().st_mtime:
+            build_oracle()
+        L = self.L = C.CDLL(str(ORACLE_SO))
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_load_text.restype = C.c_void_p
+        L.orc_load_text.argtypes = [C.c_char_p]
+        L.orc_free.argtypes = [C.c_void_p]
+        for f in ("orc_ntypes", "orc_nparams"):
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.orc_ninput.argtypes = [C.c_void_p, C.c_int]
+        L.orc_rc.argtypes = [C.c_void_p]
+        L.orc_rc.restype = C.c_double
+        L.orc_get_params.argtypes = [C.c_void_p, _D]
+        L.orc_set_params.argtypes = [C.c_void_p, _D]
+        for f in ("orc_fmexp", "orc_coscut", "orc_sincut"):
+            getattr(L, f).restype = C.c_double
+            getattr(L, f).argtypes = [C.c_double]
+        L.orc_cutoff.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D]
+        L.orc_basisR.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, C.c_double, _D, _D, _D, _D]
+        L.orc_basisA.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, _I, C.c_double, C.c_double, C.c_double, _D, _D, _D, _D, _D]
+        L.orc_neighbors.restype = C.c_longlong
+        L.orc_neighbors.argtypes = [C.c_int, _D, _D, C.c_double, C.c_longlong, _I, _I, _I, _D, _D]
+        L.orc_compute.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int]
+        L.orc_train.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_double, C.c_double, _D, _D]
+        L.orc_error_cost_o1.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, _D]
+        L.orc_symm_jvp.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_int]
+        L.orc_lj.restype = C.c_double
+        L.orc_lj.argtypes = [C.c_int, _D, _D, C.c_double, C.c_double, C.c_double, _D]
+        L.orc_md_step.argtypes = [C.c_void_p, C.c_int, _D, _D, _I, _D, _D, C.c_double, _D, _D, _D]
+
+    def err(self):
+        return self.L.orc_last_error().decode()
+
+    # ---- potential
+    def load_text(self, text: str):
+        p = self.L.orc_load_text(text.encode())
+        if not p:
+            raise RuntimeError(self.err())
+        return Potential(self, p)
+
+    # ---- geometry
+    def neighbors(self, x, R, rc):
+        x = np.ascontiguousarray(x, np.float64)
+        Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
+        n = len(x)
+        cap = max(1024, n * 256)
+        while True:
+            i = np.zeros(cap, np.int32); j = np.zeros(cap, np.int32); img = np.zeros(3 * cap, np.int32)
+            r = np.zeros(3 * cap); d = np.zeros(cap)
+            k = self.L.orc_neighbors(n, _d(x), _d(Rc), rc, cap, _i(i), _i(j), _i(img), _d(r), _d(d))
+            if k >= 0:
+                return i[:k], j[:k], img[:3 * k].reshape(-1, 3), r[:3 * k].reshape(-1, 3), d[:k]
+            cap = -k
+
+    def lj(self, x, R, eps=0.0104, sig=3.4, rcut=8.5):
+        x = np.ascontiguousarray(x, np.float64)
+        Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
+        F = np.zeros_like(x)
+        e = self.L.orc_lj(len(x), _d(x), _d(Rc), eps, sig, rcut, _d(F))
+        return e, F
+
+
+class Potential:
+    def __init__(self, orc: Oracle, ptr):
+        self.o, self.p = orc, C.c_void_p(ptr)
+        self.L = orc.L
+
+    def __del__(self):
+        try:
+            self.L.orc_free(self.p)
+        except Exception:
+            pass
+
+    @property
+    def ntypes(self):
+        return self.L.orc_ntypes(self.p)
+
+    @property
+    def nparams(self):
+        return self.L.orc_nparams(self.p)
+
+    def ninput(self, t):
+        return self.L.orc_ninput(self.p, t)
+
+    def get_params(self):
+        v = np.zeros(self.nparams)
+        self.L.orc_get_params(self.p, _d(v))
+        return v
+
+    def set_params(self, v):
+        v = np.ascontiguousarray(v, np.float64)
+        self.L.orc_set_params(self.p, _d(v))
+
+    def compute(self, offs, posn, types, cell, forces=True, symm=False, dedg=False, newton=1, nthreads=1):
+        offs = np.ascontiguousarray(offs, np.int64)
+        S = len(offs) - 1
+        N = int(offs[-1])
+        imax = max(self.ninput(t) for t in range(self.ntypes))
+        E = np.zeros(S)
+        F = np.zeros((N, 3)) if forces else None
+        W = np.zeros((S, 3, 3)) if forces else None
+        G = np.zeros((N, imax)) if symm else None
+        D = np.zeros((N, imax)) if dedg else None
+        rc = self.L.orc_compute(self.p, S, _l(offs), _d(np.ascontiguousarray(posn, np.float64)), _i(np.ascontiguousarray(types, np.int32)),
+                                _d(np.ascontiguousarray(cell, np.float64)), _d(E), _d(F), _d(W), _d(G), _d(D), imax, newton, nthreads)
+        if rc != 0:
+            raise RuntimeError(self.o.err())
+        return E, F, W, G, D
+
+    def train(self, offs, posn, types, cell, e_ref, f_ref, wE=1.0, wF=0.1):
+        offs = np.ascontiguousarray(offs, np.int64)
+        loss = np.zeros(3)
+        g = np.zeros(self.nparams)
+        rc = self.L.orc_train(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
+                              _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
+                              _d(np.ascontiguousarray(e_ref, np.float64)), _d(np.ascontiguousarray(f_ref, np.float64)), wE, wF, _d(loss), _d(g))
+        if rc != 0:
+            raise RuntimeError(self.o.err())
+        return loss, g
+
+    def error_cost_o1(self, offs, posn, types, cell, e_ref):
+        offs = np.ascontiguousarray(offs, np.int64)
+        loss = np.zeros(1)
+        g = np.zeros(self.nparams)
+        rc = self.L.orc_error_cost_o1(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
+                                      _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
+                                      _d(np.ascontiguousarray(e_ref, np.float64)), _d(loss), _d(g))
+        if rc != 0:
+            raise RuntimeError(self.o.err())
+        return loss[0], g
+
+    def md_step(self, x, v, types, R, masses, dt, F):
+        pe, ke = C.c_double(), C.c_double()
+        Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
+        rc = self.L.orc_md_step(self.p, len(types), _d(x), _d(v), _i(np.ascontiguousarray(types, np.int32)), _d(Rc),
+                                _d(np.ascontiguousarray(masses, np.float64)), dt, _d(F), C.byref(pe), C.byref(ke))
+        if rc != 0:
+            raise RuntimeError(self.o.err())
+        return pe.value, ke.value
+
+
+class RefBasis:
+    """The reference's own basis/cutoff/special functions (compiled from its sources)."""
+
+    def __init__(self):
+        if not REF_SO.exists():
+            if not REF_SRC.exists():
+                raise FileNotFoundError("reference sources not available")
+            build_oracle(ref=True)
+        L = self.L = C.CDLL(str(REF_SO))
+        for f in ("ref_fmexp", "ref_coscut", "ref_sincut"):
+            getattr(L, f).restype = C.c_double
+            getattr(L, f).argtypes = [C.c_double]
+        L.ref_cutoff.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D]
+        L.ref_basisR.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, C.c_double, _D, _D, _D, _D]
+        L.ref_basisA.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, _I, C.c_double, C.c_double, C.c_double, _D, _D, _D, _D, _D]
+        L.ref_read_basisR.argtypes = [C.c_char_p, _I, _D, _I, _I, _D, _D, C.c_int]
+        L.ref_read_basisA.argtypes = [C.c_char_p, _I, _D, _I, _I, _D, _D, _I, _I, C.c_int]
+
+
+def eval_basisR(lib, prefix, cut, rc, name, rs, eta, dr, dEdG):
+    n = len(eta)
+    s = np.zeros(n); sd = np.zeros(n); amp = C.c_double()
+    f = getattr(lib, prefix + "basisR")
+    assert f(cut, rc, name, n, _d(np.ascontiguousarray(rs, np.float64)), _d(np.ascontiguousarray(eta, np.float64)), dr, _d(s),
+             _d(np.ascontiguousarray(dEdG, np.float64)), C.byref(amp), _d(sd)) == 0
+    return s, amp.value, sd
+
+
+def eval_basisA(lib, prefix, cut, rc, name, eta, zeta, lam, dij, dik, cs, dEdG):
+    n = len(eta)
+    s = np.zeros(n); sd = np.zeros(3 * n); phi = C.c_double(); e2 = np.zeros(2)
+    f = getattr(lib, prefix + "basisA")
+    assert f(cut, rc, name, n, _d(np.ascontiguousarray(eta, np.float64)), _d(np.ascontiguousarray(zeta, np.float64)),
+             _i(np.ascontiguousarray(lam, np.int32)), dij, dik, cs, _d(s), _d(np.ascontiguousarray(dEdG, np.float64)), C.byref(phi),
+             _d(e2), _d(sd)) == 0
+    return s, phi.value, e2, sd
