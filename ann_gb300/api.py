@@ -78,9 +78,9 @@ _SIGS = {
     "ann_phase_times": (C.c_int, [_V, _D, C.c_int32]),
     "ann_stream": (_V, [_V]),
     "ann_symm_width": (C.c_int, [_V, _I32]),
-    "ann_get_symm": (C.c_int, [_V, _D]),
-    "ann_get_dedg": (C.c_int, [_V, _D]),
-    "ann_get_atom_energies": (C.c_int, [_V, _D]),
+    "ann_get_symm": (C.c_int, [_V, _D, C.c_int64]),
+    "ann_get_dedg": (C.c_int, [_V, _D, C.c_int64]),
+    "ann_get_atom_energies": (C.c_int, [_V, _D, C.c_int64]),
     "ann_num_neighbors": (C.c_int, [_V, _I64]),
     "ann_get_neighbors": (C.c_int, [_V, _I32, _I32, _I32, _D, C.c_int64]),
     "ann_train_forward": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, C.c_double, C.c_double, C.c_int32, _D]),
@@ -259,6 +259,7 @@ class Context:
         prec = self.precision if precision is None else precision
         S = len(offs) - 1
         N = int(offs[-1])
+        self._S, self._N = S, N
         e = np.zeros(S)
         f = np.zeros((N, 3)) if forces else None
         w = np.zeros((S, 3, 3)) if virial else None
@@ -320,17 +321,17 @@ class Context:
 
     def symm(self) -> np.ndarray:
         G = np.zeros((self._last_natoms(), self.symm_width()))
-        self._ck(self.lib.ann_get_symm(self.h, _d(G)))
+        self._ck(self.lib.ann_get_symm(self.h, _d(G), G.size))
         return G
 
     def dedg(self) -> np.ndarray:
         G = np.zeros((self._last_natoms(), self.symm_width()))
-        self._ck(self.lib.ann_get_dedg(self.h, _d(G)))
+        self._ck(self.lib.ann_get_dedg(self.h, _d(G), G.size))
         return G
 
     def atom_energies(self) -> np.ndarray:
         e = np.zeros(self._last_natoms())
-        self._ck(self.lib.ann_get_atom_energies(self.h, _d(e)))
+        self._ck(self.lib.ann_get_atom_energies(self.h, _d(e), e.size))
         return e
 
     def _last_natoms(self) -> int:

@@ -513,10 +513,10 @@ static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t s
 
 template <typename real, int PASS>
 static void configure_pass(int maxsmem) {
-    cudaFuncSetAttribute(k_bp<real, 1, true, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_bp<real, 2, true, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_bp<real, 4, true, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_bp<real, 1, false, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+    set_max_dynamic_smem(k_bp<real, 1, true, PASS>, maxsmem);
+    set_max_dynamic_smem(k_bp<real, 2, true, PASS>, maxsmem);
+    set_max_dynamic_smem(k_bp<real, 4, true, PASS>, maxsmem);
+    set_max_dynamic_smem(k_bp<real, 1, false, PASS>, maxsmem);
 }
 void configure_bp(int maxsmem) {
     configure_pass<float, PASS_SYMM>(maxsmem); configure_pass<float, PASS_FORCE>(maxsmem); configure_pass<float, PASS_JVP>(maxsmem);

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -133,6 +134,8 @@ struct ann_ctx {
     int64_t kernels = 0;            // kernels launched (graph replays add graph_kernels)
     int64_t graph_kernels = 0;
     bool profile = false;
+    bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
+    int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
     cudaEvent_t ev[16] = {};
 };
 
@@ -284,6 +287,15 @@ static NbrArgs nbr_args(ann_ctx* c, double rc) {
     return a;
 }
 
+// diagnostics: in debug mode every phase is synchronised and checked, so that a failing
+// launch is reported with its phase name
+static void check_phase(ann_ctx* c, const char* name) {
+    if (!c->debug) return;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) throw ann_error(ANN_ERR_CUDA, std::string("phase '") + name + "': " + cudaGetErrorString(e));
+}
+
 static void mark(ann_ctx* c, int k) {
     if (!c->profile) return;
     if (!c->ev[k]) cudaEventCreate(&c->ev[k]);
@@ -298,13 +310,16 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     mark(c, 0);
     if (build_list) launch_neighbors(nbr_args(c, c->pot.rc + (c->md_ready ? c->md_skin : 0.0)), fp64, st);
     else launch_refresh_geometry(nbr_args(c, c->pot.rc + c->md_skin), fp64, st);
+    check_phase(c, "neighbour list");
     mark(c, 1);
     launch_type_lists(c->N, c->pot.ntypes(), c->type.as<int32_t>(), c->tcount.as<int32_t>(), c->tstart.as<int32_t>(), c->tlist.as<int32_t>(),
                       c->status.as<int32_t>(), st);
+    check_phase(c, "type lists");
     mark(c, 2);
     BpArgs<real> b = bp_args<real>(c);
     b.prm = params_of<real>(c->pf, c->pd);
     launch_symm<real>(pot, b, st);
+    check_phase(c, "symmetry functions");
     mark(c, 3);
     MlpArgs<real> m{};
     m.natoms = c->N; m.ntypes = c->pot.ntypes(); m.imax = pot.imax;
@@ -312,14 +327,17 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     m.G = c->G.as<real>(); m.dEdG = c->dEdG.as<real>(); m.Eatom = c->Eatom.as<double>();
     m.prm = b.prm;
     launch_mlp_forward_backward<real>(pot, m, st);
+    check_phase(c, "networks");
     mark(c, 4);
     if (forces) {
         cudaMemsetAsync(c->F.p, 0, sizeof(real) * 3 * (size_t)std::max(c->N, 1), st);
         launch_force<real>(pot, b, st);
     }
+    check_phase(c, "forces");
     mark(c, 5);
     launch_reduce_structures<real>(c->S, c->off.as<int32_t>(), c->Eatom.as<double>(), forces ? c->W.as<real>() : nullptr,
                                    c->F.as<real>(), c->Es.as<double>(), c->Ws.as<double>(), forces ? c->Fout.as<double>() : nullptr, st);
+    check_phase(c, "reductions");
     mark(c, 6);
 }
 
@@ -327,6 +345,14 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
     if (!c->have_batch) throw ann_error(ANN_ERR_STATE, "no batch staged");
     if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
     ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
+    // shared-memory needs of this batch (neighbour rows are staged per warp)
+    const size_t need_bp = bp_smem_bytes(c->plan.pot, c->cap, prec == ANN_FP64) + 1024;
+    const size_t need_mlp = mlp_smem_bytes(c->plan.pot, prec == ANN_FP64, false) + 1024;
+    if (need_bp > (size_t)c->max_smem)
+        throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity " + std::to_string(c->cap) + " needs " + std::to_string(need_bp) +
+                                              " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
+    if (need_mlp > (size_t)c->max_smem)
+        throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
     const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap};
     const bool graphs = c->opt.use_graphs && build_list && c->N > 0 && !c->profile;
     if (graphs) {
@@ -336,7 +362,19 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
             const int64_t before = g_launch_counter;
             ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             if (prec == ANN_FP64) enqueue_ef<double>(c, forces, true); else enqueue_ef<float>(c, forces, true);
-            ck(cudaStreamEndCapture(c->stream, &g), "end capture");
+            const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+            if (ce != cudaSuccess) {
+                // locate the failing launch: replay the sequence eagerly with per-phase checks
+                cudaGetLastError();
+                if (g) cudaGraphDestroy(g);
+                const bool d0 = c->debug;
+                c->debug = true;
+                try {
+                    if (prec == ANN_FP64) enqueue_ef<double>(c, forces, true); else enqueue_ef<float>(c, forces, true);
+                } catch (...) { c->debug = d0; throw; }
+                c->debug = d0;
+                throw ann_error(ANN_ERR_CUDA, std::string("graph capture failed (") + cudaGetErrorString(ce) + ") but the eager replay succeeded");
+            }
             c->graph_kernels = g_launch_counter - before;
             ck(cudaGraphInstantiate(&c->gexec, g, 0), "graph instantiate");
             cudaGraphDestroy(g);
@@ -403,6 +441,10 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         set_device(c);
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream create");
         configure_kernels();
+        cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->opt.device);
+        const char* dbg = std::getenv("ANN_DEBUG");
+        c->debug = dbg && dbg[0] == '1';
+        if (c->debug) c->opt.use_graphs = 0;
     } catch (ann_error& e) {
         delete c;
         return fail(nullptr, e.code, e.what());
@@ -634,29 +676,32 @@ static void download_real_rows(ann_ctx* c, DevBuf& b, double* out, size_t n) {
         for (size_t k = 0; k < n; ++k) out[k] = h[k];
     }
 }
-int ann_get_symm(ann_ctx* c, double* G) {
+int ann_get_symm(ann_ctx* c, double* G, int64_t cap) {
     if (!c || !G) return fail(c, ANN_ERR_ARG, "NULL argument");
     ANN_TRY(c, {
         set_device(c);
         if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        if (cap < (int64_t)c->N * c->pot.max_input()) throw ann_error(ANN_ERR_ARG, "output buffer too small");
         finish_batch(c);
         download_real_rows(c, c->G, G, (size_t)c->N * c->pot.max_input());
     })
 }
-int ann_get_dedg(ann_ctx* c, double* d) {
+int ann_get_dedg(ann_ctx* c, double* d, int64_t cap) {
     if (!c || !d) return fail(c, ANN_ERR_ARG, "NULL argument");
     ANN_TRY(c, {
         set_device(c);
         if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        if (cap < (int64_t)c->N * c->pot.max_input()) throw ann_error(ANN_ERR_ARG, "output buffer too small");
         finish_batch(c);
         download_real_rows(c, c->dEdG, d, (size_t)c->N * c->pot.max_input());
     })
 }
-int ann_get_atom_energies(ann_ctx* c, double* e) {
+int ann_get_atom_energies(ann_ctx* c, double* e, int64_t cap) {
     if (!c || !e) return fail(c, ANN_ERR_ARG, "NULL argument");
     ANN_TRY(c, {
         set_device(c);
         if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        if (cap < (int64_t)c->N) throw ann_error(ANN_ERR_ARG, "output buffer too small");
         finish_batch(c);
         if (c->N > 0) ck(cudaMemcpy(e, c->Eatom.p, sizeof(double) * c->N, cudaMemcpyDeviceToHost), "D2H");
     })

@@ -108,6 +108,16 @@ void launch_reduce_structures(int nstruc, const int32_t* off, const double* Eato
 void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st);
 size_t scan_tmp_ints(int n);
 
+// raise the dynamic shared-memory limit of a kernel to what the device allows beside its static
+// shared memory; returns the granted dynamic limit (0 on failure)
+template <typename K>
+inline int set_max_dynamic_smem(K kernel, int maxsmem) {
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) { cudaGetLastError(); return 0; }
+    const int dyn = maxsmem - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) { cudaGetLastError(); return 0; }
+    return dyn;
+}
 // raise the dynamic shared-memory limit of every kernel once (outside any graph capture)
 void configure_bp(int maxsmem);
 void configure_mlp(int maxsmem);

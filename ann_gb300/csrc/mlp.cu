@@ -290,10 +290,10 @@ void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream
     ++::ann::g_launch_counter, k_mlp_train<real><<<grid, MLP_T, smem, st>>>(pot, a, ld);
 }
 void configure_mlp(int maxsmem) {
-    cudaFuncSetAttribute(k_mlp_fb<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_mlp_fb<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_mlp_train<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_mlp_train<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+    set_max_dynamic_smem(k_mlp_fb<float>, maxsmem);
+    set_max_dynamic_smem(k_mlp_fb<double>, maxsmem);
+    set_max_dynamic_smem(k_mlp_train<float>, maxsmem);
+    set_max_dynamic_smem(k_mlp_train<double>, maxsmem);
 }
 size_t mlp_smem_bytes(const DevPot& pot, bool fp64, bool train) {
     const int ld = mlp_ld<float>(pot), L = mlp_maxL(pot);

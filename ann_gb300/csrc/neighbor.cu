@@ -28,10 +28,11 @@ static __device__ __forceinline__ void unpack3(int32_t p, int& a, int& b, int& c
 static __device__ __forceinline__ int floordiv(int a, int b) { int q = a / b; if ((a % b != 0) && ((a < 0) != (b < 0))) --q; return q; }
 
 // ---------------------------------------------------------------- per-structure geometry
-// one block; thread t handles structures t, t+blockDim...; bins per structure bounded by
-// 2*natoms+1 so that the bin arrays can be sized from the atom count alone.
-__global__ void k_struc_setup(NbrArgs a) {
-    __shared__ int32_t part[1024];
+// one block of SETUP_T threads, each owning a contiguous range of structures; bins per structure
+// bounded by 2*natoms+1 so that the bin arrays can be sized from the atom count alone.
+constexpr int SETUP_T = 256;
+__global__ void __launch_bounds__(SETUP_T) k_struc_setup(NbrArgs a) {
+    __shared__ int32_t part[SETUP_T];
     const int S = a.nstruc;
     const int per = (S + blockDim.x - 1) / blockDim.x;
     const int lo = threadIdx.x * per, hi = min(S, lo + per);
@@ -72,7 +73,7 @@ __global__ void k_struc_setup(NbrArgs a) {
     }
     part[threadIdx.x] = local;
     __syncthreads();
-    if (threadIdx.x == 0) {  // serial prefix over <=1024 partials
+    if (threadIdx.x == 0) {  // serial prefix over the SETUP_T partials
         int32_t run = 0;
         for (int t = 0; t < (int)blockDim.x; ++t) { const int32_t v = part[t]; part[t] = run; run += v; }
         *a.nbins_total = run;
@@ -285,7 +286,7 @@ __global__ void k_refresh(NbrArgs a) {
 }
 
 void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st) {
-    ++::ann::g_launch_counter, k_struc_setup<<<1, 1024, 0, st>>>(a);
+    ++::ann::g_launch_counter, k_struc_setup<<<1, SETUP_T, 0, st>>>(a);
     cudaMemsetAsync(a.bcount, 0, sizeof(int32_t) * (a.nbins_cap + 1), st);
     const int nb = (a.natoms + 255) / 256;
     if (a.natoms > 0) ++::ann::g_launch_counter, k_atom_bin<<<nb, 256, 0, st>>>(a);
@@ -303,8 +304,8 @@ void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st) {
 }
 
 void configure_nbr(int maxsmem) {
-    cudaFuncSetAttribute(k_neighbors<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
-    cudaFuncSetAttribute(k_neighbors<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsmem);
+    set_max_dynamic_smem(k_neighbors<true>, maxsmem);
+    set_max_dynamic_smem(k_neighbors<false>, maxsmem);
 }
 
 void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st) {

@@ -139,9 +139,10 @@ int ann_phase_times(ann_ctx* ctx, double* ms, int32_t n);
 /* ---- inspection (parity tests) -------------------------------------------------------------- */
 /* Max inputs over types: rows of ann_get_symm / ann_get_dedg are padded to this width.           */
 int ann_symm_width(ann_ctx* ctx, int32_t* width);
-int ann_get_symm(ann_ctx* ctx, double* symm /* N*width */);       /* NNP::symm of last batch     */
-int ann_get_dedg(ann_ctx* ctx, double* dedg /* N*width */);       /* dE_i/dG_i (DODZ::dodi row 0) */
-int ann_get_atom_energies(ann_ctx* ctx, double* e /* N */);
+/* The output capacities (in doubles) are checked against the last batch: N*width, N*width, N.  */
+int ann_get_symm(ann_ctx* ctx, double* symm, int64_t cap);        /* NNP::symm of last batch     */
+int ann_get_dedg(ann_ctx* ctx, double* dedg, int64_t cap);        /* dE_i/dG_i (DODZ::dodi row 0) */
+int ann_get_atom_energies(ann_ctx* ctx, double* e, int64_t cap);
 /* neighbour list of the last batch: total entries, then (i, j, image n0,n1,n2) per entry.        */
 int ann_num_neighbors(ann_ctx* ctx, int64_t* total);
 int ann_get_neighbors(ann_ctx* ctx, int32_t* i_out, int32_t* j_out, int32_t* img_out /* 3 per */,
