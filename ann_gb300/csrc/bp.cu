@@ -8,18 +8,22 @@
 // Per centre atom i (one warp):
 //  1. its neighbour row (type-sorted by the list builder) is staged into shared memory with a
 //     bulk asynchronous copy (cp.async.bulk + mbarrier), then compacted to d < rc and turned
-//     into per-neighbour quantities: unit vector, 1/d, cutoff f and f', and for every damping
-//     group g of the angular GAUSS functions D_g = f * exp(-d^2/eta_g^2) and its d-derivative.
-//  2. radial functions: lanes own functions, loop over the neighbours of each type block.
+//     into per-neighbour records: (unit vector, 1/d), d, cutoff f and f', and for every damping
+//     group g of the angular GAUSS functions D_g = f exp(-d^2/eta_g^2) and its d-derivative.
+//  2. radial functions: lanes own neighbours and keep the block's functions in registers
+//     (symmetry functions / tangents, then a transposing warp reduction), or own neighbours and
+//     loop over functions (force pass).
 //  3. angular functions: lanes own (j,k) triplets of each (J,K) type block. In the fast path
 //     (GAUSS, lambda=+-1, zeta=2^k) the reference's exp(-(rij^2+rik^2)/eta^2) factorises into
 //     D_g(j) D_g(k) and |1/2 +- cos/2|^zeta comes from a squaring chain, so no transcendental
-//     is evaluated per triplet. Per-slot sums are reduced across the warp by a transposing
-//     butterfly (each lane ends up owning one slot).
+//     is evaluated per triplet.
 //  4. force pass: per triplet the vectors v_j = -dE_i/dr_ij, v_k = -dE_i/dr_ik are added to
-//     per-neighbour shared-memory accumulators; F_i = sum_j v_j, F_j -= v_j (Newton's third law,
-//     nnp.cpp:491,509-516) and the virial W += r_ij (x) v_j are then formed once per neighbour.
+//     per-neighbour shared-memory accumulators; the triplets are visited along diagonals
+//     (k - j constant within a warp step), so the 32 lanes of a step hit 32 different j and 32
+//     different k accumulators. F_i = sum_j v_j, F_j -= v_j (Newton's third law,
+//     nnp.cpp:491,509-516) and the virial W += r_ij (x) v_j are formed once per neighbour.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include "dev_math.cuh"
 #include "kernels.hpp"
@@ -28,7 +32,7 @@ namespace ann {
 
 enum { PASS_SYMM = 0, PASS_FORCE = 1, PASS_JVP = 2 };
 constexpr int BP_WARPS = 4;
-constexpr int GEN_CHUNK = 16;
+constexpr int CHUNK = 16;   // functions per register chunk (radial and generic angular)
 
 // ---------------------------------------------------------------- PTX helpers (bulk copy + mbarrier)
 static __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -72,6 +76,7 @@ __device__ __forceinline__ real warp_slot_reduce(real (&v)[S], int lane) {
     for (int off = (16 >> LOGS); off >= 1; off >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
     return v[0];
 }
+template <int S> struct SlotShift { static constexpr int v = (S == 8) ? 2 : (S == 16) ? 1 : (S == 32) ? 0 : 3; };
 template <typename real>
 __device__ __forceinline__ real warp_sum(real v) {
 #pragma unroll
@@ -80,59 +85,106 @@ __device__ __forceinline__ real warp_sum(real v) {
 }
 
 // ---------------------------------------------------------------- triplet enumeration
-struct TriIter {      // pairs j<k of [0,n) in row-major order, lane-strided by 32
+// pairs j<k of [0,n), lane-strided by 32. ROWS: row-major (row j, then k) -- the warp shares j.
+// otherwise diagonal-major (k-j fixed, then j) -- every lane has a different j and k.
+template <bool ROWS>
+struct TriIter {
     int r, c, len;
     __device__ __forceinline__ void init(int n, int t) { r = 0; len = n - 1; c = t; while (len > 0 && c >= len) { c -= len; ++r; --len; } }
     __device__ __forceinline__ void adv() { c += 32; while (len > 0 && c >= len) { c -= len; ++r; --len; } }
-    __device__ __forceinline__ int j() const { return r; }
-    __device__ __forceinline__ int k() const { return r + 1 + c; }
+    __device__ __forceinline__ int j() const { return ROWS ? r : c; }
+    __device__ __forceinline__ int k() const { return ROWS ? r + 1 + c : c + r + 1; }
 };
-struct RectIter {     // pairs (q, c) of [0,nJ) x [0,nK), lane-strided by 32
-    int q, c, nK;
-    __device__ __forceinline__ void init(int nk, int t) { nK = nk; q = t / nk; c = t - q * nk; }
-    __device__ __forceinline__ void adv() { c += 32; while (c >= nK) { c -= nK; ++q; } }
+// pairs of [0,nJ) x [0,nK), lane-strided by 32. ROWS: row-major. otherwise rotated:
+// t -> (d = t / nJ, j = t % nJ, k = (j + d) mod nK), distinct j and k within a warp step.
+template <bool ROWS>
+struct RectIter {
+    int q, c, nJ, nK;
+    __device__ __forceinline__ void init(int nj, int nk, int t) {
+        nJ = nj; nK = nk;
+        if (ROWS) { q = t / nk; c = t - q * nk; }
+        else { const int d = t / nj; q = t - d * nj; c = (q + d) % nk; }
+    }
+    __device__ __forceinline__ void adv() {
+        if (ROWS) { c += 32; while (c >= nK) { c -= nK; ++q; } }
+        else {
+            q += 32; c += 32;
+            while (q >= nJ) { q -= nJ; c -= nJ - 1; }
+            while (c >= nK) c -= nK;
+            while (c < 0) c += nK;
+        }
+    }
 };
 
 // ---------------------------------------------------------------- shared-memory layout of one warp
-template <typename real, int NG>
+template <typename real, int NG, int PASS>
 struct WarpMem {
-    real *ux, *uy, *uz, *d, *id, *fc, *fcg, *D, *Dp, *ax, *ay, *az, *drx, *dry, *drz, *dd, *dE;
-    typename V4<real>::T* stage;
-    int32_t *jj, *img, *stagej;
+    typedef typename V4<real>::T R4;
+    R4* geo;             // (ux, uy, uz, 1/d)
+    real* dp;            // [e][2*NG]: D_0, Dp_0, D_1, Dp_1, ...
+    real *d, *fc, *fcg;
+    real *ax, *ay, *az;  // force accumulators (FORCE)
+    R4* tg;              // tangent of the pair vector (drx, dry, drz, dd) (JVP)
+    real* dE;            // dE/dG row (FORCE)
+    R4* stage;
+    int32_t *stagej, *jj, *img;
     uint64_t* bar;
-    static __host__ __device__ size_t bytes(int cap, int imax) {
-        size_t r = (size_t)(7 + 2 * NG + 3 + 4) * cap + (size_t)imax;
-        size_t b = ((r * sizeof(real) + 31) / 32) * 32;
-        b += (size_t)cap * sizeof(typename V4<real>::T);
-        b += (size_t)3 * cap * sizeof(int32_t);
-        b = ((b + 15) / 16) * 16 + 16;
-        return ((b + 31) / 32) * 32;
+    static constexpr int NDP = 2 * NG;
+    static __host__ __device__ size_t align(size_t x, size_t a) { return (x + a - 1) / a * a; }
+    static __host__ __device__ size_t layout(int cap, int imax, WarpMem* w, unsigned char* base) {
+        size_t off = 0;
+        auto take = [&](size_t bytes, size_t al) { off = align(off, al); const size_t o = off; off += bytes; return o; };
+        const size_t o_geo = take(sizeof(R4) * cap, 32);
+        const size_t o_stage = take(sizeof(R4) * cap, 32);
+        const size_t o_tg = (PASS == PASS_JVP) ? take(sizeof(R4) * cap, 32) : 0;
+        const size_t o_dp = take(sizeof(real) * NDP * cap, 16);
+        const size_t o_d = take(sizeof(real) * cap, 16), o_fc = take(sizeof(real) * cap, 16), o_fcg = take(sizeof(real) * cap, 16);
+        size_t o_ax = 0, o_ay = 0, o_az = 0, o_dE = 0, o_jj = 0, o_img = 0;
+        if (PASS == PASS_FORCE) {
+            o_ax = take(sizeof(real) * cap, 16); o_ay = take(sizeof(real) * cap, 16); o_az = take(sizeof(real) * cap, 16);
+            o_dE = take(sizeof(real) * imax, 16);
+            o_jj = take(sizeof(int32_t) * cap, 16); o_img = take(sizeof(int32_t) * cap, 16);
+        }
+        const size_t o_sj = take(sizeof(int32_t) * cap, 16);
+        const size_t o_bar = take(16, 16);
+        if (w) {
+            w->geo = reinterpret_cast<R4*>(base + o_geo); w->stage = reinterpret_cast<R4*>(base + o_stage);
+            w->tg = reinterpret_cast<R4*>(base + o_tg); w->dp = reinterpret_cast<real*>(base + o_dp);
+            w->d = reinterpret_cast<real*>(base + o_d); w->fc = reinterpret_cast<real*>(base + o_fc); w->fcg = reinterpret_cast<real*>(base + o_fcg);
+            w->ax = reinterpret_cast<real*>(base + o_ax); w->ay = reinterpret_cast<real*>(base + o_ay); w->az = reinterpret_cast<real*>(base + o_az);
+            w->dE = reinterpret_cast<real*>(base + o_dE);
+            w->jj = reinterpret_cast<int32_t*>(base + o_jj); w->img = reinterpret_cast<int32_t*>(base + o_img);
+            w->stagej = reinterpret_cast<int32_t*>(base + o_sj);
+            w->bar = reinterpret_cast<uint64_t*>(base + o_bar);
+        }
+        return align(off, 128);
     }
-    __device__ void carve(unsigned char* base, int cap, int imax) {
-        real* p = reinterpret_cast<real*>(base);
-        ux = p; p += cap; uy = p; p += cap; uz = p; p += cap; d = p; p += cap; id = p; p += cap; fc = p; p += cap; fcg = p; p += cap;
-        D = p; p += NG * cap; Dp = p; p += NG * cap; ax = p; p += cap; ay = p; p += cap; az = p; p += cap;
-        drx = p; p += cap; dry = p; p += cap; drz = p; p += cap; dd = p; p += cap; dE = p; p += imax;
-        size_t off = (size_t)(7 + 2 * NG + 3 + 4) * cap + (size_t)imax;
-        off = ((off * sizeof(real) + 31) / 32) * 32;
-        stage = reinterpret_cast<typename V4<real>::T*>(base + off);
-        off += (size_t)cap * sizeof(typename V4<real>::T);
-        jj = reinterpret_cast<int32_t*>(base + off); img = jj + cap; stagej = img + cap;
-        off += (size_t)3 * cap * sizeof(int32_t);
-        off = ((off + 15) / 16) * 16;
-        bar = reinterpret_cast<uint64_t*>(base + off);
+    static __host__ __device__ size_t bytes(int cap, int imax) { return layout(cap, imax, nullptr, nullptr); }
+};
+
+// D/Dp pairs of one neighbour for the fast path
+template <typename real, int NG>
+struct DampRec {
+    real v[2 * NG];
+    __device__ __forceinline__ void load(const real* p) {
+#pragma unroll
+        for (int q = 0; q < 2 * NG; ++q) v[q] = p[q];
     }
+    __device__ __forceinline__ real D(int g) const { return v[2 * g]; }
+    __device__ __forceinline__ real Dp(int g) const { return v[2 * g + 1]; }
 };
 
 // ---------------------------------------------------------------- the kernel
 template <typename real, int NG, bool FAST, int PASS>
 __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
+    typedef typename V4<real>::T R4;
     extern __shared__ __align__(128) unsigned char bsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int cap = a.cap, imax = pot.imax, T = a.ntypes;
-    const size_t wbytes = WarpMem<real, NG>::bytes(cap, imax);
-    WarpMem<real, NG> w;
-    w.carve(bsm + (size_t)wid * wbytes, cap, imax);
+    const size_t wbytes = WarpMem<real, NG, PASS>::bytes(cap, imax);
+    WarpMem<real, NG, PASS> w;
+    WarpMem<real, NG, PASS>::layout(cap, imax, &w, bsm + (size_t)wid * wbytes);
+    constexpr int NDP = 2 * NG;
     if (lane == 0) mbar_init(w.bar, 1);
     __syncwarp();
     uint32_t phase = 0;
@@ -153,11 +205,11 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
         // ---- 1. stage the neighbour row (bulk async copy) -----------------------------------
         if (nin > 0) {
             if (lane == 0) {
-                const uint32_t b1 = (uint32_t)(nin * sizeof(typename V4<real>::T));
+                const uint32_t b1 = (uint32_t)(nin * sizeof(R4));
                 const uint32_t b2 = (uint32_t)(((nin + 3) / 4) * 16);
                 fence_proxy_async();
                 mbar_expect_tx(w.bar, b1 + b2);
-                bulk_g2s(w.stage, reinterpret_cast<const typename V4<real>::T*>(a.nr) + row, b1, w.bar);
+                bulk_g2s(w.stage, reinterpret_cast<const R4*>(a.nr) + row, b1, w.bar);
                 bulk_g2s(w.stagej, a.nj + row, b2, w.bar);
             }
             bool done = false;
@@ -169,8 +221,11 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
             }
             phase ^= 1u;
         }
-        // ---- compaction to d < rc, per-type active ranges ---------------------------------------
+        // ---- compaction to d < rc, per-type active ranges, per-neighbour records ---------------
         const real rc = (real)TT.rc;
+        real ie2[NG];
+#pragma unroll
+        for (int q = 0; q < NG; ++q) ie2[q] = (real)TT.ietar2[q];
         int tstart[MAXT], tcnt[MAXT];
         int pos = 0, base_in = 0;
         for (int t = 0; t < T; ++t) {
@@ -179,29 +234,29 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
             for (int e0 = 0; e0 < cin; e0 += 32) {
                 const int e = base_in + e0 + lane;
                 bool keep = false;
-                typename V4<real>::T r4;
+                R4 r4;
                 if (e0 + lane < cin && e < nin) { r4 = w.stage[e]; keep = r4.w < rc; }
                 const unsigned msk = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
                     const int o = pos + __popc(msk & lt);
                     const real dd = r4.w, idd = real(1) / dd;
-                    w.ux[o] = r4.x * idd; w.uy[o] = r4.y * idd; w.uz[o] = r4.z * idd;
-                    w.d[o] = dd; w.id[o] = idd;
+                    R4 g4; g4.x = r4.x * idd; g4.y = r4.y * idd; g4.z = r4.z * idd; g4.w = idd;
+                    w.geo[o] = g4;
+                    w.d[o] = dd;
                     real f, g;
                     cutoff_fg<real>(TT.cut, rc, dd, f, g);
                     w.fc[o] = f; w.fcg[o] = g;
                     if (FAST) {
 #pragma unroll
                         for (int q = 0; q < NG; ++q) {
-                            const real ie2 = (real)TT.ietar2[q];
-                            const real ex = M<real>::bexp(-dd * dd * ie2);
-                            w.D[q * cap + o] = f * ex;
-                            w.Dp[q * cap + o] = ex * (g - real(2) * dd * f * ie2);
+                            const real ex = M<real>::bexp(-dd * dd * ie2[q]);
+                            w.dp[o * NDP + 2 * q] = f * ex;
+                            w.dp[o * NDP + 2 * q + 1] = ex * (g - real(2) * dd * f * ie2[q]);
                         }
                     }
                     const int j = w.stagej[e];
-                    w.jj[o] = j;
                     if (PASS == PASS_FORCE) {
+                        w.jj[o] = j;
                         w.ax[o] = real(0); w.ay[o] = real(0); w.az[o] = real(0);
                         w.img[o] = a.newton_untranslated ? a.nimg[row + e] : 0;
                     }
@@ -209,8 +264,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         const real lx = a.lam[3 * (size_t)i] - a.lam[3 * (size_t)j];
                         const real ly = a.lam[3 * (size_t)i + 1] - a.lam[3 * (size_t)j + 1];
                         const real lz = a.lam[3 * (size_t)i + 2] - a.lam[3 * (size_t)j + 2];
-                        w.drx[o] = lx; w.dry[o] = ly; w.drz[o] = lz;
-                        w.dd[o] = w.ux[o] * lx + w.uy[o] * ly + w.uz[o] * lz;
+                        R4 t4; t4.x = lx; t4.y = ly; t4.z = lz; t4.w = g4.x * lx + g4.y * ly + g4.z * lz;
+                        w.tg[o] = t4;
                     }
                 }
                 pos += __popc(msk);
@@ -239,20 +294,35 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         radial_vd<real>(R.name, a.prm.reta[R.pidx + m], a.prm.rs[R.pidx + m], dd, f, g, val, der);
                         amp -= w.dE[R.off + m] * der;
                     }
-                    w.ax[e] += amp * w.ux[e]; w.ay[e] += amp * w.uy[e]; w.az[e] += amp * w.uz[e];
+                    const R4 g4 = w.geo[e];
+                    w.ax[e] += amp * g4.x; w.ay[e] += amp * g4.y; w.az[e] += amp * g4.z;
                 }
             } else {
-                for (int m0 = 0; m0 < R.n; m0 += 32) {
-                    const int m = m0 + lane;
-                    if (m < R.n) {
-                        const real eta = a.prm.reta[R.pidx + m], rs = a.prm.rs[R.pidx + m];
-                        real acc = real(0);
-                        for (int e = e0; e < e1; ++e) {
-                            real val, der;
-                            radial_vd<real>(R.name, eta, rs, w.d[e], w.fc[e], w.fcg[e], val, der);
-                            acc += (PASS == PASS_SYMM) ? val : der * w.dd[e];
+                for (int m0 = 0; m0 < R.n; m0 += CHUNK) {
+                    real eta[CHUNK], rs[CHUNK], acc[CHUNK];
+#pragma unroll
+                    for (int s = 0; s < CHUNK; ++s) {
+                        const bool ok = m0 + s < R.n;
+                        eta[s] = ok ? a.prm.reta[R.pidx + m0 + s] : real(0);
+                        rs[s] = ok ? a.prm.rs[R.pidx + m0 + s] : real(0);
+                        acc[s] = real(0);
+                    }
+                    for (int e = e0 + lane; e < e1; e += 32) {
+                        const real dd = w.d[e], f = w.fc[e], g = w.fcg[e];
+                        const real tdd = (PASS == PASS_JVP) ? w.tg[e].w : real(0);
+#pragma unroll
+                        for (int s = 0; s < CHUNK; ++s) {
+                            if (m0 + s < R.n) {
+                                real val, der;
+                                radial_vd<real>(R.name, eta[s], rs[s], dd, f, g, val, der);
+                                acc[s] += (PASS == PASS_SYMM) ? val : der * tdd;
+                            }
                         }
-                        Gout[R.off + m] = acc;
+                    }
+                    const real v = warp_slot_reduce<real, CHUNK>(acc, lane);
+                    if ((lane & 1) == 0) {
+                        const int m = m0 + ((lane >> 1) & (CHUNK - 1));
+                        if (m < R.n) Gout[R.off + m] = v;
                     }
                 }
             }
@@ -267,6 +337,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 if (A.n == 0) continue;
                 const int nJ = tcnt[J], nK = tcnt[K], aJ = tstart[J], aK = tstart[K];
                 const int total = (J == K) ? nJ * (nJ - 1) / 2 : nJ * nK;
+                constexpr bool ROWS = (PASS != PASS_FORCE);
                 if (FAST) {
                     // ------------------------------------------------ fast path (GAUSS, zeta=2^k)
                     real acc[S];
@@ -282,15 +353,16 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                             cB[s] = dv * real(1 << k) * ((s & 1) ? real(-0.5) : real(0.5));
                         }
                     }
-                    TriIter ti; RectIter ri;
-                    if (J == K) ti.init(nJ, lane); else ri.init(max(nK, 1), lane);
+                    TriIter<ROWS> ti; RectIter<ROWS> ri;
+                    if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane);
                     for (int t = lane; t < total; t += 32) {
                         int j, k;
                         if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
                         else { j = aJ + ri.q; k = aK + ri.c; ri.adv(); }
-                        const real ujx = w.ux[j], ujy = w.uy[j], ujz = w.uz[j];
-                        const real ukx = w.ux[k], uky = w.uy[k], ukz = w.uz[k];
-                        const real cs = ujx * ukx + ujy * uky + ujz * ukz;
+                        const R4 gj = w.geo[j], gk = w.geo[k];
+                        DampRec<real, NG> dj, dk;
+                        dj.load(w.dp + j * NDP); dk.load(w.dp + k * NDP);
+                        const real cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
                         const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
                         real pp[4], pm[4];
                         pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
@@ -298,7 +370,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         if (PASS == PASS_SYMM) {
 #pragma unroll
                             for (int g = 0; g < NG; ++g) {
-                                const real DD = w.D[g * cap + j] * w.D[g * cap + k];
+                                const real DD = dj.D(g) * dk.D(g);
 #pragma unroll
                                 for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
                             }
@@ -316,26 +388,24 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                                         Ag += cA[g * 8 + 2 * q] * pp[q] + cA[g * 8 + 2 * q + 1] * pm[q];
                                         Bg += cB[g * 8 + 2 * q] * qp[q] + cB[g * 8 + 2 * q + 1] * qm[q];
                                     }
-                                    const real Dj = w.D[g * cap + j], Dk = w.D[g * cap + k];
-                                    phi -= Bg * Dj * Dk;
-                                    e0 -= Ag * w.Dp[g * cap + j] * Dk;
-                                    e1 -= Ag * Dj * w.Dp[g * cap + k];
+                                    phi -= Bg * dj.D(g) * dk.D(g);
+                                    e0 -= Ag * dj.Dp(g) * dk.D(g);
+                                    e1 -= Ag * dj.D(g) * dk.Dp(g);
                                 }
-                                const real idj = w.id[j], idk = w.id[k];
+                                const real idj = gj.w, idk = gk.w;
                                 const real cj = -phi * cs * idj + e0, bj = phi * idj;
                                 const real ck = -phi * cs * idk + e1, bk = phi * idk;
-                                atomicAdd(&w.ax[j], cj * ujx + bj * ukx); atomicAdd(&w.ay[j], cj * ujy + bj * uky); atomicAdd(&w.az[j], cj * ujz + bj * ukz);
-                                atomicAdd(&w.ax[k], ck * ukx + bk * ujx); atomicAdd(&w.ay[k], ck * uky + bk * ujy); atomicAdd(&w.az[k], ck * ukz + bk * ujz);
+                                atomicAdd(&w.ax[j], cj * gj.x + bj * gk.x); atomicAdd(&w.ay[j], cj * gj.y + bj * gk.y); atomicAdd(&w.az[j], cj * gj.z + bj * gk.z);
+                                atomicAdd(&w.ax[k], ck * gk.x + bk * gj.x); atomicAdd(&w.ay[k], ck * gk.y + bk * gj.y); atomicAdd(&w.az[k], ck * gk.z + bk * gj.z);
                             } else {  // PASS_JVP
-                                const real idj = w.id[j], idk = w.id[k];
-                                const real ddj = w.dd[j], ddk = w.dd[k];
-                                const real dcos = (w.drx[j] * ukx + w.dry[j] * uky + w.drz[j] * ukz) * idj +
-                                                  (w.drx[k] * ujx + w.dry[k] * ujy + w.drz[k] * ujz) * idk - cs * (ddj * idj + ddk * idk);
+                                const R4 tj = w.tg[j], tk = w.tg[k];
+                                const real idj = gj.w, idk = gk.w;
+                                const real dcos = (tj.x * gk.x + tj.y * gk.y + tj.z * gk.z) * idj +
+                                                  (tk.x * gj.x + tk.y * gj.y + tk.z * gj.z) * idk - cs * (tj.w * idj + tk.w * idk);
 #pragma unroll
                                 for (int g = 0; g < NG; ++g) {
-                                    const real Dj = w.D[g * cap + j], Dk = w.D[g * cap + k];
-                                    const real DD = Dj * Dk;
-                                    const real dDD = w.Dp[g * cap + j] * Dk * ddj + Dj * w.Dp[g * cap + k] * ddk;
+                                    const real DD = dj.D(g) * dk.D(g);
+                                    const real dDD = dj.Dp(g) * dk.D(g) * tj.w + dj.D(g) * dk.Dp(g) * tk.w;
 #pragma unroll
                                     for (int q = 0; q < 4; ++q) {
                                         const real z = real(1 << q);
@@ -348,7 +418,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                     }
                     if (PASS != PASS_FORCE) {
                         const real v = warp_slot_reduce<real, S>(acc, lane);
-                        constexpr int SH = (S == 8) ? 2 : (S == 16) ? 1 : 0;
+                        constexpr int SH = SlotShift<S>::v;
                         if ((lane & ((1 << SH) - 1)) == 0) {
                             const int s = (lane >> SH) & (S - 1);
                             const int ref = a.prm.slot2ref[A.sidx + s];
@@ -358,72 +428,71 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 } else {
                     // ------------------------------------------------ generic path (any BasisA)
                     if (PASS == PASS_FORCE) {
-                        TriIter ti; RectIter ri;
-                        if (J == K) ti.init(nJ, lane); else ri.init(max(nK, 1), lane);
+                        TriIter<false> ti; RectIter<false> ri;
+                        if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane);
                         for (int t = lane; t < total; t += 32) {
                             int j, k;
                             if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
                             else { j = aJ + ri.q; k = aK + ri.c; ri.adv(); }
-                            const real ujx = w.ux[j], ujy = w.uy[j], ujz = w.uz[j];
-                            const real ukx = w.ux[k], uky = w.uy[k], ukz = w.uz[k];
-                            const real cs = ujx * ukx + ujy * uky + ujz * ukz;
+                            const R4 gj = w.geo[j], gk = w.geo[k];
+                            const real cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
                             const real dj = w.d[j], dk = w.d[k];
                             const real r2s = dj * dj + dk * dk;
-                            const real fj = w.fc[j], fk = w.fc[k], gj = w.fcg[j], gk = w.fcg[k];
+                            const real fj = w.fc[j], fk = w.fc[k], gjj = w.fcg[j], gkk = w.fcg[k];
                             real phi = real(0), e0 = real(0), e1 = real(0);
                             for (int m = 0; m < A.n; ++m) {
                                 const real eta = a.prm.aeta[A.pidx + m], zeta = a.prm.zeta[A.pidx + m];
                                 const real lf = real(0.5) * a.prm.alam[A.pidx + m];
-                                const real ie2 = real(1) / (eta * eta);
+                                const real iex = real(1) / (eta * eta);
                                 real h, dq;
-                                angular_damp<real>(A.name, ie2, r2s, h, dq);
+                                angular_damp<real>(A.name, iex, r2s, h, dq);
                                 const real cw = fabs(real(0.5) + lf * cs);
                                 const real ga = w.dE[A.off + m] * M<real>::pow(cw, zeta - real(1)) * h;
                                 const real fa = cw * ga;
                                 phi -= zeta * lf * ga;
-                                e0 -= fa * (-dq * real(2) * dj * fj + gj);
-                                e1 -= fa * (-dq * real(2) * dk * fk + gk);
+                                e0 -= fa * (-dq * real(2) * dj * fj + gjj);
+                                e1 -= fa * (-dq * real(2) * dk * fk + gkk);
                             }
                             phi *= fj * fk; e0 *= fk; e1 *= fj;
-                            const real idj = w.id[j], idk = w.id[k];
+                            const real idj = gj.w, idk = gk.w;
                             const real cj = -phi * cs * idj + e0, bj = phi * idj;
                             const real ck = -phi * cs * idk + e1, bk = phi * idk;
-                            atomicAdd(&w.ax[j], cj * ujx + bj * ukx); atomicAdd(&w.ay[j], cj * ujy + bj * uky); atomicAdd(&w.az[j], cj * ujz + bj * ukz);
-                            atomicAdd(&w.ax[k], ck * ukx + bk * ujx); atomicAdd(&w.ay[k], ck * uky + bk * ujy); atomicAdd(&w.az[k], ck * ukz + bk * ujz);
+                            atomicAdd(&w.ax[j], cj * gj.x + bj * gk.x); atomicAdd(&w.ay[j], cj * gj.y + bj * gk.y); atomicAdd(&w.az[j], cj * gj.z + bj * gk.z);
+                            atomicAdd(&w.ax[k], ck * gk.x + bk * gj.x); atomicAdd(&w.ay[k], ck * gk.y + bk * gj.y); atomicAdd(&w.az[k], ck * gk.z + bk * gj.z);
                         }
                     } else {
-                        for (int m0 = 0; m0 < A.n; m0 += GEN_CHUNK) {
-                            real acc[GEN_CHUNK];
+                        for (int m0 = 0; m0 < A.n; m0 += CHUNK) {
+                            real acc[CHUNK];
 #pragma unroll
-                            for (int s = 0; s < GEN_CHUNK; ++s) acc[s] = real(0);
-                            TriIter ti; RectIter ri;
-                            if (J == K) ti.init(nJ, lane); else ri.init(max(nK, 1), lane);
+                            for (int s = 0; s < CHUNK; ++s) acc[s] = real(0);
+                            TriIter<true> ti; RectIter<true> ri;
+                            if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane);
                             for (int t = lane; t < total; t += 32) {
                                 int j, k;
                                 if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
                                 else { j = aJ + ri.q; k = aK + ri.c; ri.adv(); }
-                                const real ujx = w.ux[j], ujy = w.uy[j], ujz = w.uz[j];
-                                const real ukx = w.ux[k], uky = w.uy[k], ukz = w.uz[k];
-                                const real cs = ujx * ukx + ujy * uky + ujz * ukz;
+                                const R4 gj = w.geo[j], gk = w.geo[k];
+                                const real cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
                                 const real dj = w.d[j], dk = w.d[k];
                                 const real r2s = dj * dj + dk * dk;
-                                const real fj = w.fc[j], fk = w.fc[k], gj = w.fcg[j], gk = w.fcg[k];
+                                const real fj = w.fc[j], fk = w.fc[k], gjj = w.fcg[j], gkk = w.fcg[k];
                                 real dcos = real(0), ddj = real(0), ddk = real(0);
                                 if (PASS == PASS_JVP) {
-                                    const real idj = w.id[j], idk = w.id[k];
-                                    ddj = w.dd[j]; ddk = w.dd[k];
-                                    dcos = (w.drx[j] * ukx + w.dry[j] * uky + w.drz[j] * ukz) * idj +
-                                           (w.drx[k] * ujx + w.dry[k] * ujy + w.drz[k] * ujz) * idk - cs * (ddj * idj + ddk * idk);
+                                    const R4 tj = w.tg[j], tk = w.tg[k];
+                                    const real idj = gj.w, idk = gk.w;
+                                    ddj = tj.w; ddk = tk.w;
+                                    dcos = (tj.x * gk.x + tj.y * gk.y + tj.z * gk.z) * idj + (tk.x * gj.x + tk.y * gj.y + tk.z * gj.z) * idk -
+                                           cs * (ddj * idj + ddk * idk);
                                 }
 #pragma unroll
-                                for (int s = 0; s < GEN_CHUNK; ++s) {
+                                for (int s = 0; s < CHUNK; ++s) {
                                     const int m = m0 + s;
                                     if (m < A.n) {
                                         const real eta = a.prm.aeta[A.pidx + m], zeta = a.prm.zeta[A.pidx + m];
                                         const real lf = real(0.5) * a.prm.alam[A.pidx + m];
-                                        const real ie2 = real(1) / (eta * eta);
+                                        const real iex = real(1) / (eta * eta);
                                         real h, dq;
-                                        angular_damp<real>(A.name, ie2, r2s, h, dq);
+                                        angular_damp<real>(A.name, iex, r2s, h, dq);
                                         const real cw = fabs(real(0.5) + lf * cs);
                                         if (PASS == PASS_SYMM) {
                                             acc[s] += M<real>::pow(cw, zeta) * h * fj * fk;
@@ -431,16 +500,16 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                                             const real ga = M<real>::pow(cw, zeta - real(1)) * h;
                                             const real fa = cw * ga;
                                             const real fphi = zeta * lf * ga * fj * fk;
-                                            const real fe0 = fa * (-dq * real(2) * dj * fj + gj) * fk;
-                                            const real fe1 = fa * (-dq * real(2) * dk * fk + gk) * fj;
+                                            const real fe0 = fa * (-dq * real(2) * dj * fj + gjj) * fk;
+                                            const real fe1 = fa * (-dq * real(2) * dk * fk + gkk) * fj;
                                             acc[s] += fphi * dcos + fe0 * ddj + fe1 * ddk;
                                         }
                                     }
                                 }
                             }
-                            const real v = warp_slot_reduce<real, GEN_CHUNK>(acc, lane);
+                            const real v = warp_slot_reduce<real, CHUNK>(acc, lane);
                             if ((lane & 1) == 0) {
-                                const int m = m0 + ((lane >> 1) & (GEN_CHUNK - 1));
+                                const int m = m0 + ((lane >> 1) & (CHUNK - 1));
                                 if (m < A.n) Gout[A.off + m] = v;
                             }
                         }
@@ -459,7 +528,9 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
             for (int e = lane; e < pos; e += 32) {
                 const real vx = w.ax[e], vy = w.ay[e], vz = w.az[e];
                 fx += vx; fy += vy; fz += vz;
-                const real rx = w.ux[e] * w.d[e], ry = w.uy[e] * w.d[e], rz = w.uz[e] * w.d[e];
+                const R4 g4 = w.geo[e];
+                const real dd = w.d[e];
+                const real rx = g4.x * dd, ry = g4.y * dd, rz = g4.z * dd;
                 W9[0] += rx * vx; W9[1] += rx * vy; W9[2] += rx * vz;
                 W9[3] += ry * vx; W9[4] += ry * vy; W9[5] += ry * vz;
                 W9[6] += rz * vx; W9[7] += rz * vy; W9[8] += rz * vz;
@@ -477,7 +548,6 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 for (int q = 0; q < 9; ++q) a.W[9 * (size_t)i + q] = W9[q];
             }
         }
-        // symmetry functions of angular blocks with no triplets stay as written by the zero fill
         __syncwarp();
     }
 }
@@ -496,18 +566,20 @@ static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t s
         ++::ann::g_launch_counter, k_zero<real><<<1024, 256, 0, st>>>(out, (size_t)a.natoms * pot.imax);
     }
     cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), st);
-    int grid = (a.natoms + BP_WARPS - 1) / BP_WARPS;
-    grid = std::min(grid, 152 * 16);
     auto go = [&](auto kern, size_t wb) {
         const size_t smem = wb * BP_WARPS;
+        int per_sm = (int)std::max<size_t>(1, (size_t)(227 * 1024) / std::max<size_t>(smem, 1));
+        per_sm = std::min(per_sm, 16);
+        int grid = (a.natoms + BP_WARPS - 1) / BP_WARPS;
+        grid = std::min(grid, 152 * per_sm);
         ++::ann::g_launch_counter, kern<<<grid, BP_WARPS * 32, smem, st>>>(pot, a);
     };
     if (pot.fast) {
-        if (pot.fastNG == 1) go(k_bp<real, 1, true, PASS>, WarpMem<real, 1>::bytes(a.cap, pot.imax));
-        else if (pot.fastNG == 2) go(k_bp<real, 2, true, PASS>, WarpMem<real, 2>::bytes(a.cap, pot.imax));
-        else go(k_bp<real, 4, true, PASS>, WarpMem<real, 4>::bytes(a.cap, pot.imax));
+        if (pot.fastNG == 1) go(k_bp<real, 1, true, PASS>, WarpMem<real, 1, PASS>::bytes(a.cap, pot.imax));
+        else if (pot.fastNG == 2) go(k_bp<real, 2, true, PASS>, WarpMem<real, 2, PASS>::bytes(a.cap, pot.imax));
+        else go(k_bp<real, 4, true, PASS>, WarpMem<real, 4, PASS>::bytes(a.cap, pot.imax));
     } else {
-        go(k_bp<real, 1, false, PASS>, WarpMem<real, 1>::bytes(a.cap, pot.imax));
+        go(k_bp<real, 1, false, PASS>, WarpMem<real, 1, PASS>::bytes(a.cap, pot.imax));
     }
 }
 
@@ -522,11 +594,14 @@ void configure_bp(int maxsmem) {
     configure_pass<float, PASS_SYMM>(maxsmem); configure_pass<float, PASS_FORCE>(maxsmem); configure_pass<float, PASS_JVP>(maxsmem);
     configure_pass<double, PASS_SYMM>(maxsmem); configure_pass<double, PASS_FORCE>(maxsmem); configure_pass<double, PASS_JVP>(maxsmem);
 }
+// the largest per-block shared memory any pass needs for this potential and capacity
 size_t bp_smem_bytes(const DevPot& pot, int cap, bool fp64) {
     const int ng = pot.fast ? pot.fastNG : 1;
     auto b = [&](auto tag) -> size_t {
         using real = decltype(tag);
-        return ng == 1 ? WarpMem<real, 1>::bytes(cap, pot.imax) : ng == 2 ? WarpMem<real, 2>::bytes(cap, pot.imax) : WarpMem<real, 4>::bytes(cap, pot.imax);
+        if (ng == 1) return std::max({WarpMem<real, 1, PASS_SYMM>::bytes(cap, pot.imax), WarpMem<real, 1, PASS_FORCE>::bytes(cap, pot.imax), WarpMem<real, 1, PASS_JVP>::bytes(cap, pot.imax)});
+        if (ng == 2) return std::max({WarpMem<real, 2, PASS_SYMM>::bytes(cap, pot.imax), WarpMem<real, 2, PASS_FORCE>::bytes(cap, pot.imax), WarpMem<real, 2, PASS_JVP>::bytes(cap, pot.imax)});
+        return std::max({WarpMem<real, 4, PASS_SYMM>::bytes(cap, pot.imax), WarpMem<real, 4, PASS_FORCE>::bytes(cap, pot.imax), WarpMem<real, 4, PASS_JVP>::bytes(cap, pot.imax)});
     };
     return (fp64 ? b(double()) : b(float())) * BP_WARPS;
 }

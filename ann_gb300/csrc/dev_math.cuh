@@ -81,7 +81,8 @@ template <> struct M<double> {
 template <> struct M<float> {
     static __device__ __forceinline__ float bexp(float x) { return __expf(x); }
     static __device__ __forceinline__ float exp(float x) { return __expf(x); }
-    static __device__ __forceinline__ float pow(float x, float y) { return __powf(x, y); }
+    // x >= 0 here; pow(x, 0) = 1 also for x = 0 (as std::pow), where exp2(0 * log2(0)) is NaN
+    static __device__ __forceinline__ float pow(float x, float y) { return (y == 0.0f) ? 1.0f : __powf(x, y); }
     static __device__ __forceinline__ float tanh(float x) { return ::tanhf(x); }
     static __device__ __forceinline__ float log1p(float x) { return ::log1pf(x); }
     static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }

@@ -145,10 +145,11 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_fb(const __grid_constant__ DevPot
     }
     layer_bwd<real>(A.prm.wt + net.woff[0], net.nodes[0], nin, x, y, ld);
     __syncthreads();
-    for (int idx = threadIdx.x; idx < TA * nin; idx += MLP_T) {
-        const int a = idx / nin, m = idx % nin;
+    // rows are padded to the widest type: inputs beyond this type's nInput read as zero
+    for (int idx = threadIdx.x; idx < TA * A.imax; idx += MLP_T) {
+        const int a = idx / A.imax, m = idx % A.imax;
         const int at = atoms[a];
-        if (at >= 0) A.dEdG[(size_t)at * A.imax + m] = y[a * ld + m] * inpw[m];
+        if (at >= 0) A.dEdG[(size_t)at * A.imax + m] = (m < nin) ? y[a * ld + m] * inpw[m] : real(0);
     }
 }
 

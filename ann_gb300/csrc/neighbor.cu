@@ -152,69 +152,151 @@ static __device__ __forceinline__ void pair_vec_d(const double* xi, const double
     d2 = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
 }
 
+// one candidate (j, image n) tested by one lane; accepted entries are compacted into the warp's
+// staging row with a ballot
 template <bool FP64>
-__global__ void __launch_bounds__(256) k_neighbors(NbrArgs a) {
+struct Cand {
+    int i, cap;
+    unsigned lt;
+    float4 xi4;
+    double xid[3];
+    float Rf[9];
+    float rc2f;
+    double rc2;
+    int mi0, mi1, mi2;
+    __device__ __forceinline__ void test(const NbrArgs& a, const StrucGeo& g, int c, bool valid, int k0, int k1, int k2,
+                                         int32_t* sj, int32_t* simg, int32_t* styp, int& cursor) const {
+        bool acc = false;
+        int j = 0, n0 = 0, n1 = 0, n2 = 0, tj = 0;
+        if (valid) {
+            j = a.bidx[c];
+            int mj0, mj1, mj2;
+            unpack3(a.bm[c], mj0, mj1, mj2);
+            n0 = k0 + mi0 - mj0; n1 = k1 + mi1 - mj1; n2 = k2 + mi2 - mj2;
+            const float4 pj = a.bpos4[c];
+            tj = __float_as_int(pj.w);
+            const float fn0 = (float)n0, fn1 = (float)n1, fn2 = (float)n2;
+            const float rx = (xi4.x - pj.x) - (fn0 * Rf[0] + fn1 * Rf[3] + fn2 * Rf[6]);
+            const float ry = (xi4.y - pj.y) - (fn0 * Rf[1] + fn1 * Rf[4] + fn2 * Rf[7]);
+            const float rz = (xi4.z - pj.z) - (fn0 * Rf[2] + fn1 * Rf[5] + fn2 * Rf[8]);
+            const float d2f = rx * rx + ry * ry + rz * rz;
+            acc = d2f < rc2f;
+            if (FP64 && acc) {
+                double r[3], d2;
+                pair_vec_d(xid, a.bposd + 3 * c, g.R, n0, n1, n2, r, d2);
+                acc = d2 < rc2;
+            }
+            if (j == i && n0 == 0 && n1 == 0 && n2 == 0) acc = false;
+        }
+        const unsigned msk = __ballot_sync(0xffffffffu, acc);
+        const int pos = cursor + __popc(msk & lt);
+        if (acc && pos < cap) { sj[pos] = j; simg[pos] = pack3(n0, n1, n2); styp[pos] = tj; }
+        cursor += __popc(msk);
+    }
+};
+
+constexpr int NBR_WARPS = 4;
+constexpr int MAX_RANGES = 512;   // atom ranges per centre atom in the flattened stencil walk
+
+template <bool FP64>
+__global__ void __launch_bounds__(NBR_WARPS * 32) k_neighbors(NbrArgs a) {
     extern __shared__ int32_t nsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int cap = a.cap;
-    int32_t* sj = nsm + wid * 3 * cap;
+    int32_t* sj = nsm + wid * (3 * cap + 3 * MAX_RANGES);
     int32_t* simg = sj + cap;
     int32_t* styp = simg + cap;
+    int32_t* rstart = styp + cap;            // first bin-ordered atom of each range
+    int32_t* rpre = rstart + MAX_RANGES;     // inclusive prefix of range lengths
+    int32_t* rimg = rpre + MAX_RANGES;       // packed image shift k of the range
+    Cand<FP64> cd;
     const unsigned lt = (1u << lane) - 1u;
+    cd.lt = lt;
+    cd.cap = cap;
     const float rcf = (float)a.rc;
-    const float rc2f = FP64 ? (rcf + 0.05f) * (rcf + 0.05f) : rcf * rcf;
-    const double rc2 = a.rc * a.rc;
+    cd.rc2f = FP64 ? (rcf + 0.05f) * (rcf + 0.05f) : rcf * rcf;
+    cd.rc2 = a.rc * a.rc;
     for (;;) {
         int i = 0;
         if (lane == 0) i = (int)atomicAdd(a.counter, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= a.natoms) break;
+        cd.i = i;
         const StrucGeo& g = a.geo[a.sid[i]];
-        int b0, b1, b2, mi0, mi1, mi2;
+        int b0, b1, b2;
         unpack3(a.abc[i], b0, b1, b2);
-        unpack3(a.am[i], mi0, mi1, mi2);
-        const float4 xi4 = a.pos4[i];
-        const double xid[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
+        unpack3(a.am[i], cd.mi0, cd.mi1, cd.mi2);
+        cd.xi4 = a.pos4[i];
+        cd.xid[0] = a.pos[3 * i]; cd.xid[1] = a.pos[3 * i + 1]; cd.xid[2] = a.pos[3 * i + 2];
+        const double* xid = cd.xid;
+        const float4 xi4 = cd.xi4;
         float Rf[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Rf[k] = (float)g.R[k];
+        for (int k = 0; k < 9; ++k) { Rf[k] = (float)g.R[k]; cd.Rf[k] = Rf[k]; }
+        const int nb0 = g.nb[0], nb1 = g.nb[1], nb2 = g.nb[2];
+        const int s0 = g.sten[0], s1 = g.sten[1], s2 = g.sten[2];
+        const int w1 = 2 * s1 + 1, nrows = w1 * (2 * s2 + 1);
+        const int segmax = (2 * s0) / nb0 + 2;
         int cursor = 0;
-        for (int e2 = -g.sten[2]; e2 <= g.sten[2]; ++e2) {
-            const int u2 = b2 + e2, k2 = floordiv(u2, g.nb[2]), q2 = u2 - k2 * g.nb[2];
-            for (int e1 = -g.sten[1]; e1 <= g.sten[1]; ++e1) {
-                const int u1 = b1 + e1, k1 = floordiv(u1, g.nb[1]), q1 = u1 - k1 * g.nb[1];
-                for (int e0 = -g.sten[0]; e0 <= g.sten[0]; ++e0) {
-                    const int u0 = b0 + e0, k0 = floordiv(u0, g.nb[0]), q0 = u0 - k0 * g.nb[0];
-                    const int bin = g.bin0 + (q2 * g.nb[1] + q1) * g.nb[0] + q0;
-                    const int st = a.bstart[bin], en = a.bstart[bin + 1];
-                    for (int c0 = st; c0 < en; c0 += 32) {
-                        const int c = c0 + lane;
-                        bool acc = false;
-                        int j = 0, n0 = 0, n1 = 0, n2 = 0, tj = 0;
-                        if (c < en) {
-                            j = a.bidx[c];
-                            int mj0, mj1, mj2;
-                            unpack3(a.bm[c], mj0, mj1, mj2);
-                            n0 = k0 + mi0 - mj0; n1 = k1 + mi1 - mj1; n2 = k2 + mi2 - mj2;
-                            const float4 pj = a.bpos4[c];
-                            tj = __float_as_int(pj.w);
-                            const float fn0 = (float)n0, fn1 = (float)n1, fn2 = (float)n2;
-                            const float rx = (xi4.x - pj.x) - (fn0 * Rf[0] + fn1 * Rf[3] + fn2 * Rf[6]);
-                            const float ry = (xi4.y - pj.y) - (fn0 * Rf[1] + fn1 * Rf[4] + fn2 * Rf[7]);
-                            const float rz = (xi4.z - pj.z) - (fn0 * Rf[2] + fn1 * Rf[5] + fn2 * Rf[8]);
-                            const float d2f = rx * rx + ry * ry + rz * rz;
-                            acc = d2f < rc2f;
-                            if (FP64 && acc) {
-                                double r[3], d2;
-                                pair_vec_d(xid, a.bposd + 3 * c, g.R, n0, n1, n2, r, d2);
-                                acc = d2 < rc2;
-                            }
-                            if (j == i && n0 == 0 && n1 == 0 && n2 == 0) acc = false;
-                        }
-                        const unsigned msk = __ballot_sync(0xffffffffu, acc);
-                        const int pos = cursor + __popc(msk & lt);
-                        if (acc && pos < cap) { sj[pos] = j; simg[pos] = pack3(n0, n1, n2); styp[pos] = tj; }
-                        cursor += __popc(msk);
+        if (nrows * segmax <= MAX_RANGES) {
+            // ---- flattened walk: each stencil row (e1,e2) contributes <= segmax contiguous atom
+            //      ranges (one per x image); lanes then take consecutive candidates across ranges
+            for (int r = lane; r < nrows; r += 32) {
+                const int e1 = r % w1 - s1, e2 = r / w1 - s2;
+                const int u1 = b1 + e1, k1 = floordiv(u1, nb1), q1 = u1 - k1 * nb1;
+                const int u2 = b2 + e2, k2 = floordiv(u2, nb2), q2 = u2 - k2 * nb2;
+                const int rowbin = g.bin0 + (q2 * nb1 + q1) * nb0;
+                int u = b0 - s0, seg = 0;
+                const int uend = b0 + s0;
+                while (u <= uend && seg < segmax) {
+                    const int k0 = floordiv(u, nb0), q0 = u - k0 * nb0;
+                    const int len = min(uend - u + 1, nb0 - q0);
+                    const int st = a.bstart[rowbin + q0];
+                    rstart[r * segmax + seg] = st;
+                    rpre[r * segmax + seg] = a.bstart[rowbin + q0 + len] - st;
+                    rimg[r * segmax + seg] = pack3(k0, k1, k2);
+                    ++seg;
+                    u += len;
+                }
+                for (; seg < segmax; ++seg) { rstart[r * segmax + seg] = 0; rpre[r * segmax + seg] = 0; rimg[r * segmax + seg] = 0; }
+            }
+            __syncwarp();
+            const int nr = nrows * segmax;
+            int carry = 0;
+            for (int r0 = 0; r0 < nr; r0 += 32) {   // inclusive prefix of the range lengths
+                const int r = r0 + lane;
+                int v = (r < nr) ? rpre[r] : 0;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) { const int t = __shfl_up_sync(0xffffffffu, v, off); if (lane >= off) v += t; }
+                if (r < nr) rpre[r] = carry + v;
+                carry += __shfl_sync(0xffffffffu, v, 31);
+            }
+            __syncwarp();
+            const int total = carry;
+            int rr = 0;   // this lane's current range
+            for (int c0 = 0; c0 < total; c0 += 32) {
+                const int c = c0 + lane;
+                const bool valid = c < total;
+                int k0 = 0, k1 = 0, k2 = 0, ca = 0;
+                if (valid) {
+                    while (rpre[rr] <= c) ++rr;
+                    const int before = (rr == 0) ? 0 : rpre[rr - 1];
+                    ca = rstart[rr] + (c - before);
+                    unpack3(rimg[rr], k0, k1, k2);
+                }
+                cd.test(a, g, ca, valid, k0, k1, k2, sj, simg, styp, cursor);
+            }
+        } else {
+            // ---- per-bin walk for cells needing very many images
+            for (int e2 = -s2; e2 <= s2; ++e2) {
+                const int u2 = b2 + e2, k2 = floordiv(u2, nb2), q2 = u2 - k2 * nb2;
+                for (int e1 = -s1; e1 <= s1; ++e1) {
+                    const int u1 = b1 + e1, k1 = floordiv(u1, nb1), q1 = u1 - k1 * nb1;
+                    for (int e0 = -s0; e0 <= s0; ++e0) {
+                        const int u0 = b0 + e0, k0 = floordiv(u0, nb0), q0 = u0 - k0 * nb0;
+                        const int bin = g.bin0 + (q2 * nb1 + q1) * nb0 + q0;
+                        const int st = a.bstart[bin], en = a.bstart[bin + 1];
+                        for (int c0 = st; c0 < en; c0 += 32) cd.test(a, g, c0 + lane, c0 + lane < en, k0, k1, k2, sj, simg, styp, cursor);
                     }
                 }
             }
@@ -294,10 +376,10 @@ void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st) {
     if (a.natoms > 0) ++::ann::g_launch_counter, k_bin_scatter<<<nb, 256, 0, st>>>(a);
     ++::ann::g_launch_counter, k_bin_sort<<<(a.nbins_cap + 255) / 256, 256, 0, st>>>(a, a.nbins_cap);
     cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), st);
-    const int warps = 8;
-    const size_t smem = (size_t)warps * 3 * a.cap * sizeof(int32_t);
+    const int warps = NBR_WARPS;
+    const size_t smem = (size_t)warps * (3 * a.cap + 3 * MAX_RANGES) * sizeof(int32_t);
     int grid = (a.natoms + warps - 1) / warps;
-    grid = std::min(grid, 152 * 8);
+    grid = std::min(grid, 152 * 16);
     if (grid < 1) grid = 1;
     if (fp64) ++::ann::g_launch_counter, k_neighbors<true><<<grid, warps * 32, smem, st>>>(a);
     else ++::ann::g_launch_counter, k_neighbors<false><<<grid, warps * 32, smem, st>>>(a);
