@@ -22,6 +22,8 @@ Configurations:
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 SEED0 = 20261203
@@ -138,7 +140,7 @@ class _StdMT19937Normal:
             r2 = x * x + y * y
             if r2 <= 1.0 and r2 != 0.0:
                 break
-        mult = np.sqrt(-2.0 * np.log(r2) / r2)
+        mult = math.sqrt(-2.0 * math.log(r2) / r2)   # libm, as std::log / std::sqrt
         self.saved = x * mult
         return y * mult * sd
 

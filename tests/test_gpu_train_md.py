@@ -1,0 +1,121 @@
+"""GPU training adjoint and molecular dynamics vs the oracle, through the C ABI.
+
+Training: L = wE/S sum 1/2 ((E_s-Eref_s)/N_s)^2 + wF/(3N) sum 1/2 |F-Fref|^2. The FP64 gradient
+matches the oracle (relative to the gradient's scale, 1e-9) and central finite differences of the
+GPU's own loss; with wF = 0 it equals the reference trainer's energy gradient
+(NNPTEFR::error_cost_o1, nnptefr2.cpp:1321-1374 + 984-995, restated in the oracle).
+MD: velocity Verlet (integrator.cpp:177-200) step by step against the oracle, and energy
+conservation over a longer run.
+"""
+import numpy as np
+import pytest
+
+import cases
+from ann_gb300 import FP64, MIXED, Context
+from ann_gb300 import workloads as W
+from ann_gb300.api import pack_batch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_lib):
+    c = Context(use_graphs=True)
+    yield c
+    c.close()
+
+
+def _train_case():
+    structs = cases.small_binary(n_struc=3, seed=8)
+    offs, posn, types, cell = pack_batch(structs)
+    Eref, Fref = W.lennard_jones(structs)
+    return offs, posn, types, cell, Eref * 0.01, np.concatenate(Fref) * 0.01
+
+
+def test_init_network_matches_reference_rng(ctx):
+    ctx.load_text(W.config_potential_text(2, with_weights=False))
+    ctx.init_network(0, 1234, dist=0, init=4, sigma_b=0.001, sigma_w=1.0)
+    ctx.init_network(1, 99, dist=0, init=4, sigma_b=0.001, sigma_w=1.0)
+    p = ctx.get_params()
+    want = np.concatenate([W.xavier_network(1234, 72, [64, 64, 1]), W.xavier_network(99, 72, [64, 64, 1])])
+    assert np.array_equal(p, want)
+
+
+@pytest.mark.parametrize("wE,wF", [(1.0, 0.1), (1.0, 0.0), (0.0, 1.0)])
+def test_gradient_matches_oracle(ctx, oracle, tmp_path, wE, wF):
+    text = cases.config_potential(ctx, 3, tmp_path)
+    pot = oracle.load_text(text)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    loss = ctx.train_forward(offs, posn, types, cell, Eref, Fref, wE, wF, precision=FP64)
+    g = ctx.train_backward()
+    lo, go = pot.train(offs, posn, types, cell, Eref, Fref, wE, wF)
+    assert np.allclose(loss, lo, rtol=1e-10, atol=1e-14)
+    scale = np.abs(go).max()
+    assert np.abs(g - go).max() <= 1e-9 * scale
+    if wF == 0.0:
+        l2, g2 = pot.error_cost_o1(offs, posn, types, cell, Eref)
+        assert np.abs(g - g2).max() <= 1e-9 * np.abs(g2).max()
+    # mixed precision gradient stays close to FP64
+    ctx.train_forward(offs, posn, types, cell, Eref, Fref, wE, wF, precision=MIXED)
+    gm = ctx.train_backward()
+    assert np.abs(gm - g).max() <= 1e-3 * scale
+
+
+def test_gradient_finite_differences_on_gpu(ctx, tmp_path):
+    cases.config_potential(ctx, 3, tmp_path)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+    g = ctx.train_backward()
+    p0 = ctx.get_params()
+    rng = np.random.default_rng(5)
+    scale = np.abs(g).max()
+    for k in rng.choice(len(p0), 10, replace=False):
+        h = 1e-5 * max(1.0, abs(p0[k]))
+        pp = p0.copy(); pp[k] += h
+        ctx.set_params(pp)
+        lp = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)[0]
+        pp[k] -= 2 * h
+        ctx.set_params(pp)
+        lm = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)[0]
+        ctx.set_params(p0)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * abs(g[k]) + 1e-7 * scale, (k, fd, g[k])
+
+
+def _md_case():
+    x, v, t, R = W.config5(cells=(3, 3, 3))
+    return x, v, t, R
+
+
+def test_md_steps_match_oracle(ctx, oracle, tmp_path):
+    text = cases.config_potential(ctx, 5, tmp_path)
+    pot = oracle.load_text(text)
+    x, v, t, R = _md_case()
+    masses = np.array([39.948])
+    ctx.md_init(x, v, t, R, masses, dt_fs=2.0, skin=0.5, precision=FP64)
+    xo, vo = x.copy(), v.copy()
+    offs, _, _, cell = pack_batch([(x, t, R)])
+    Fo = pot.compute(offs, xo, t, cell)[1]
+    for step in range(5):
+        pe, ke, _ = ctx.md_run(1)
+        peo, keo = pot.md_step(xo, vo, t, R, masses, 2.0, Fo)
+        xg, vg, fg = ctx.md_state()
+        d = xg - xo
+        Ri = np.linalg.inv(R)
+        d -= (np.round(d @ Ri.T)) @ R.T      # the GPU wraps only when it rebuilds its list
+        assert np.abs(d).max() < 1e-9
+        assert np.abs(vg - vo).max() < 1e-10
+        assert abs(pe - peo) < 1e-9 * max(1.0, abs(peo)) and abs(ke - keo) < 1e-9 * max(1.0, keo)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_md_energy_conservation(ctx, tmp_path, prec):
+    cases.config_potential(ctx, 5, tmp_path)
+    x, v, t, R = _md_case()
+    ctx.md_init(x, v, t, R, np.array([39.948]), dt_fs=2.0, skin=0.5, precision=prec)
+    pe0, ke0, _ = ctx.md_run(1)
+    e0 = pe0 + ke0
+    pe, ke, rebuilds = ctx.md_run(400)
+    drift = abs(pe + ke - e0) / len(t)          # eV/atom over 0.8 ps
+    assert drift < 2e-4, drift
+    assert rebuilds >= 0
