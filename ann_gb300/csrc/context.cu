@@ -16,6 +16,7 @@
 
 #include "../../include/ann_gpu.h"
 #include "kernels.hpp"
+#include "mlp_tc.hpp"
 #include "plan_build.hpp"
 #include "potential.hpp"
 
@@ -98,6 +99,8 @@ struct ann_ctx {
     bool have_pot = false;
     Potential pot;
     PlanHost plan;
+    TcPlan tc;                      // tensor-core network images (MIXED precision)
+    DevBuf tcimg;
     ParamSet<float> pf;
     ParamSet<double> pd;
     DevBuf poff;
@@ -170,6 +173,12 @@ static void reset_graph(ann_ctx* c) {
 }
 static void rebuild_plan(ann_ctx* c) {
     build_plan(c->pot, c->plan);
+    build_tc_plan(c->plan.pot, c->plan.w, c->plan.b, c->plan.inpw, c->plan.inpb, c->max_smem, c->tc);
+    if (c->opt.mlp_backend == 2 && !c->tc.ok)
+        throw ann_error(ANN_ERR_UNSUPPORTED, "the networks do not fit the tensor-core kernel (hidden layers 1..5, widths <= 256)");
+    c->tcimg.ensure(c->tc.image.size());
+    ck(cudaMemcpyAsync(c->tcimg.p, c->tc.image.data(), c->tc.image.size(), cudaMemcpyHostToDevice, c->stream), "upload network images");
+    ck(cudaStreamSynchronize(c->stream), "upload network images");
     upload_params<float>(c, c->pf);
     upload_params<double>(c, c->pd);
     std::vector<int> po;
@@ -302,6 +311,9 @@ static void mark(ann_ctx* c, int k) {
     cudaEventRecord(c->ev[k], c->stream);
 }
 
+// the MIXED network pass runs on the tensor cores unless the SIMT kernels are asked for
+static bool use_tc(const ann_ctx* c) { return c->opt.mlp_backend != 1 && c->tc.ok; }
+
 template <typename real>
 static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     cudaStream_t st = c->stream;
@@ -326,7 +338,18 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     m.tstart = c->tstart.as<int32_t>(); m.tlist = c->tlist.as<int32_t>();
     m.G = c->G.as<real>(); m.dEdG = c->dEdG.as<real>(); m.Eatom = c->Eatom.as<double>();
     m.prm = b.prm;
-    launch_mlp_forward_backward<real>(pot, m, st);
+    if (!fp64 && use_tc(c)) {
+        for (int ty = 0; ty < c->pot.ntypes(); ++ty) {
+            TcArgs ta{};
+            ta.natoms = c->N; ta.imax = pot.imax; ta.type = ty;
+            ta.tstart = m.tstart; ta.tlist = m.tlist;
+            ta.G = c->G.as<float>(); ta.dEdG = c->dEdG.as<float>(); ta.Eatom = m.Eatom;
+            ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>();
+            launch_mlp_tc(c->tc.t[ty], ta, c->tc.smem_bytes(ty), st);
+        }
+    } else {
+        launch_mlp_forward_backward<real>(pot, m, st);
+    }
     check_phase(c, "networks");
     mark(c, 4);
     if (forces) {
@@ -351,7 +374,7 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
     if (need_bp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity " + std::to_string(c->cap) + " needs " + std::to_string(need_bp) +
                                               " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
-    if (need_mlp > (size_t)c->max_smem)
+    if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
     const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap};
     const bool graphs = c->opt.use_graphs && build_list && c->N > 0 && !c->profile;
@@ -442,6 +465,8 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream create");
         configure_kernels();
         cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->opt.device);
+        cudaDeviceGetAttribute(&c->tc.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->opt.device);
+        if (c->opt.mlp_backend < 0 || c->opt.mlp_backend > 2) throw ann_error(ANN_ERR_ARG, "mlp_backend must be 0, 1 or 2");
         const char* dbg = std::getenv("ANN_DEBUG");
         c->debug = dbg && dbg[0] == '1';
         if (c->debug) c->opt.use_graphs = 0;

@@ -21,27 +21,6 @@ constexpr int TA = 32;        // atoms per block (energy/force network pass)
 constexpr int TAT = 16;       // atoms per block (training pass, more state per atom)
 constexpr int MLP_T = 128;    // threads per block
 
-// activation value, first and second derivative (nn.cpp:149-236 linear/sigmoid/tanh,
-// nn.cpp:676-720 softplus shifted by -ln2/c)
-template <typename real>
-__device__ __forceinline__ void act_fd(int neuron, real c, real z, real& a, real& d, real& d2) {
-    switch (neuron) {
-        case N_SIGMOID: {
-            if (z >= real(0)) { const real e = M<real>::exp(-c * z); const real f = real(1) / (real(1) + e); a = f; d = c * e * f * f; d2 = -c * c * e * (real(1) - e) * f * f * f; }
-            else { const real e = M<real>::exp(c * z); const real f = real(1) / (real(1) + e); a = e * f; d = c * e * f * f; d2 = -c * c * e * (e - real(1)) * f * f * f; }
-            return;
-        }
-        case N_TANH: { const real t = M<real>::tanh(c * z); a = t; d = c * (real(1) - t * t); d2 = c * c * (real(-2) * t * (real(1) - t * t)); return; }
-        case N_SOFTPLUS: {
-            const real ci = real(1) / c;
-            if (z > real(0)) { const real e = M<real>::exp(-c * z); const real den = real(1) / (e + real(1)); a = z + ci * (M<real>::log1p(e) - real(kLOG2)); d = den; d2 = c * e * den * den; }
-            else { const real e = M<real>::exp(c * z); const real den = real(1) / (e + real(1)); a = ci * (M<real>::log1p(e) - real(kLOG2)); d = e * den; d2 = c * e * den * den; }
-            return;
-        }
-        default: a = z; d = real(1); d2 = real(0); return;  // LINEAR
-    }
-}
-
 // map block -> (type, first atom in the type list); returns false if the block is spare
 template <int TAn>
 __device__ __forceinline__ bool tile_of_block(int ntypes, const int32_t* tstart, int& type, int& a0, int& na) {

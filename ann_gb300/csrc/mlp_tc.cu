@@ -1,0 +1,259 @@
+// K3 on the 5th-generation tensor cores: per-element networks (forward, energy, backward to dE/dG)
+// over tiles of 128 atoms of one type, as tcgen05 BF16 GEMMs with FP32 accumulators in TMEM.
+//
+// Reference: NN::ANN::fpbp (src/ml/nn.cpp:1343-1409), NN::DODZ::grad (nn.cpp:1801-1824) and
+// NNH::energy (src/nnp/nnh.cpp:118-121), the same computation as the SIMT kernel in mlp.cu.
+//
+// Per CTA (128 threads, thread t <-> atom row t <-> TMEM lane t), persistent over the type's tiles:
+//   weights   : one bulk asynchronous copy (cp.async.bulk + mbarrier) of the type's image
+//               (B operands W_l and W_l^T in the canonical K-major no-swizzle layout, BF16 hi/lo).
+//   per tile  : A0 = inpw*(G+inpb) split into BF16 hi+lo rows, then for every hidden layer
+//               D = A W_l^T (tcgen05.mma kind::f16, M=128, issued by one thread, completion via
+//               tcgen05.commit on an mbarrier), epilogue = tcgen05.ld of the thread's row, bias,
+//               activation, next A; the last hidden layer's epilogue forms the energy and
+//               delta = outw w_last f'(z); the backward GEMMs D = delta W_l multiply by f'(z_{l-1})
+//               recomputed from the forward accumulators kept in TMEM, down to dE/dG = D inpw.
+//   split     : A = A_hi + A_lo (and W = W_hi + W_lo when the image fits) accumulate 2 or 3
+//               MMAs per k-step, giving close to FP32 products from BF16 operands.
+// Every wait is bounded; on a timeout the CTA records ST_TIMEOUT, drains, frees TMEM and returns.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cstdint>
+#include "dev_math.cuh"
+#include "kernels.hpp"
+#include "mlp_tc.hpp"
+
+namespace ann {
+
+static __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// ---------------------------------------------------------------- mbarrier / bulk copy
+static __device__ __forceinline__ void tc_mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+static __device__ __forceinline__ bool tc_try_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(su32(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+static __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t phase) {
+    for (int it = 0; it < (1 << 22); ++it) if (tc_try_wait(bar, phase)) return true;
+    return false;
+}
+
+// ---------------------------------------------------------------- tcgen05
+// shared-memory matrix descriptor: start address, leading (K) and stride (8-row group) byte
+// offsets, fixed 0b001 at bits 46-48, no swizzle
+static __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, N and M=128
+static __device__ __forceinline__ uint32_t idesc_bf16(int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
+static __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(accum) : "memory");
+}
+static __device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
+}
+static __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+static __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+static __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 8 consecutive values of row r into the A tiles (hi, and lo = remainder when lo != nullptr)
+static __device__ __forceinline__ void put8(uint8_t* hi, uint8_t* lo, int r, int c0, uint32_t sbo, const float* v) {
+    const uint32_t off = (uint32_t)(r >> 3) * sbo + (uint32_t)(c0 >> 3) * 128u + (uint32_t)(r & 7) * 16u;
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat16 a0 = __float2bfloat16_rn(v[2 * q]), a1 = __float2bfloat16_rn(v[2 * q + 1]);
+        h[q] = (uint32_t)__bfloat16_as_ushort(a0) | ((uint32_t)__bfloat16_as_ushort(a1) << 16);
+        if (lo) {
+            const __nv_bfloat16 b0 = __float2bfloat16_rn(v[2 * q] - __bfloat162float(a0));
+            const __nv_bfloat16 b1 = __float2bfloat16_rn(v[2 * q + 1] - __bfloat162float(a1));
+            l[q] = (uint32_t)__bfloat16_as_ushort(b0) | ((uint32_t)__bfloat16_as_ushort(b1) << 16);
+        }
+    }
+    *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    if (lo) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+__global__ void __launch_bounds__(TC_M, 1) k_mlp_tc(const __grid_constant__ TcType tt, const TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    const int t = threadIdx.x, warp = t >> 5;
+    const int a0 = a.tstart[a.type], cnt = a.tstart[a.type + 1] - a0;
+    const int ntiles = (cnt + TC_M - 1) / TC_M;
+    if ((int)blockIdx.x >= ntiles) return;
+
+    uint8_t* img = sm;
+    const uint32_t abytes = (uint32_t)TC_M * tt.wmax * 2;
+    uint8_t* Ahi = sm + ((tt.img_bytes + 127) / 128) * 128;
+    uint8_t* Alo = (tt.split >= 2) ? Ahi + abytes : nullptr;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Ahi + abytes * (tt.split >= 2 ? 2 : 1));
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
+    const uint32_t asbo = (uint32_t)tt.wmax * 16u;   // (wmax / 8) * 128
+
+    if (t == 0) { tc_mbar_init(&bar[0]); tc_mbar_init(&bar[1]); }
+    __syncthreads();
+    if (t == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(&bar[0])), "r"(tt.img_bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(su32(img)), "l"(a.image + tt.img_off), "r"(tt.img_bytes), "r"(su32(&bar[0])) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)), "r"((uint32_t)tt.tmem_cols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    bool good = tc_wait(&bar[0], 0);
+    tc_fence_before();
+    good = __syncthreads_and(good);
+    const bool image_ok = good;
+    bool mma_pending = false;       // an MMA group whose completion was not observed
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    uint32_t mphase = 0;
+
+    const float* inpw = reinterpret_cast<const float*>(img + tt.inpw);
+    const float* inpb = reinterpret_cast<const float*>(img + tt.inpb);
+    const float* wlast = reinterpret_cast<const float*>(img + tt.wlast);
+    const float c = tt.c;
+    const uint32_t img_s = su32(img), ahi_s = su32(Ahi), alo_s = Alo ? su32(Alo) : 0u;
+
+    // one GEMM: D[tmem col] = A (rows x K) . B^T (B: N x K image), accumulate hi/lo parts
+    auto gemm = [&](uint32_t b_hi, uint32_t b_lo, int K, int N, uint32_t dcol) -> bool {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (t == 0) {
+            const uint32_t idesc = idesc_bf16(N);
+            const uint32_t bsbo = (uint32_t)(K / 8) * 128u;
+            for (int s = 0; s < K / 16; ++s) {
+                const uint64_t ad = smem_desc(ahi_s + 256u * s, 128u, asbo);
+                const uint64_t bd = smem_desc(img_s + b_hi + 256u * s, 128u, bsbo);
+                tc_mma(tmem + dcol, ad, bd, idesc, s > 0 ? 1u : 0u);
+                if (tt.split >= 2) tc_mma(tmem + dcol, smem_desc(alo_s + 256u * s, 128u, asbo), bd, idesc, 1u);
+                if (tt.split >= 3) tc_mma(tmem + dcol, ad, smem_desc(img_s + b_lo + 256u * s, 128u, bsbo), idesc, 1u);
+            }
+            tc_commit(&bar[1]);
+        }
+        const bool ok = __syncthreads_and(tc_wait(&bar[1], mphase));
+        tc_fence_after();
+        if (ok) mphase ^= 1u;
+        else mma_pending = true;
+        return ok;
+    };
+
+    for (int tile = blockIdx.x; tile < ntiles && good; tile += gridDim.x) {
+        const int row = tile * TC_M + t;
+        const int at = (row < cnt) ? a.tlist[a0 + row] : -1;
+        // ---- A0 = inpw * (G + inpb)
+        for (int c0 = 0; c0 < tt.K0; c0 += 8) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int k = c0 + q;
+                v[q] = (at >= 0 && k < tt.nin) ? inpw[k] * (a.G[(size_t)at * a.imax + k] + inpb[k]) : 0.0f;
+            }
+            put8(Ahi, Alo, t, c0, asbo, v);
+        }
+        // ---- forward
+        float epart = 0.0f;
+        for (int l = 0; l < tt.nhidden && good; ++l) {
+            const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
+            const int N = tt.width[l];
+            good = gemm(tt.fwd_hi[l], tt.fwd_lo[l], Kin, N, (uint32_t)tt.fwd_col[l]);
+            if (!good) break;
+            const float* bias = reinterpret_cast<const float*>(img + tt.bias[l]);
+            const bool last = (l == tt.nhidden - 1);
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                float v[16];
+                tc_ld16(tmem + lane_off + (uint32_t)(tt.fwd_col[l] + c0), v);
+                float o[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int col = c0 + q;
+                    float av, d1, d2;
+                    act_fd<float>(tt.neuron, c, v[q] + bias[col], av, d1, d2);
+                    if (col >= tt.nodes[l]) { av = 0.0f; d1 = 0.0f; }
+                    if (last) { epart += wlast[col] * av; o[q] = tt.outw * wlast[col] * d1; }
+                    else o[q] = av;
+                }
+                put8(Ahi, Alo, t, c0, asbo, o);
+                put8(Ahi, Alo, t, c0 + 8, asbo, o + 8);
+            }
+        }
+        if (!good) break;
+        if (at >= 0) a.Eatom[at] = (double)(tt.outb + tt.outw * (epart + tt.blast)) + tt.evac;
+        // ---- backward: A holds delta of hidden layer l
+        for (int l = tt.nhidden - 1; l >= 0 && good; --l) {
+            const int Nout = (l == 0) ? tt.K0 : tt.width[l - 1];
+            good = gemm(tt.bwd_hi[l], tt.bwd_lo[l], tt.width[l], Nout, (uint32_t)tt.bwd_col);
+            if (!good) break;
+            for (int c0 = 0; c0 < Nout; c0 += 16) {
+                float g[16];
+                tc_ld16(tmem + lane_off + (uint32_t)(tt.bwd_col + c0), g);
+                if (l > 0) {
+                    float z[16];
+                    tc_ld16(tmem + lane_off + (uint32_t)(tt.fwd_col[l - 1] + c0), z);
+                    const float* bias = reinterpret_cast<const float*>(img + tt.bias[l - 1]);
+                    float o[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int col = c0 + q;
+                        float av, d1, d2;
+                        act_fd<float>(tt.neuron, c, z[q] + bias[col], av, d1, d2);
+                        o[q] = (col < tt.nodes[l - 1]) ? g[q] * d1 : 0.0f;
+                    }
+                    put8(Ahi, Alo, t, c0, asbo, o);
+                    put8(Ahi, Alo, t, c0 + 8, asbo, o + 8);
+                } else if (at >= 0) {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int col = c0 + q;
+                        if (col < a.imax) a.dEdG[(size_t)at * a.imax + col] = (col < tt.nin) ? g[q] * inpw[col] : 0.0f;
+                    }
+                }
+            }
+            if (l == 0 && at >= 0)
+                for (int col = tt.K0; col < a.imax; ++col) a.dEdG[(size_t)at * a.imax + col] = 0.0f;
+        }
+    }
+    if (!good) {
+        if (t == 0) atomicOr(a.status, (int)ST_TIMEOUT);
+        // drain what may still be in flight before the shared memory and TMEM go away (bounded)
+        if (!image_ok) tc_wait(&bar[0], 0);
+        if (mma_pending) tc_wait(&bar[1], mphase);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)tt.tmem_cols) : "memory");
+}
+
+void launch_mlp_tc(const TcType& tt, const TcArgs& a, size_t smem, cudaStream_t st) {
+    if (a.natoms <= 0) return;
+    int grid = (a.natoms + TC_M - 1) / TC_M;
+    grid = std::min(grid, 152);
+    ++::ann::g_launch_counter, k_mlp_tc<<<grid, TC_M, smem, st>>>(tt, a);
+}
+void configure_mlp_tc(int maxsmem) { set_max_dynamic_smem(k_mlp_tc, maxsmem); }
+
+}  // namespace ann

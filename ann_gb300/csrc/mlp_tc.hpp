@@ -1,0 +1,66 @@
+// Tensor-core (tcgen05) form of the per-element networks: host-built weight images and the
+// per-type launch description shared by plan_tc.cpp (host) and mlp_tc.cu (device).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+#include "plan.hpp"
+
+namespace ann {
+
+constexpr int TC_M = 128;          // atoms per tile (one TMEM lane each)
+constexpr int TC_MAXH = 5;         // hidden layers
+
+// Operands live in shared memory in the canonical K-major no-swizzle layout of tcgen05:
+// 8-row x 16-byte core matrices (128 B each); along K adjacent core matrices are 128 B apart
+// (leading byte offset), along rows the 8-row groups are K/8 * 128 B apart (stride byte offset).
+// The image of one type holds, for every hidden layer l, the B operands of the forward GEMM
+// (W_l, N = nodes[l] x K = ni(l)) and of the backward GEMM (W_l^T, N = ni(l) x K = nodes[l]),
+// each as BF16 hi and (split > 1) lo parts, followed by FP32 vectors.
+struct TcType {
+    int32_t nhidden;                 // hidden layers (the last layer is a dot product)
+    int32_t nin, K0;                 // inputs and inputs padded to 16
+    int32_t width[TC_MAXH];          // padded width of hidden layer l
+    int32_t nodes[TC_MAXH];          // true width of hidden layer l
+    uint32_t fwd_hi[TC_MAXH], fwd_lo[TC_MAXH], bwd_hi[TC_MAXH], bwd_lo[TC_MAXH];  // byte offsets in the image
+    uint32_t bias[TC_MAXH];          // byte offset of the FP32 bias of hidden layer l (padded width)
+    uint32_t wlast;                  // FP32 weights of the last layer (padded width of the last hidden layer)
+    uint32_t inpw, inpb;             // FP32 input scaling (K0 entries)
+    uint32_t img_bytes;              // size of the image (multiple of 16)
+    uint32_t img_off;                // offset of this type's image in the device buffer
+    float blast, outw, outb, c;
+    double evac;
+    int32_t neuron;
+    int32_t wmax;                    // widest padded operand width (K0 or any hidden width)
+    int32_t fwd_col[TC_MAXH];        // TMEM column of the forward accumulator of hidden layer l
+    int32_t bwd_col;                 // TMEM column of the backward accumulators
+    int32_t tmem_cols;               // allocated TMEM columns (power of two, <= 512)
+    int32_t split;                   // 1: A and B single BF16; 2: A split hi+lo; 3: A and B split
+};
+
+struct TcPlan {
+    bool ok = false;                 // every type fits the tensor-core kernel
+    TcType t[MAXT];
+    std::vector<uint8_t> image;      // all types' images, back to back (128-byte aligned)
+    int smem_per_sm = 228 * 1024;    // shared memory of one SM (limits co-resident CTAs)
+    size_t smem_bytes(int type) const;
+};
+
+// builds the images from the row-major FP64 weights of the plan (w[l][n*ni+m], b[l][n])
+void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::vector<double>& b,
+                   const std::vector<double>& inpw, const std::vector<double>& inpb, int max_smem, TcPlan& out);
+
+struct TcArgs {
+    int32_t natoms, imax, type;
+    const int32_t* tstart;
+    const int32_t* tlist;
+    const float* G;                  // [N*imax] FP32 symmetry functions
+    float* dEdG;                     // [N*imax]
+    double* Eatom;                   // [N]
+    const uint8_t* image;            // device copy of TcPlan::image
+    int32_t* status;
+};
+void launch_mlp_tc(const TcType& tt, const TcArgs& a, size_t smem, cudaStream_t st);
+void configure_mlp_tc(int maxsmem);
+
+}  // namespace ann

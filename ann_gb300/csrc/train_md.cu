@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "kernels.hpp"
+#include "mlp_tc.hpp"
 
 namespace ann {
 
@@ -106,6 +107,7 @@ void configure_kernels() {
     configure_bp(maxs);
     configure_mlp(maxs);
     configure_nbr(maxs);
+    configure_mlp_tc(maxs);
     done = true;
 }
 

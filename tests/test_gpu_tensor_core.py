@@ -1,0 +1,110 @@
+"""The tcgen05 network kernel (MIXED precision, mlp_backend auto / 2) against the SIMT kernels
+and the FP64 pipeline, through the C ABI.
+
+Bars: atom energies and dE/dG of the tensor-core pass within 1e-4 eV / 1e-4 relative of the FP64
+pass (BF16 hi+lo operands, FP32 accumulation); structure energies and forces within the mixed
+bars of 1 meV/atom and 10 meV/A.
+"""
+import numpy as np
+import pytest
+
+import cases
+from ann_gb300 import FP64, MIXED, AnnError, Context
+
+pytestmark = pytest.mark.gpu
+
+E_MEV_ATOM = 1.0
+F_MEV_A = 10.0
+
+
+@pytest.fixture(scope="module")
+def contexts(gpu_lib):
+    tc = Context(mlp_backend=2)
+    simt = Context(mlp_backend=1)
+    yield tc, simt
+    tc.close()
+    simt.close()
+
+
+def _mixed_bars(E, F, E64, F64, offs):
+    nat = np.maximum(np.diff(offs), 1)
+    e_err = np.max(np.abs(E - E64) / nat) * 1e3
+    f_err = np.max(np.abs(F - F64)) * 1e3 if len(F) else 0.0
+    assert e_err < E_MEV_ATOM, f"energy error {e_err} meV/atom"
+    assert f_err < F_MEV_A, f"force error {f_err} meV/A"
+
+
+def _compare(tc, simt, text, structs):
+    offs, posn, types, cell = cases.batch(structs)
+    tc.load_text(text)
+    simt.load_text(text)
+    E64, F64, W64 = tc.compute(offs, posn, types, cell, precision=FP64)
+    e64 = tc.atom_energies()
+    d64 = tc.dedg()
+    E, F, Wv = tc.compute(offs, posn, types, cell, precision=MIXED)
+    e = tc.atom_energies()
+    d = tc.dedg()
+    assert np.max(np.abs(e - e64)) < 1e-4, "atom energies"
+    assert np.max(np.abs(d - d64)) < 1e-4 * max(np.max(np.abs(d64)), 1.0), "dE/dG"
+    _mixed_bars(E, F, E64, F64, offs)
+    Es, Fs, _ = simt.compute(offs, posn, types, cell, precision=MIXED)
+    _mixed_bars(E, F, Es, Fs, offs)
+    return e, e64
+
+
+def test_binary_batch_matches_fp64(contexts, tmp_path):
+    tc, simt = contexts
+    structs = cases.small_binary(n_struc=6, seed=13)
+    offs, posn, types, cell = cases.batch(structs)
+    text = cases.config_potential(tc, 2, tmp_path, precondition_batch=(offs, posn, types, cell))
+    _compare(tc, simt, text, structs)
+
+
+def test_many_tiles_per_block(contexts, tmp_path):
+    """More 128-atom tiles of one type than blocks in the grid: the persistent loop is exercised."""
+    tc, simt = contexts
+    structs = cases.W.config2(nstruc=96)
+    offs, posn, types, cell = cases.batch(structs)
+    assert np.sum(types == 0) > 152 * 128
+    text = cases.config_potential(tc, 2, tmp_path, precondition_batch=(offs, posn, types, cell))
+    _compare(tc, simt, text, structs)
+
+
+def test_ragged_and_missing_types(contexts, tmp_path):
+    """Type counts that are not multiples of 128 and a type with no atoms at all."""
+    tc, simt = contexts
+    text = cases.config_potential(tc, 2, tmp_path)
+    one_type = [(x, np.zeros_like(t), R) for (x, t, R) in cases.small_binary(n_struc=2, seed=3)]
+    _compare(tc, simt, text, one_type)
+    _compare(tc, simt, text, cases.tiny_cells())
+
+
+def test_activation_variants(contexts, tmp_path):
+    """Sigmoid / tanh / softplus networks with odd widths (padding to 16 columns)."""
+    tc, simt = contexts
+    text = cases.generic_potential_text()
+    structs = cases.small_binary(n_struc=3, seed=21) + cases.tiny_cells()
+    _compare(tc, simt, text, structs)
+
+
+def test_config1_argon(contexts, tmp_path):
+    tc, simt = contexts
+    text = cases.config_potential(tc, 1, tmp_path)
+    _compare(tc, simt, text, cases.W.config1())
+
+
+def test_too_wide_for_tensor_core_is_reported(contexts, tmp_path):
+    """128-wide networks do not fit the split BF16 image: mlp_backend=2 refuses them, auto uses SIMT."""
+    tc, _ = contexts
+    text = cases.W.config_potential_text(4)
+    with pytest.raises(AnnError):
+        tc.load_text(text)
+    auto = Context()
+    try:
+        auto.load_text(text)
+        offs, posn, types, cell = cases.batch(cases.ternary_box(dims=(6, 6, 4)))
+        E64, F64, _ = auto.compute(offs, posn, types, cell, precision=FP64)
+        E, F, _ = auto.compute(offs, posn, types, cell, precision=MIXED)
+        _mixed_bars(E, F, E64, F64, offs)
+    finally:
+        auto.close()
