@@ -19,7 +19,9 @@ INCLUDE = HERE.parent / "include"
 OBJ = HERE / "_build"
 LIB = HERE / "libann_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# host code is compiled without floating-point contraction so that x86-64 and aarch64 hosts give
+# the same bits (the std::mt19937 / normal_distribution network initialisation and the plans)
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function", "-diag-suppress", "177,550"]
 
 
@@ -54,6 +56,12 @@ def build(verbose_ptxas: bool = False, jobs: int | None = None) -> Path:
     """Compile and link libann_gpu.so; returns its path."""
     nvcc = _nvcc()
     OBJ.mkdir(exist_ok=True)
+    stamp = OBJ / "flags.txt"   # a change of compiler or flags invalidates every object
+    key = " ".join([nvcc, *ARCH, *FLAGS])
+    if not stamp.exists() or stamp.read_text() != key:
+        for o in OBJ.glob("*.o"):
+            o.unlink()
+        stamp.write_text(key)
     srcs = sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(jobs) as ex:

@@ -63,7 +63,7 @@ def test_binary_batch_matches_fp64(contexts, tmp_path):
 def test_many_tiles_per_block(contexts, tmp_path):
     """More 128-atom tiles of one type than blocks in the grid: the persistent loop is exercised."""
     tc, simt = contexts
-    structs = cases.W.config2(nstruc=96)
+    structs = cases.W.config2(nstruc=160)
     offs, posn, types, cell = cases.batch(structs)
     assert np.sum(types == 0) > 152 * 128
     text = cases.config_potential(tc, 2, tmp_path, precondition_batch=(offs, posn, types, cell))
