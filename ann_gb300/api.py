@@ -88,6 +88,7 @@ _SIGS = {
     "ann_md_init": (C.c_int, [_V, C.c_int64, _D, _D, _I32, _D, _D, C.c_double, C.c_double, C.c_int32]),
     "ann_md_run": (C.c_int, [_V, C.c_int32, _D, _D, _I32]),
     "ann_md_get_state": (C.c_int, [_V, _D, _D, _D]),
+    "ann_network_noalloc": (C.c_int, [_V, C.c_int32, _V, _V, _V, _V, C.c_int32]),
 }
 
 ABI_SYMBOLS = tuple(_SIGS)
@@ -380,6 +381,10 @@ class Context:
         pe, ke, rb = C.c_double(), C.c_double(), C.c_int32()
         self._ck(self.lib.ann_md_run(self.h, nsteps, C.byref(pe), C.byref(ke), C.byref(rb)))
         return pe.value, ke.value, rb.value
+
+    def network_noalloc(self, natoms: int, type_ptr: int, G_ptr: int, Eatom_ptr: int, dEdG_ptr: int, precision: int = MIXED):
+        """ann_network_noalloc on device pointers (integers, e.g. torch tensors' data_ptr())."""
+        self._ck(self.lib.ann_network_noalloc(self.h, int(natoms), type_ptr, G_ptr, Eatom_ptr, dEdG_ptr, int(precision)))
 
     def md_state(self):
         x = np.zeros((self._N, 3))

@@ -171,6 +171,24 @@ int ann_md_init(ann_ctx* ctx, int64_t natoms, const double* posn, const double* 
 int ann_md_run(ann_ctx* ctx, int32_t nsteps, double* pe, double* ke, int32_t* rebuilds);
 int ann_md_get_state(ann_ctx* ctx, double* posn, double* vel, double* forces);
 
+/* ---- network pass without device allocation (no counterpart in the reference) ---------------
+ * The network stage of ann_compute alone: energy per atom (network output + vacuum energy) and
+ * dE/dG for symmetry functions that are already on the device. All pointers are device memory:
+ * type_dev[natoms] (int32), G_dev and dEdG_dev [natoms * ann_symm_width] (double for ANN_FP64,
+ * float for ANN_MIXED), Eatom_dev[natoms] (double). Runs on ann_stream(ctx); returns after the
+ * stream has finished and the device status has been checked.
+ * It allocates no device memory, for callers that must not allocate during a step (an MD engine
+ * or plugin host that reserves its device memory up front; cudaMalloc/cudaFree synchronise the
+ * device and can fail mid-run). Its scratch is one static device array of the library,
+ * ANN_NOALLOC_SCRATCH_BYTES, shared by every call on a device: calls that overlap in time
+ * (other threads, contexts or streams) race on it and must be serialised by the caller.
+ * natoms > ANN_NOALLOC_MAX_ATOMS returns ANN_ERR_CAPACITY. The first call on each device resolves
+ * the array's address (cudaGetSymbolAddress); make that first call before any stream capture.  */
+#define ANN_NOALLOC_MAX_ATOMS 262144
+#define ANN_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024 + 4096)
+int ann_network_noalloc(ann_ctx* ctx, int32_t natoms, const int32_t* type_dev, const void* G_dev,
+                        double* Eatom_dev, void* dEdG_dev, int32_t precision);
+
 #ifdef __cplusplus
 }
 #endif
