@@ -17,14 +17,16 @@
 //     (GAUSS, lambda=+-1, zeta=2^k) the reference's exp(-(rij^2+rik^2)/eta^2) factorises into
 //     D_g(j) D_g(k) and |1/2 +- cos/2|^zeta comes from a squaring chain, so no transcendental
 //     is evaluated per triplet.
-//  4. force pass: per triplet the vectors v_j = -dE_i/dr_ij, v_k = -dE_i/dr_ik are added to
-//     per-neighbour shared-memory accumulators; the triplets are visited along diagonals
-//     (k - j constant within a warp step), so the 32 lanes of a step hit 32 different j and 32
-//     different k accumulators. F_i = sum_j v_j, F_j -= v_j (Newton's third law,
-//     nnp.cpp:491,509-516) and the virial W += r_ij (x) v_j are formed once per neighbour.
+//  4. force pass: per triplet the vectors v_j = -dE_i/dr_ij, v_k = -dE_i/dr_ik are summed per
+//     neighbour. Fast path: lanes own neighbours (chunks of 32 per type range) and visit their
+//     partners along a rotation, keeping their own sums in registers and shuffling the partner's
+//     share to its owner lane (no atomics). Generic path: triplets along diagonals with shared
+//     atomics. F_i = sum_j v_j, F_j -= v_j (Newton's third law, nnp.cpp:491,509-516) and the
+//     virial W += r_ij (x) v_j are formed once per neighbour.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 #include "dev_math.cuh"
 #include "kernels.hpp"
 
@@ -127,8 +129,8 @@ struct WarpMem {
     R4* tg;              // tangent of the pair vector (drx, dry, drz, dd) (JVP)
     real* dE;            // dE/dG row (FORCE)
     R4* stage;
-    int32_t *stagej, *jj, *img;
-    uint64_t* bar;
+    int32_t *stagej, *stagej2, *jj, *img;
+    uint64_t* bar;       // two mbarriers, one per staging buffer
     static constexpr int NDP = 2 * NG;
     static __host__ __device__ size_t align(size_t x, size_t a) { return (x + a - 1) / a * a; }
     static __host__ __device__ size_t layout(int cap, int imax, WarpMem* w, unsigned char* base) {
@@ -146,6 +148,7 @@ struct WarpMem {
             o_jj = take(sizeof(int32_t) * cap, 16); o_img = take(sizeof(int32_t) * cap, 16);
         }
         const size_t o_sj = take(sizeof(int32_t) * cap, 16);
+        const size_t o_sj2 = take(sizeof(int32_t) * cap, 16);
         const size_t o_bar = take(16, 16);
         if (w) {
             w->geo = reinterpret_cast<R4*>(base + o_geo); w->stage = reinterpret_cast<R4*>(base + o_stage);
@@ -155,6 +158,7 @@ struct WarpMem {
             w->dE = reinterpret_cast<real*>(base + o_dE);
             w->jj = reinterpret_cast<int32_t*>(base + o_jj); w->img = reinterpret_cast<int32_t*>(base + o_img);
             w->stagej = reinterpret_cast<int32_t*>(base + o_sj);
+            w->stagej2 = reinterpret_cast<int32_t*>(base + o_sj2);
             w->bar = reinterpret_cast<uint64_t*>(base + o_bar);
         }
         return align(off, 128);
@@ -174,6 +178,92 @@ struct DampRec {
     __device__ __forceinline__ real Dp(int g) const { return v[2 * g + 1]; }
 };
 
+// ---------------------------------------------------------------- force pass, fast path
+// One triplet (i; j, k) of a fast-path angular block: v_j = -dE_i/dr_ij and v_k = -dE_i/dr_ik
+// (BasisA::force, basis_angular.cpp:430-563, with the damping factorised per group).
+// cA[s] = dE/dG of slot s, cB[s] = cA[s] * zeta_s * lambda_s / 2.
+template <typename real, int NG, int S>
+__device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, const DampRec<real, NG>& dj,
+                                              const typename V4<real>::T& gk, const DampRec<real, NG>& dk,
+                                              const real (&cA)[S], const real (&cB)[S], real (&vj)[3], real (&vk)[3]) {
+    const real cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
+    const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
+    real pp[4], pm[4], qp[4], qm[4];   // cw^zeta and cw^(zeta-1) for zeta = 1,2,4,8
+    pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
+    pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
+    qp[0] = real(1); qp[1] = cwp; qp[2] = cwp * pp[1]; qp[3] = qp[2] * pp[2];
+    qm[0] = real(1); qm[1] = cwm; qm[2] = cwm * pm[1]; qm[3] = qm[2] * pm[2];
+    real phi = real(0), e0 = real(0), e1 = real(0);
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+        real Ag = real(0), Bg = real(0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            Ag += cA[g * 8 + 2 * q] * pp[q] + cA[g * 8 + 2 * q + 1] * pm[q];
+            Bg += cB[g * 8 + 2 * q] * qp[q] + cB[g * 8 + 2 * q + 1] * qm[q];
+        }
+        phi -= Bg * dj.D(g) * dk.D(g);
+        e0 -= Ag * dj.Dp(g) * dk.D(g);
+        e1 -= Ag * dj.D(g) * dk.Dp(g);
+    }
+    const real idj = gj.w, idk = gk.w;
+    const real cj = -phi * cs * idj + e0, bj = phi * idj;
+    const real ck = -phi * cs * idk + e1, bk = phi * idk;
+    vj[0] = cj * gj.x + bj * gk.x; vj[1] = cj * gj.y + bj * gk.y; vj[2] = cj * gj.z + bj * gk.z;
+    vk[0] = ck * gk.x + bk * gj.x; vk[1] = ck * gk.y + bk * gj.y; vk[2] = ck * gk.z + bk * gj.z;
+}
+
+// One chunk task of the force pass: the neighbours of an atom are split, per type range, into
+// chunks of at most 32, and lane L owns element L of every chunk (chunk start + L). A task is
+// either the triangle of one chunk (tri: pairs a < b of [p0, p0+np)) or the rectangle of two
+// chunks P x Q (np >= nq). Partners follow a rotation (b = a + step mod n), so in every step the
+// 32 lanes touch 32 different partners and each partner is the target of exactly one lane: the
+// contribution to the lane's own element accumulates in registers, the partner's contribution is
+// routed to its owner lane with a shuffle, and each owner adds its totals to the element's
+// shared-memory accumulator once per task. No atomics; every unordered pair is evaluated once.
+template <typename real, int NG, int S, int PASS>
+__device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&cA)[S], const real (&cB)[S], int lane,
+                                           int p0, int np, int q0, int nq, bool tri) {
+    typedef typename V4<real>::T R4;
+    constexpr int NDP = 2 * NG;
+    const bool ownP = lane < np, ownQ = !tri && lane < nq;
+    R4 ga;
+    DampRec<real, NG> da;
+    if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
+    else {
+        ga.x = ga.y = ga.z = ga.w = real(0);
+#pragma unroll
+        for (int q = 0; q < NDP; ++q) da.v[q] = real(0);
+    }
+    real sa[3] = {real(0), real(0), real(0)}, sb[3] = {real(0), real(0), real(0)};
+    const int n = np;
+    const int steps = tri ? np / 2 : np;
+    const int qb = tri ? p0 : q0;
+    int part = tri ? lane : lane - 1;   // partner slot (lane + step) mod n
+    int src = tri ? lane : lane + 1;    // sending lane (lane - step) mod n
+#pragma unroll 1
+    for (int st = tri ? 1 : 0; st <= (tri ? steps : steps - 1); ++st) {
+        if (++part >= n) part -= n;
+        if (--src < 0) src += n;
+        const bool valid = ownP && (tri ? (2 * st < n || lane < steps) : part < nq);
+        real vj[3] = {real(0), real(0), real(0)}, vk[3] = {real(0), real(0), real(0)};
+        if (valid) {
+            const R4 gb = w.geo[qb + part];
+            DampRec<real, NG> db;
+            db.load(w.dp + (qb + part) * NDP);
+            triplet_force<real, NG, S>(ga, da, gb, db, cA, cB, vj, vk);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            sa[c] += vj[c];
+            const real r = __shfl_sync(0xffffffffu, vk[c], src & 31);
+            if (tri) sa[c] += r; else sb[c] += r;
+        }
+    }
+    if (ownP) { w.ax[p0 + lane] += sa[0]; w.ay[p0 + lane] += sa[1]; w.az[p0 + lane] += sa[2]; }
+    if (ownQ) { w.ax[q0 + lane] += sb[0]; w.ay[q0 + lane] += sb[1]; w.az[q0 + lane] += sb[2]; }
+}
+
 // ---------------------------------------------------------------- the kernel
 template <typename real, int NG, bool FAST, int PASS>
 __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
@@ -185,42 +275,68 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
     WarpMem<real, NG, PASS> w;
     WarpMem<real, NG, PASS>::layout(cap, imax, &w, bsm + (size_t)wid * wbytes);
     constexpr int NDP = 2 * NG;
-    if (lane == 0) mbar_init(w.bar, 1);
+    if (lane == 0) { mbar_init(&w.bar[0], 1); mbar_init(&w.bar[1], 1); }
     __syncwarp();
-    uint32_t phase = 0;
+    uint32_t phase = 0;   // bit b: parity of the next phase of barrier b
     const unsigned lt = (1u << lane) - 1u;
     constexpr int S = NG * 8;
 
+    // ---- 1. neighbour rows are staged by bulk asynchronous copies into two buffers: the row of
+    //         the next atom is in flight while the current one is processed. A staged row is
+    //         compacted in place, so a buffer serves as stage and then as the atom's records.
+    R4* const gbuf0 = w.geo;
+    R4* const gbuf1 = w.stage;
+    int32_t* const jbuf0 = w.stagej;
+    int32_t* const jbuf1 = w.stagej2;
+    auto next_atom = [&]() {
+        int v = 0;
+        if (lane == 0) v = (int)atomicAdd(a.counter, 1u);
+        return __shfl_sync(0xffffffffu, v, 0);
+    };
+    auto stage_row = [&](int i, int b) -> bool {   // false: nothing was issued
+        if (i >= a.natoms) return false;
+        const int nin = min(a.nn[i], cap);
+        if (nin <= 0) return false;
+        if (lane == 0) {
+            const size_t row = (size_t)i * cap;
+            const uint32_t b1 = (uint32_t)(nin * sizeof(R4));
+            const uint32_t b2 = (uint32_t)(((nin + 3) / 4) * 16);
+            fence_proxy_async();
+            mbar_expect_tx(&w.bar[b], b1 + b2);
+            bulk_g2s(b ? gbuf1 : gbuf0, reinterpret_cast<const R4*>(a.nr) + row, b1, &w.bar[b]);
+            bulk_g2s(b ? jbuf1 : jbuf0, a.nj + row, b2, &w.bar[b]);
+        }
+        return true;
+    };
+    int nx_i = next_atom(), nx_b = 0;
+    bool nx_issued = stage_row(nx_i, 0);
+
     for (;;) {
-        int i = 0;
-        if (lane == 0) i = (int)atomicAdd(a.counter, 1u);
-        i = __shfl_sync(0xffffffffu, i, 0);
+        const int i = nx_i, cb = nx_b;
+        const bool issued = nx_issued;
         if (i >= a.natoms) break;
+        nx_i = next_atom();
+        nx_b = cb ^ 1;
+        nx_issued = stage_row(nx_i, nx_b);
+        if (issued) {
+            bool done = false;
+            for (int it = 0; it < (1 << 24) && !done; ++it) done = mbar_try_wait(&w.bar[cb], (phase >> cb) & 1u);
+            if (!__all_sync(0xffffffffu, done)) {  // bounded wait gave up: report, drain (bounded), stop
+                if (lane == 0) atomicOr(a.status, (int)ST_TIMEOUT);
+                for (int it = 0; it < (1 << 24); ++it) if (mbar_try_wait(&w.bar[cb], (phase >> cb) & 1u)) break;
+                if (nx_issued)
+                    for (int it = 0; it < (1 << 24); ++it) if (mbar_try_wait(&w.bar[nx_b], (phase >> nx_b) & 1u)) break;
+                return;
+            }
+            phase ^= 1u << cb;
+        }
+        w.geo = cb ? gbuf1 : gbuf0;
+        w.stagej = cb ? jbuf1 : jbuf0;
         const int I = a.type[i];
         if (I < 0 || I >= T) { if (lane == 0) atomicOr(a.status, (int)ST_BAD_TYPE); continue; }
         const DevType& TT = pot.t[I];
         const int nin = min(a.nn[i], cap);
         const size_t row = (size_t)i * cap;
-
-        // ---- 1. stage the neighbour row (bulk async copy) -----------------------------------
-        if (nin > 0) {
-            if (lane == 0) {
-                const uint32_t b1 = (uint32_t)(nin * sizeof(R4));
-                const uint32_t b2 = (uint32_t)(((nin + 3) / 4) * 16);
-                fence_proxy_async();
-                mbar_expect_tx(w.bar, b1 + b2);
-                bulk_g2s(w.stage, reinterpret_cast<const R4*>(a.nr) + row, b1, w.bar);
-                bulk_g2s(w.stagej, a.nj + row, b2, w.bar);
-            }
-            bool done = false;
-            for (int it = 0; it < (1 << 24) && !done; ++it) done = mbar_try_wait(w.bar, phase);
-            if (!__all_sync(0xffffffffu, done)) {  // bounded wait gave up: report, drain (bounded), stop
-                if (lane == 0) atomicOr(a.status, (int)ST_TIMEOUT);
-                for (int it = 0; it < (1 << 24); ++it) if (mbar_try_wait(w.bar, phase)) break;
-                return;
-            }
-            phase ^= 1u;
-        }
         // ---- compaction to d < rc, per-type active ranges, per-neighbour records ---------------
         const real rc = (real)TT.rc;
         real ie2[NG];
@@ -235,7 +351,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 const int e = base_in + e0 + lane;
                 bool keep = false;
                 R4 r4;
-                if (e0 + lane < cin && e < nin) { r4 = w.stage[e]; keep = r4.w < rc; }
+                if (e0 + lane < cin && e < nin) { r4 = w.geo[e]; keep = r4.w < rc; }   // in place: o <= e
                 const unsigned msk = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
                     const int o = pos + __popc(msk & lt);
@@ -280,24 +396,30 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
 
         real* Gout = (PASS == PASS_SYMM) ? a.G + (size_t)i * imax : (PASS == PASS_JVP) ? a.U + (size_t)i * imax : nullptr;
 
-        // ---- 2. radial ----------------------------------------------------------------------------
+        // ---- 2. radial: lanes own neighbours. Symmetry functions / tangents take the block's
+        //         functions in register chunks (parameters hoisted, the radial form resolved once
+        //         per block); the force pass loops over the functions with uniform loads ----------
         for (int J = 0; J < T; ++J) {
             const DevRadial& R = TT.R[J];
             if (R.n == 0) continue;
             const int e0 = tstart[J], e1 = e0 + tcnt[J];
-            if (PASS == PASS_FORCE) {
-                for (int e = e0 + lane; e < e1; e += 32) {
-                    const real dd = w.d[e], f = w.fc[e], g = w.fcg[e];
-                    real amp = real(0);
-                    for (int m = 0; m < R.n; ++m) {
-                        real val, der;
-                        radial_vd<real>(R.name, a.prm.reta[R.pidx + m], a.prm.rs[R.pidx + m], dd, f, g, val, der);
-                        amp -= w.dE[R.off + m] * der;
+            auto block = [&](auto form) {
+                constexpr int NAME = decltype(form)::value;
+                if (PASS == PASS_FORCE) {
+                    for (int e = e0 + lane; e < e1; e += 32) {
+                        const real dd = w.d[e], f = w.fc[e], g = w.fcg[e];
+                        real amp = real(0);
+#pragma unroll 4
+                        for (int m = 0; m < R.n; ++m) {
+                            real val, der;
+                            radial_vd_t<NAME, real>(R.name, __ldg(a.prm.reta + R.pidx + m), __ldg(a.prm.rs + R.pidx + m), dd, f, g, val, der);
+                            amp -= w.dE[R.off + m] * der;
+                        }
+                        const R4 g4 = w.geo[e];
+                        w.ax[e] += amp * g4.x; w.ay[e] += amp * g4.y; w.az[e] += amp * g4.z;
                     }
-                    const R4 g4 = w.geo[e];
-                    w.ax[e] += amp * g4.x; w.ay[e] += amp * g4.y; w.az[e] += amp * g4.z;
+                    return;
                 }
-            } else {
                 for (int m0 = 0; m0 < R.n; m0 += CHUNK) {
                     real eta[CHUNK], rs[CHUNK], acc[CHUNK];
 #pragma unroll
@@ -314,7 +436,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         for (int s = 0; s < CHUNK; ++s) {
                             if (m0 + s < R.n) {
                                 real val, der;
-                                radial_vd<real>(R.name, eta[s], rs[s], dd, f, g, val, der);
+                                radial_vd_t<NAME, real>(R.name, eta[s], rs[s], dd, f, g, val, der);
                                 acc[s] += (PASS == PASS_SYMM) ? val : der * tdd;
                             }
                         }
@@ -325,7 +447,9 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         if (m < R.n) Gout[R.off + m] = v;
                     }
                 }
-            }
+            };
+            if (R.name == R_GAUSSIAN) block(std::integral_constant<int, R_GAUSSIAN>{});
+            else block(std::integral_constant<int, -1>{});
         }
         __syncwarp();
 
@@ -353,9 +477,35 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                             cB[s] = dv * real(1 << k) * ((s & 1) ? real(-0.5) : real(0.5));
                         }
                     }
+                    if (PASS == PASS_FORCE) {
+                        // chunk tasks: triangles of each chunk, rectangles of chunk pairs (larger first)
+                        auto task = [&](int p0, int np, int q0, int nq, bool tri) {
+                            force_task<real, NG, S, PASS>(w, cA, cB, lane, p0, np, q0, nq, tri);
+                        };
+                        if (J == K) {
+                            for (int c0 = 0; c0 < nJ; c0 += 32) {
+                                const int n0 = min(32, nJ - c0);
+                                task(aJ + c0, n0, 0, 0, true);
+                                for (int c1 = c0 + 32; c1 < nJ; c1 += 32) {
+                                    const int n1 = min(32, nJ - c1);
+                                    if (n0 >= n1) task(aJ + c0, n0, aJ + c1, n1, false);
+                                    else task(aJ + c1, n1, aJ + c0, n0, false);
+                                }
+                            }
+                        } else {
+                            for (int c0 = 0; c0 < nJ; c0 += 32) {
+                                const int n0 = min(32, nJ - c0);
+                                for (int c1 = 0; c1 < nK; c1 += 32) {
+                                    const int n1 = min(32, nK - c1);
+                                    if (n0 >= n1) task(aJ + c0, n0, aK + c1, n1, false);
+                                    else task(aK + c1, n1, aJ + c0, n0, false);
+                                }
+                            }
+                        }
+                    }
                     TriIter<ROWS> ti; RectIter<ROWS> ri;
-                    if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane);
-                    for (int t = lane; t < total; t += 32) {
+                    if (PASS != PASS_FORCE) { if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane); }
+                    for (int t = lane; PASS != PASS_FORCE && t < total; t += 32) {
                         int j, k;
                         if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
                         else { j = aJ + ri.q; k = aK + ri.c; ri.adv(); }
@@ -367,6 +517,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         real pp[4], pm[4];
                         pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
                         pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
+                        // symmetry functions and tangents: row order, the warp shares j
                         if (PASS == PASS_SYMM) {
 #pragma unroll
                             for (int g = 0; g < NG; ++g) {
@@ -374,45 +525,24 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
 #pragma unroll
                                 for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
                             }
-                        } else {
-                            real qp[4], qm[4];   // cw^(zeta-1) for zeta = 1,2,4,8
-                            qp[0] = real(1); qp[1] = cwp; qp[2] = cwp * pp[1]; qp[3] = qp[2] * pp[2];
-                            qm[0] = real(1); qm[1] = cwm; qm[2] = cwm * pm[1]; qm[3] = qm[2] * pm[2];
-                            if (PASS == PASS_FORCE) {
-                                real phi = real(0), e0 = real(0), e1 = real(0);
+                            continue;
+                        }
+                        real qp[4], qm[4];   // cw^(zeta-1) for zeta = 1,2,4,8
+                        qp[0] = real(1); qp[1] = cwp; qp[2] = cwp * pp[1]; qp[3] = qp[2] * pp[2];
+                        qm[0] = real(1); qm[1] = cwm; qm[2] = cwm * pm[1]; qm[3] = qm[2] * pm[2];
+                        const R4 tj = w.tg[j], tk = w.tg[k];
+                        const real idj = gj.w, idk = gk.w;
+                        const real dcos = (tj.x * gk.x + tj.y * gk.y + tj.z * gk.z) * idj +
+                                          (tk.x * gj.x + tk.y * gj.y + tk.z * gj.z) * idk - cs * (tj.w * idj + tk.w * idk);
 #pragma unroll
-                                for (int g = 0; g < NG; ++g) {
-                                    real Ag = real(0), Bg = real(0);
+                        for (int g = 0; g < NG; ++g) {
+                            const real DD = dj.D(g) * dk.D(g);
+                            const real dDD = dj.Dp(g) * dk.D(g) * tj.w + dj.D(g) * dk.Dp(g) * tk.w;
 #pragma unroll
-                                    for (int q = 0; q < 4; ++q) {
-                                        Ag += cA[g * 8 + 2 * q] * pp[q] + cA[g * 8 + 2 * q + 1] * pm[q];
-                                        Bg += cB[g * 8 + 2 * q] * qp[q] + cB[g * 8 + 2 * q + 1] * qm[q];
-                                    }
-                                    phi -= Bg * dj.D(g) * dk.D(g);
-                                    e0 -= Ag * dj.Dp(g) * dk.D(g);
-                                    e1 -= Ag * dj.D(g) * dk.Dp(g);
-                                }
-                                const real idj = gj.w, idk = gk.w;
-                                const real cj = -phi * cs * idj + e0, bj = phi * idj;
-                                const real ck = -phi * cs * idk + e1, bk = phi * idk;
-                                atomicAdd(&w.ax[j], cj * gj.x + bj * gk.x); atomicAdd(&w.ay[j], cj * gj.y + bj * gk.y); atomicAdd(&w.az[j], cj * gj.z + bj * gk.z);
-                                atomicAdd(&w.ax[k], ck * gk.x + bk * gj.x); atomicAdd(&w.ay[k], ck * gk.y + bk * gj.y); atomicAdd(&w.az[k], ck * gk.z + bk * gj.z);
-                            } else {  // PASS_JVP
-                                const R4 tj = w.tg[j], tk = w.tg[k];
-                                const real idj = gj.w, idk = gk.w;
-                                const real dcos = (tj.x * gk.x + tj.y * gk.y + tj.z * gk.z) * idj +
-                                                  (tk.x * gj.x + tk.y * gj.y + tk.z * gj.z) * idk - cs * (tj.w * idj + tk.w * idk);
-#pragma unroll
-                                for (int g = 0; g < NG; ++g) {
-                                    const real DD = dj.D(g) * dk.D(g);
-                                    const real dDD = dj.Dp(g) * dk.D(g) * tj.w + dj.D(g) * dk.Dp(g) * tk.w;
-#pragma unroll
-                                    for (int q = 0; q < 4; ++q) {
-                                        const real z = real(1 << q);
-                                        acc[g * 8 + 2 * q] += z * real(0.5) * qp[q] * DD * dcos + pp[q] * dDD;
-                                        acc[g * 8 + 2 * q + 1] += -z * real(0.5) * qm[q] * DD * dcos + pm[q] * dDD;
-                                    }
-                                }
+                            for (int q = 0; q < 4; ++q) {
+                                const real z = real(1 << q);
+                                acc[g * 8 + 2 * q] += z * real(0.5) * qp[q] * DD * dcos + pp[q] * dDD;
+                                acc[g * 8 + 2 * q + 1] += -z * real(0.5) * qm[q] * DD * dcos + pm[q] * dDD;
                             }
                         }
                     }

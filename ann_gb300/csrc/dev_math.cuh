@@ -186,6 +186,20 @@ __device__ __forceinline__ void radial_vd(int name, real eta, real rs, real dr, 
     }
 }
 
+// radial_vd with the form fixed at compile time when it is GAUSSIAN (NAME = R_GAUSSIAN), so that
+// unrolled loops over a block's functions carry no per-function dispatch; NAME = -1: any form
+template <int NAME, typename real>
+__device__ __forceinline__ void radial_vd_t(int name, real eta, real rs, real dr, real fc, real fcg, real& val, real& der) {
+    if (NAME == R_GAUSSIAN) {
+        const real a = eta * (dr - rs);
+        const real e = M<real>::bexp(-a * a);
+        val = e * fc;
+        der = e * (real(-2) * eta * a * fc + fcg);
+    } else {
+        radial_vd<real>(name, eta, rs, dr, fc, fcg, val, der);
+    }
+}
+
 // ------------------------------------------------------------------ angular damping of the generic path
 // returns the radial damping value h(r2s) of one angular function and dh/dr2s-based factors
 // following basis_angular.cpp:212-364: value part multiplies |1/2+lambda/2 cos|^zeta * fc_j fc_k,
