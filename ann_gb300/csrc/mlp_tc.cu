@@ -93,9 +93,52 @@ static __device__ __forceinline__ void put8(uint8_t* hi, uint8_t* lo, int r, int
     if (lo) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-__global__ void __launch_bounds__(TC_M, 1) k_mlp_tc(const __grid_constant__ TcType tt, const TcArgs a) {
+// activation value and first derivative with the hardware approximations (exp2 / log2 / rcp);
+// absolute errors ~1e-7, far inside the FP32 path's tolerance (nn.cpp:149-236 forms)
+static __device__ __forceinline__ void act_fast(int neuron, float c, float z, float& a, float& d) {
+    switch (neuron) {
+        case N_SIGMOID: {
+            const float e = __expf(-c * fabsf(z)), r = __frcp_rn(1.0f + e);
+            a = (z >= 0.0f) ? r : e * r;
+            d = c * e * r * r;
+            return;
+        }
+        case N_TANH: {
+            const float e = __expf(-2.0f * c * fabsf(z));
+            const float t = copysignf((1.0f - e) * __frcp_rn(1.0f + e), z);
+            a = t;
+            d = c * (1.0f - t * t);
+            return;
+        }
+        case N_SOFTPLUS: {
+            const float e = __expf(-c * fabsf(z)), r = __frcp_rn(1.0f + e);
+            a = fmaxf(z, 0.0f) + (__logf(1.0f + e) - (float)kLOG2) / c;
+            d = (z > 0.0f) ? r : e * r;
+            return;
+        }
+        default: a = z; d = 1.0f; return;
+    }
+}
+
+static __device__ __forceinline__ void tc_st16(uint32_t taddr, const float (&v)[16]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
+                 ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+                   "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+                   "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+                   "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+                 : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// TC_GROUPS warps share each TMEM lane quadrant (warp w: rows 32*(w%4).., column chunks c with
+// c % TC_GROUPS == w / 4), so an epilogue runs on TC_GROUPS * 4 warps
+constexpr int TC_THREADS = TC_M * TC_GROUPS;
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant__ TcType tt, const TcArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    const int t = threadIdx.x, warp = t >> 5;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int quad = warp & 3, grp = warp >> 2;
+    const int r = quad * 32 + lane;                 // the thread's row of the tile (= TMEM lane)
     const int a0 = a.tstart[a.type], cnt = a.tstart[a.type + 1] - a0;
     const int ntiles = (cnt + TC_M - 1) / TC_M;
     if ((int)blockIdx.x >= ntiles) return;
@@ -106,6 +149,7 @@ __global__ void __launch_bounds__(TC_M, 1) k_mlp_tc(const __grid_constant__ TcTy
     uint8_t* Alo = (tt.split >= 2) ? Ahi + abytes : nullptr;
     uint64_t* bar = reinterpret_cast<uint64_t*>(Ahi + abytes * (tt.split >= 2 ? 2 : 1));
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
+    float* ered = reinterpret_cast<float*>(bar + 4);      // [TC_GROUPS][TC_M] energy partial sums
     const uint32_t asbo = (uint32_t)tt.wmax * 16u;   // (wmax / 8) * 128
 
     if (t == 0) { tc_mbar_init(&bar[0]); tc_mbar_init(&bar[1]); }
@@ -127,7 +171,7 @@ __global__ void __launch_bounds__(TC_M, 1) k_mlp_tc(const __grid_constant__ TcTy
     bool mma_pending = false;       // an MMA group whose completion was not observed
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     uint32_t mphase = 0;
 
     const float* inpw = reinterpret_cast<const float*>(img + tt.inpw);
@@ -162,19 +206,20 @@ __global__ void __launch_bounds__(TC_M, 1) k_mlp_tc(const __grid_constant__ TcTy
     };
 
     for (int tile = blockIdx.x; tile < ntiles && good; tile += gridDim.x) {
-        const int row = tile * TC_M + t;
+        const int row = tile * TC_M + r;
         const int at = (row < cnt) ? a.tlist[a0 + row] : -1;
-        // ---- A0 = inpw * (G + inpb)
-        for (int c0 = 0; c0 < tt.K0; c0 += 8) {
+        const float* Grow = a.G + (size_t)(at >= 0 ? at : 0) * a.imax;
+        // ---- A0 = inpw * (G + inpb), 8-column chunks shared out over the groups
+        for (int c0 = grp * 8; c0 < tt.K0; c0 += 8 * TC_GROUPS) {
             float v[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int k = c0 + q;
-                v[q] = (at >= 0 && k < tt.nin) ? inpw[k] * (a.G[(size_t)at * a.imax + k] + inpb[k]) : 0.0f;
+                v[q] = (at >= 0 && k < tt.nin) ? inpw[k] * (Grow[k] + inpb[k]) : 0.0f;
             }
-            put8(Ahi, Alo, t, c0, asbo, v);
+            put8(Ahi, Alo, r, c0, asbo, v);
         }
-        // ---- forward
+        // ---- forward; f'(z) replaces z in TMEM for the backward pass
         float epart = 0.0f;
         for (int l = 0; l < tt.nhidden && good; ++l) {
             const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
@@ -183,56 +228,58 @@ __global__ void __launch_bounds__(TC_M, 1) k_mlp_tc(const __grid_constant__ TcTy
             if (!good) break;
             const float* bias = reinterpret_cast<const float*>(img + tt.bias[l]);
             const bool last = (l == tt.nhidden - 1);
-            for (int c0 = 0; c0 < N; c0 += 16) {
-                float v[16];
-                tc_ld16(tmem + lane_off + (uint32_t)(tt.fwd_col[l] + c0), v);
-                float o[16];
+            for (int c0 = grp * 16; c0 < N; c0 += 16 * TC_GROUPS) {
+                float v[16], o[16];
+                const uint32_t ta = tmem + lane_off + (uint32_t)(tt.fwd_col[l] + c0);
+                tc_ld16(ta, v);
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     const int col = c0 + q;
-                    float av, d1, d2;
-                    act_fd<float>(tt.neuron, c, v[q] + bias[col], av, d1, d2);
+                    float av, d1;
+                    act_fast(tt.neuron, c, v[q] + bias[col], av, d1);
                     if (col >= tt.nodes[l]) { av = 0.0f; d1 = 0.0f; }
                     if (last) { epart += wlast[col] * av; o[q] = tt.outw * wlast[col] * d1; }
                     else o[q] = av;
+                    v[q] = d1;
                 }
-                put8(Ahi, Alo, t, c0, asbo, o);
-                put8(Ahi, Alo, t, c0 + 8, asbo, o + 8);
+                if (!last) tc_st16(ta, v);
+                put8(Ahi, Alo, r, c0, asbo, o);
+                put8(Ahi, Alo, r, c0 + 8, asbo, o + 8);
             }
         }
         if (!good) break;
-        if (at >= 0) a.Eatom[at] = (double)(tt.outb + tt.outw * (epart + tt.blast)) + tt.evac;
+        ered[grp * TC_M + r] = epart;
         // ---- backward: A holds delta of hidden layer l
         for (int l = tt.nhidden - 1; l >= 0 && good; --l) {
             const int Nout = (l == 0) ? tt.K0 : tt.width[l - 1];
             good = gemm(tt.bwd_hi[l], tt.bwd_lo[l], tt.width[l], Nout, (uint32_t)tt.bwd_col);
             if (!good) break;
-            for (int c0 = 0; c0 < Nout; c0 += 16) {
-                float g[16];
-                tc_ld16(tmem + lane_off + (uint32_t)(tt.bwd_col + c0), g);
+            if (l == tt.nhidden - 1 && grp == 0 && at >= 0) {   // ered is complete after the GEMM's barrier
+                float e = 0.0f;
+#pragma unroll
+                for (int g = 0; g < TC_GROUPS; ++g) e += ered[g * TC_M + r];
+                a.Eatom[at] = (double)(tt.outb + tt.outw * (e + tt.blast)) + tt.evac;
+            }
+            for (int c0 = grp * 16; c0 < Nout; c0 += 16 * TC_GROUPS) {
+                float gv[16];
+                tc_ld16(tmem + lane_off + (uint32_t)(tt.bwd_col + c0), gv);
                 if (l > 0) {
-                    float z[16];
-                    tc_ld16(tmem + lane_off + (uint32_t)(tt.fwd_col[l - 1] + c0), z);
-                    const float* bias = reinterpret_cast<const float*>(img + tt.bias[l - 1]);
-                    float o[16];
+                    float dz[16], o[16];
+                    tc_ld16(tmem + lane_off + (uint32_t)(tt.fwd_col[l - 1] + c0), dz);
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const int col = c0 + q;
-                        float av, d1, d2;
-                        act_fd<float>(tt.neuron, c, z[q] + bias[col], av, d1, d2);
-                        o[q] = (col < tt.nodes[l - 1]) ? g[q] * d1 : 0.0f;
-                    }
-                    put8(Ahi, Alo, t, c0, asbo, o);
-                    put8(Ahi, Alo, t, c0 + 8, asbo, o + 8);
+                    for (int q = 0; q < 16; ++q) o[q] = gv[q] * dz[q];   // f' is zero in padded columns
+                    put8(Ahi, Alo, r, c0, asbo, o);
+                    put8(Ahi, Alo, r, c0 + 8, asbo, o + 8);
                 } else if (at >= 0) {
+                    float* drow = a.dEdG + (size_t)at * a.imax;
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
                         const int col = c0 + q;
-                        if (col < a.imax) a.dEdG[(size_t)at * a.imax + col] = (col < tt.nin) ? g[q] * inpw[col] : 0.0f;
+                        if (col < a.imax) drow[col] = (col < tt.nin) ? gv[q] * inpw[col] : 0.0f;
                     }
                 }
             }
-            if (l == 0 && at >= 0)
+            if (l == 0 && at >= 0 && grp == 0)
                 for (int col = tt.K0; col < a.imax; ++col) a.dEdG[(size_t)at * a.imax + col] = 0.0f;
         }
     }
@@ -252,7 +299,7 @@ void launch_mlp_tc(const TcType& tt, const TcArgs& a, size_t smem, cudaStream_t 
     if (a.natoms <= 0) return;
     int grid = (a.natoms + TC_M - 1) / TC_M;
     grid = std::min(grid, 152);
-    ++::ann::g_launch_counter, k_mlp_tc<<<grid, TC_M, smem, st>>>(tt, a);
+    ++::ann::g_launch_counter, k_mlp_tc<<<grid, TC_THREADS, smem, st>>>(tt, a);
 }
 void configure_mlp_tc(int maxsmem) { set_max_dynamic_smem(k_mlp_tc, maxsmem); }
 

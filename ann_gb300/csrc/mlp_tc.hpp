@@ -10,6 +10,9 @@ namespace ann {
 
 constexpr int TC_M = 128;          // atoms per tile (one TMEM lane each)
 constexpr int TC_MAXH = 5;         // hidden layers
+constexpr int TC_GROUPS = 4;       // warps per TMEM lane quadrant (the epilogue's column split)
+// shared memory after the A tiles: 2 mbarriers, the TMEM address, per-group energy partials
+constexpr int TC_TAIL_BYTES = 32 + 4 * TC_GROUPS * TC_M;
 
 // Operands live in shared memory in the canonical K-major no-swizzle layout of tcgen05:
 // 8-row x 16-byte core matrices (128 B each); along K adjacent core matrices are 128 B apart

@@ -32,7 +32,7 @@ static size_t canon(int r, int k, int K) { return (size_t)(r / 8) * (K / 8) * 12
 size_t TcPlan::smem_bytes(int type) const {
     const TcType& tt = t[type];
     const size_t a = (size_t)TC_M * tt.wmax * 2 * (tt.split >= 2 ? 2 : 1);
-    const size_t need = ((size_t)tt.img_bytes + 127) / 128 * 128 + a + 128;
+    const size_t need = ((size_t)tt.img_bytes + 127) / 128 * 128 + a + TC_TAIL_BYTES;
     const size_t allowed = 512 / (size_t)std::max(tt.tmem_cols, 32);
     return std::max(need, (size_t)smem_per_sm / (allowed + 1) + 1);
 }
@@ -83,7 +83,7 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
         vec += (size_t)tt.width[tt.nhidden - 1] * 4 + (size_t)tt.K0 * 8;
         auto total = [&](int split) {
             const size_t img = bf * (split == 3 ? 2 : 1) + vec + 16 * (4 * TC_MAXH + 4);
-            return (img + 127) / 128 * 128 + (size_t)TC_M * tt.wmax * 2 * (split >= 2 ? 2 : 1) + 128;
+            return (img + 127) / 128 * 128 + (size_t)TC_M * tt.wmax * 2 * (split >= 2 ? 2 : 1) + TC_TAIL_BYTES;
         };
         // both operands split (three MMAs per k-step) keep the products within ~1e-5 relative of
         // FP32; a single-BF16 weight image (2^-9 relative) is not accurate enough for the forces,
