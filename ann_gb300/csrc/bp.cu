@@ -13,10 +13,14 @@
 //  2. radial functions: lanes own neighbours and keep the block's functions in registers
 //     (symmetry functions / tangents, then a transposing warp reduction), or own neighbours and
 //     loop over functions (force pass).
-//  3. angular functions: lanes own (j,k) triplets of each (J,K) type block. In the fast path
-//     (GAUSS, lambda=+-1, zeta=2^k) the reference's exp(-(rij^2+rik^2)/eta^2) factorises into
-//     D_g(j) D_g(k) and |1/2 +- cos/2|^zeta comes from a squaring chain, so no transcendental
-//     is evaluated per triplet.
+//  3. angular functions of each (J,K) type block. In the fast path (GAUSS, lambda=+-1,
+//     zeta=2^k) the reference's exp(-(rij^2+rik^2)/eta^2) factorises into D_g(j) D_g(k) and
+//     |1/2 +- cos/2|^zeta comes from a squaring chain (symmetry functions) or from a degree-8
+//     polynomial in cos (force pass), so no transcendental is evaluated per triplet. There the
+//     neighbours of a type range are split into chunks of 32 and lane L owns element L of every
+//     chunk; a chunk's triangle and each pair of chunks are walked along rotations (partner =
+//     own + step mod n), so the lane's own record stays in registers. The generic path and the
+//     tangent pass hand out (j,k) triplets to lanes instead.
 //  4. force pass: per triplet the vectors v_j = -dE_i/dr_ij, v_k = -dE_i/dr_ik are summed per
 //     neighbour. Fast path: lanes own neighbours (chunks of 32 per type range) and visit their
 //     partners along a rotation, keeping their own sums in registers and shuffling the partner's
@@ -181,36 +185,54 @@ struct DampRec {
 // ---------------------------------------------------------------- force pass, fast path
 // One triplet (i; j, k) of a fast-path angular block: v_j = -dE_i/dr_ij and v_k = -dE_i/dr_ik
 // (BasisA::force, basis_angular.cpp:430-563, with the damping factorised per group).
-// cA[s] = dE/dG of slot s, cB[s] = cA[s] * zeta_s * lambda_s / 2.
-template <typename real, int NG, int S>
+// The block's weighted sum over slots, A_g(cos) = sum_s dE/dG_s |1/2 + lambda_s cos/2|^zeta_s,
+// is a polynomial of degree 8 in cos (zeta = 1,2,4,8; the bases are never negative for
+// |cos| <= 1); al[g][p] holds its coefficients and Horner's rule gives A_g and dA_g/dcos together.
+template <typename real, int NG>
 __device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, const DampRec<real, NG>& dj,
                                               const typename V4<real>::T& gk, const DampRec<real, NG>& dk,
-                                              const real (&cA)[S], const real (&cB)[S], real (&vj)[3], real (&vk)[3]) {
+                                              const real (&al)[NG][9], real (&vj)[3], real (&vk)[3]) {
     const real cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
-    const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
-    real pp[4], pm[4], qp[4], qm[4];   // cw^zeta and cw^(zeta-1) for zeta = 1,2,4,8
-    pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
-    pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
-    qp[0] = real(1); qp[1] = cwp; qp[2] = cwp * pp[1]; qp[3] = qp[2] * pp[2];
-    qm[0] = real(1); qm[1] = cwm; qm[2] = cwm * pm[1]; qm[3] = qm[2] * pm[2];
     real phi = real(0), e0 = real(0), e1 = real(0);
 #pragma unroll
     for (int g = 0; g < NG; ++g) {
-        real Ag = real(0), Bg = real(0);
+        real A = al[g][8], B = real(0);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            Ag += cA[g * 8 + 2 * q] * pp[q] + cA[g * 8 + 2 * q + 1] * pm[q];
-            Bg += cB[g * 8 + 2 * q] * qp[q] + cB[g * 8 + 2 * q + 1] * qm[q];
-        }
-        phi -= Bg * dj.D(g) * dk.D(g);
-        e0 -= Ag * dj.Dp(g) * dk.D(g);
-        e1 -= Ag * dj.D(g) * dk.Dp(g);
+        for (int p = 7; p >= 0; --p) { B = B * cs + A; A = A * cs + al[g][p]; }
+        const real DD = dj.D(g) * dk.D(g);
+        phi -= B * DD;
+        e0 -= A * dj.Dp(g) * dk.D(g);
+        e1 -= A * dj.D(g) * dk.Dp(g);
     }
     const real idj = gj.w, idk = gk.w;
     const real cj = -phi * cs * idj + e0, bj = phi * idj;
     const real ck = -phi * cs * idk + e1, bk = phi * idk;
     vj[0] = cj * gj.x + bj * gk.x; vj[1] = cj * gj.y + bj * gk.y; vj[2] = cj * gj.z + bj * gk.z;
     vk[0] = ck * gk.x + bk * gj.x; vk[1] = ck * gk.y + bk * gj.y; vk[2] = ck * gk.z + bk * gj.z;
+}
+
+// coefficients of A_g(cos) from the block's dE/dG per slot (slot g*8 + 2q + (lambda < 0), zeta = 2^q):
+// ((1 +- x)/2)^zeta = 2^-zeta sum_p C(zeta, p) (+-x)^p
+template <typename real, int NG>
+__device__ __forceinline__ void angular_poly(const real* dE, const int32_t* slot2ref, int sidx, real (&al)[NG][9]) {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+#pragma unroll
+        for (int p = 0; p < 9; ++p) al[g][p] = real(0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int rp = slot2ref[sidx + g * 8 + 2 * q], rm = slot2ref[sidx + g * 8 + 2 * q + 1];
+            const real cp = (rp >= 0) ? dE[rp] : real(0), cm = (rm >= 0) ? dE[rm] : real(0);
+            const int z = 1 << q;
+            real binom = real(1);                      // C(z, p)
+            const real scale = real(1) / real(1 << z);
+#pragma unroll
+            for (int p = 0; p <= 8; ++p) {
+                if (p <= z) al[g][p] += scale * binom * ((p & 1) ? cp - cm : cp + cm);
+                binom = binom * real(z - p) / real(p + 1);
+            }
+        }
+    }
 }
 
 // One chunk task of the force pass: the neighbours of an atom are split, per type range, into
@@ -221,8 +243,8 @@ __device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, co
 // contribution to the lane's own element accumulates in registers, the partner's contribution is
 // routed to its owner lane with a shuffle, and each owner adds its totals to the element's
 // shared-memory accumulator once per task. No atomics; every unordered pair is evaluated once.
-template <typename real, int NG, int S, int PASS>
-__device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&cA)[S], const real (&cB)[S], int lane,
+template <typename real, int NG, int PASS>
+__device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&al)[NG][9], int lane,
                                            int p0, int np, int q0, int nq, bool tri) {
     typedef typename V4<real>::T R4;
     constexpr int NDP = 2 * NG;
@@ -251,7 +273,7 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
             const R4 gb = w.geo[qb + part];
             DampRec<real, NG> db;
             db.load(w.dp + (qb + part) * NDP);
-            triplet_force<real, NG, S>(ga, da, gb, db, cA, cB, vj, vk);
+            triplet_force<real, NG>(ga, da, gb, db, al, vj, vk);
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -262,6 +284,42 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     }
     if (ownP) { w.ax[p0 + lane] += sa[0]; w.ay[p0 + lane] += sa[1]; w.az[p0 + lane] += sa[2]; }
     if (ownQ) { w.ax[q0 + lane] += sb[0]; w.ay[q0 + lane] += sb[1]; w.az[q0 + lane] += sb[2]; }
+}
+
+// The same chunk tasks for the symmetry functions of a fast-path block: the lane's own neighbour
+// stays in registers and only the partner's record is read per pair; acc[s] collects slot s.
+template <typename real, int NG, int S, int PASS>
+__device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real (&acc)[S], int lane, int p0, int np, int q0, int nq,
+                                          bool tri) {
+    typedef typename V4<real>::T R4;
+    constexpr int NDP = 2 * NG;
+    if (lane >= np) return;
+    const R4 ga = w.geo[p0 + lane];
+    DampRec<real, NG> da;
+    da.load(w.dp + (p0 + lane) * NDP);
+    const int n = np;
+    const int steps = tri ? np / 2 : np;
+    const int qb = tri ? p0 : q0;
+    int part = tri ? lane : lane - 1;
+#pragma unroll 1
+    for (int st = tri ? 1 : 0; st <= (tri ? steps : steps - 1); ++st) {
+        if (++part >= n) part -= n;
+        if (tri ? (2 * st == n && lane >= steps) : part >= nq) continue;
+        const R4 gb = w.geo[qb + part];
+        DampRec<real, NG> db;
+        db.load(w.dp + (qb + part) * NDP);
+        const real cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
+        const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
+        real pp[4], pm[4];
+        pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
+        pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+            const real DD = da.D(g) * db.D(g);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
+        }
+    }
 }
 
 // ---------------------------------------------------------------- the kernel
@@ -465,22 +523,15 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 if (FAST) {
                     // ------------------------------------------------ fast path (GAUSS, zeta=2^k)
                     real acc[S];
-                    real cA[S], cB[S];
 #pragma unroll
-                    for (int s = 0; s < S; ++s) {
-                        acc[s] = real(0);
-                        if (PASS == PASS_FORCE) {
-                            const int ref = a.prm.slot2ref[A.sidx + s];
-                            const real dv = (ref >= 0) ? w.dE[A.off + ref] : real(0);
-                            const int k = (s & 7) >> 1;
-                            cA[s] = dv;
-                            cB[s] = dv * real(1 << k) * ((s & 1) ? real(-0.5) : real(0.5));
-                        }
-                    }
-                    if (PASS == PASS_FORCE) {
+                    for (int s = 0; s < S; ++s) acc[s] = real(0);
+                    if (PASS != PASS_JVP) {
                         // chunk tasks: triangles of each chunk, rectangles of chunk pairs (larger first)
+                        real al[NG][9];
+                        if (PASS == PASS_FORCE) angular_poly<real, NG>(w.dE + A.off, a.prm.slot2ref, A.sidx, al);
                         auto task = [&](int p0, int np, int q0, int nq, bool tri) {
-                            force_task<real, NG, S, PASS>(w, cA, cB, lane, p0, np, q0, nq, tri);
+                            if (PASS == PASS_FORCE) force_task<real, NG, PASS>(w, al, lane, p0, np, q0, nq, tri);
+                            else symm_task<real, NG, S, PASS>(w, acc, lane, p0, np, q0, nq, tri);
                         };
                         if (J == K) {
                             for (int c0 = 0; c0 < nJ; c0 += 32) {
@@ -504,8 +555,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         }
                     }
                     TriIter<ROWS> ti; RectIter<ROWS> ri;
-                    if (PASS != PASS_FORCE) { if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane); }
-                    for (int t = lane; PASS != PASS_FORCE && t < total; t += 32) {
+                    if (PASS == PASS_JVP) { if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane); }
+                    for (int t = lane; PASS == PASS_JVP && t < total; t += 32) {
                         int j, k;
                         if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
                         else { j = aJ + ri.q; k = aK + ri.c; ri.adv(); }
@@ -517,16 +568,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         real pp[4], pm[4];
                         pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
                         pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
-                        // symmetry functions and tangents: row order, the warp shares j
-                        if (PASS == PASS_SYMM) {
-#pragma unroll
-                            for (int g = 0; g < NG; ++g) {
-                                const real DD = dj.D(g) * dk.D(g);
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
-                            }
-                            continue;
-                        }
+                        // tangents (training): row order, the warp shares j
                         real qp[4], qm[4];   // cw^(zeta-1) for zeta = 1,2,4,8
                         qp[0] = real(1); qp[1] = cwp; qp[2] = cwp * pp[1]; qp[3] = qp[2] * pp[2];
                         qm[0] = real(1); qm[1] = cwm; qm[2] = cwm * pm[1]; qm[3] = qm[2] * pm[2];
