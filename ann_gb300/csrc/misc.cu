@@ -72,12 +72,26 @@ void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp,
 }
 
 // ---------------------------------------------------------------- per-type atom lists
+// slots within each type: lanes of a warp with the same type are counted together
+// (match + popc), the block's counts go to global memory with one atomic per type
 __global__ void k_type_count(int n, int ntypes, const int32_t* type, int32_t* tcount, int32_t* slot, int32_t* status) {
+    __shared__ int32_t hist[MAXT], base[MAXT];
+    if (threadIdx.x < MAXT) hist[threadIdx.x] = 0;
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int t = type[i];
-    if (t < 0 || t >= ntypes) { atomicOr(status, (int)ST_BAD_TYPE); slot[i] = -1; return; }
-    slot[i] = atomicAdd(&tcount[t], 1);
+    int t = (i < n) ? type[i] : -1;
+    if (i < n && (t < 0 || t >= ntypes)) { atomicOr(status, (int)ST_BAD_TYPE); t = -1; }
+    const unsigned peers = __match_any_sync(0xffffffffu, t);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int first = 0;
+    if (t >= 0 && lane == leader) first = atomicAdd(&hist[t], __popc(peers));
+    first = __shfl_sync(0xffffffffu, first, leader);
+    const int local = first + __popc(peers & ((1u << lane) - 1u));
+    __syncthreads();
+    if (threadIdx.x < ntypes) base[threadIdx.x] = hist[threadIdx.x] ? atomicAdd(&tcount[threadIdx.x], hist[threadIdx.x]) : 0;
+    __syncthreads();
+    if (i < n) slot[i] = (t >= 0) ? base[t] + local : -1;
 }
 __global__ void k_type_start(int ntypes, const int32_t* tcount, int32_t* tstart) {
     if (threadIdx.x == 0) { int32_t r = 0; for (int t = 0; t < ntypes; ++t) { tstart[t] = r; r += tcount[t]; } tstart[ntypes] = r; }

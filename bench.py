@@ -13,6 +13,9 @@ symmetry functions, networks, forces, virials, per-structure energies).
   fp64   : the plain FP64 GPU form on the same batch (the 5x target's denominator).
   --impl reference : the CPU path (the FP64 oracle that restates the reference's code) on all host
            cores, on a bounded sample of the same workload.
+  training : structures/s of one training step (loss, adjoint, parameter gradient) on the
+           64-structure batch with LJ labels, mixed and FP64 (secondary keys).
+  md     : atom-steps/s and energy drift of velocity-Verlet MD on the 262,144-atom FCC Ar box.
 Multi-GPU: structures are independent, so each rank runs its own full batch (weak scaling);
 no collective on the data path, a barrier and a max over ranks around the timed region.
 """
@@ -158,6 +161,62 @@ def cpu_reference(offs, posn, types, cell, pot_text, budget_s=12.0, steps=1, war
                        f"structures block-distributed over threads (thread::Dist rule)")
 
 
+def training_leg(dev, steps=10, warmup=3):
+    """Training throughput on the 64-structure binary batch with Lennard-Jones labels: one
+    ann_train_forward + ann_train_backward (loss, adjoint, parameter gradient) per step, host
+    arrays in and the gradient out, wall-clock per step."""
+    from ann_gb300 import FP64, MIXED, Context
+    from ann_gb300 import workloads as WL
+    from ann_gb300.api import pack_batch
+    structs = WL.config3()
+    offs, posn, types, cell = pack_batch(structs)
+    Eref, Fref = WL.lennard_jones(structs)
+    Fref = np.concatenate(Fref)
+    ctx = Context(device=dev)
+    WL.make_potential(ctx, 3)
+    WL.precondition(ctx, offs, posn, types, cell)
+    out = {"workload": f"{len(structs)} binary structures, N~U{{32..256}} ({int(offs[-1])} atoms), LJ labels, "
+                       "loss = mean (dE/N)^2 + 0.1 mean |dF|^2/3",
+           "unit": "structures/s", "nparams": int(ctx.nparams)}
+    for name, prec in (("mixed", MIXED), ("fp64", FP64)):
+        for _ in range(warmup):
+            ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
+            ctx.train_backward()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            loss = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
+            ctx.train_backward()
+        dt = (time.perf_counter() - t0) / steps
+        out[name] = len(structs) / dt
+        out[name + "_ms_per_step"] = dt * 1e3
+        out[name + "_loss"] = float(loss[0])
+    ctx.close()
+    return out
+
+
+def md_leg(dev, steps=1000, warmup=20):
+    """Velocity-Verlet MD of the 262,144-atom FCC argon box (16-32-32-1 tanh networks, dt = 2 fs,
+    list cutoff rc + 0.5 A, rebuild at 0.25 A displacement), mixed precision: atom-steps/s and
+    the total-energy drift."""
+    from ann_gb300 import MIXED, Context
+    from ann_gb300 import workloads as WL
+    x, v, t, R = WL.config5()
+    ctx = Context(device=dev)
+    WL.make_potential(ctx, 5)
+    ctx.md_init(x, v, t, R, np.array([WL.MASS["Ar"]]), dt_fs=2.0, skin=0.5, precision=MIXED)
+    ctx.md_run(warmup)
+    pe0, ke0, _ = ctx.md_run(1)
+    t0 = time.perf_counter()
+    pe, ke, rebuilds = ctx.md_run(steps)
+    dt = time.perf_counter() - t0
+    n = len(t)
+    ps = steps * 2.0e-3
+    ctx.close()
+    return {"workload": f"FCC Ar {n} atoms, 80 K, dt 2 fs, {steps} steps", "atom_steps_per_s": n * steps / dt,
+            "ms_per_step": dt / steps * 1e3, "rebuilds": int(rebuilds),
+            "drift_mev_atom_ps": float((pe + ke - pe0 - ke0) / n * 1e3 / ps), "precision": "mixed"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -166,6 +225,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nstruc", type=int, default=256)
+    ap.add_argument("--no-extras", action="store_true", help="skip the training and MD legs")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     W_ = max(args.warmup, 3)
@@ -324,6 +384,9 @@ def main():
             "e2e": {"value": N / t_e2e, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk, "wall_s_timed_region": t_wall}
+    if rank == 0 and world == 1 and not args.no_extras:
+        line["training"] = training_leg(dev)
+        line["md"] = md_leg(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(offs, posn, types, cell, pot_text)
     if rank == 0:
