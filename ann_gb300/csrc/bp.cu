@@ -173,10 +173,23 @@ struct WarpMem {
 // D/Dp pairs of one neighbour for the fast path
 template <typename real, int NG>
 struct DampRec {
-    real v[2 * NG];
+    alignas(16) real v[2 * NG];
+    // records are 2*NG reals at a 2*NG-real stride from a 16-byte aligned base: vector loads
     __device__ __forceinline__ void load(const real* p) {
+        constexpr int B = 2 * NG * (int)sizeof(real);
+        if constexpr (B % 16 == 0) {
 #pragma unroll
-        for (int q = 0; q < 2 * NG; ++q) v[q] = p[q];
+            for (int k = 0; k < B / 16; ++k) reinterpret_cast<float4*>(v)[k] = reinterpret_cast<const float4*>(p)[k];
+        } else if constexpr (B == 8) {
+            *reinterpret_cast<float2*>(v) = *reinterpret_cast<const float2*>(p);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 2 * NG; ++q) v[q] = p[q];
+        }
+    }
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int q = 0; q < 2 * NG; ++q) v[q] = real(0);
     }
     __device__ __forceinline__ real D(int g) const { return v[2 * g]; }
     __device__ __forceinline__ real Dp(int g) const { return v[2 * g + 1]; }
@@ -243,44 +256,41 @@ __device__ __forceinline__ void angular_poly(const real* dE, const int32_t* slot
 // contribution to the lane's own element accumulates in registers, the partner's contribution is
 // routed to its owner lane with a shuffle, and each owner adds its totals to the element's
 // shared-memory accumulator once per task. No atomics; every unordered pair is evaluated once.
-template <typename real, int NG, int PASS>
+template <typename real, int NG, int PASS, bool TRI>
 __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&al)[NG][9], int lane,
-                                           int p0, int np, int q0, int nq, bool tri) {
+                                           int p0, int np, int q0, int nq) {
     typedef typename V4<real>::T R4;
     constexpr int NDP = 2 * NG;
-    const bool ownP = lane < np, ownQ = !tri && lane < nq;
+    const bool ownP = lane < np, ownQ = !TRI && lane < nq;
     R4 ga;
     DampRec<real, NG> da;
     if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
-    else {
-        ga.x = ga.y = ga.z = ga.w = real(0);
-#pragma unroll
-        for (int q = 0; q < NDP; ++q) da.v[q] = real(0);
-    }
+    else { ga.x = ga.y = ga.z = ga.w = real(0); da.zero(); }
     real sa[3] = {real(0), real(0), real(0)}, sb[3] = {real(0), real(0), real(0)};
     const int n = np;
-    const int steps = tri ? np / 2 : np;
-    const int qb = tri ? p0 : q0;
-    int part = tri ? lane : lane - 1;   // partner slot (lane + step) mod n
-    int src = tri ? lane : lane + 1;    // sending lane (lane - step) mod n
+    const int steps = TRI ? np / 2 : np;      // triangle: steps 1..n/2, rectangle: 0..n-1
+    const int qb = TRI ? p0 : q0;
+    int part = TRI ? lane + 1 : lane;         // partner slot (lane + step) mod n
+    if (part >= n) part -= n;
+    int src = TRI ? lane - 1 : lane;          // sending lane (lane - step) mod n
+    if (src < 0) src += n;
 #pragma unroll 1
-    for (int st = tri ? 1 : 0; st <= (tri ? steps : steps - 1); ++st) {
-        if (++part >= n) part -= n;
-        if (--src < 0) src += n;
-        const bool valid = ownP && (tri ? (2 * st < n || lane < steps) : part < nq);
-        real vj[3] = {real(0), real(0), real(0)}, vk[3] = {real(0), real(0), real(0)};
-        if (valid) {
-            const R4 gb = w.geo[qb + part];
-            DampRec<real, NG> db;
-            db.load(w.dp + (qb + part) * NDP);
-            triplet_force<real, NG>(ga, da, gb, db, al, vj, vk);
-        }
+    for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
+        const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
+        const int e = qb + (valid ? part : 0);
+        const R4 gb = w.geo[e];
+        DampRec<real, NG> db;
+        db.load(w.dp + e * NDP);
+        real vj[3], vk[3];
+        triplet_force<real, NG>(ga, da, gb, db, al, vj, vk);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            sa[c] += vj[c];
-            const real r = __shfl_sync(0xffffffffu, vk[c], src & 31);
-            if (tri) sa[c] += r; else sb[c] += r;
+            sa[c] += valid ? vj[c] : real(0);
+            const real r = __shfl_sync(0xffffffffu, valid ? vk[c] : real(0), src & 31);
+            if (TRI) sa[c] += r; else sb[c] += r;
         }
+        part = (part + 1 == n) ? 0 : part + 1;
+        src = (src == 0) ? n - 1 : src - 1;
     }
     if (ownP) { w.ax[p0 + lane] += sa[0]; w.ay[p0 + lane] += sa[1]; w.az[p0 + lane] += sa[2]; }
     if (ownQ) { w.ax[q0 + lane] += sb[0]; w.ay[q0 + lane] += sb[1]; w.az[q0 + lane] += sb[2]; }
@@ -288,26 +298,27 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
 
 // The same chunk tasks for the symmetry functions of a fast-path block: the lane's own neighbour
 // stays in registers and only the partner's record is read per pair; acc[s] collects slot s.
-template <typename real, int NG, int S, int PASS>
-__device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real (&acc)[S], int lane, int p0, int np, int q0, int nq,
-                                          bool tri) {
+template <typename real, int NG, int S, int PASS, bool TRI>
+__device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real (&acc)[S], int lane, int p0, int np, int q0, int nq) {
     typedef typename V4<real>::T R4;
     constexpr int NDP = 2 * NG;
-    if (lane >= np) return;
-    const R4 ga = w.geo[p0 + lane];
+    const bool ownP = lane < np;
+    R4 ga;
     DampRec<real, NG> da;
-    da.load(w.dp + (p0 + lane) * NDP);
+    if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
+    else { ga.x = ga.y = ga.z = ga.w = real(0); da.zero(); }
     const int n = np;
-    const int steps = tri ? np / 2 : np;
-    const int qb = tri ? p0 : q0;
-    int part = tri ? lane : lane - 1;
+    const int steps = TRI ? np / 2 : np;
+    const int qb = TRI ? p0 : q0;
+    int part = TRI ? lane + 1 : lane;
+    if (part >= n) part -= n;
 #pragma unroll 1
-    for (int st = tri ? 1 : 0; st <= (tri ? steps : steps - 1); ++st) {
-        if (++part >= n) part -= n;
-        if (tri ? (2 * st == n && lane >= steps) : part >= nq) continue;
-        const R4 gb = w.geo[qb + part];
+    for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
+        const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
+        const int e = qb + (valid ? part : 0);
+        const R4 gb = w.geo[e];
         DampRec<real, NG> db;
-        db.load(w.dp + (qb + part) * NDP);
+        db.load(w.dp + e * NDP);
         const real cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
         const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
         real pp[4], pm[4];
@@ -315,10 +326,11 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
         pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
-            const real DD = da.D(g) * db.D(g);
+            const real DD = valid ? da.D(g) * db.D(g) : real(0);
 #pragma unroll
             for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
         }
+        part = (part + 1 == n) ? 0 : part + 1;
     }
 }
 
@@ -530,8 +542,13 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                         real al[NG][9];
                         if (PASS == PASS_FORCE) angular_poly<real, NG>(w.dE + A.off, a.prm.slot2ref, A.sidx, al);
                         auto task = [&](int p0, int np, int q0, int nq, bool tri) {
-                            if (PASS == PASS_FORCE) force_task<real, NG, PASS>(w, al, lane, p0, np, q0, nq, tri);
-                            else symm_task<real, NG, S, PASS>(w, acc, lane, p0, np, q0, nq, tri);
+                            if (PASS == PASS_FORCE) {
+                                if (tri) force_task<real, NG, PASS, true>(w, al, lane, p0, np, q0, nq);
+                                else force_task<real, NG, PASS, false>(w, al, lane, p0, np, q0, nq);
+                            } else {
+                                if (tri) symm_task<real, NG, S, PASS, true>(w, acc, lane, p0, np, q0, nq);
+                                else symm_task<real, NG, S, PASS, false>(w, acc, lane, p0, np, q0, nq);
+                            }
                         };
                         if (J == K) {
                             for (int c0 = 0; c0 < nJ; c0 += 32) {
