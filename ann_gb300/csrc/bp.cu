@@ -133,7 +133,8 @@ struct WarpMem {
     R4* tg;              // tangent of the pair vector (drx, dry, drz, dd) (JVP)
     real* dE;            // dE/dG row (FORCE)
     R4* stage;
-    int32_t *stagej, *stagej2, *jj, *img;
+    int32_t *stagej, *stagej2;   // staged neighbour indices (two buffers); after compaction the
+                                 // current one holds j per record (-1: no Newton-3rd share, FORCE)
     uint64_t* bar;       // two mbarriers, one per staging buffer
     static constexpr int NDP = 2 * NG;
     static __host__ __device__ size_t align(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -145,11 +146,10 @@ struct WarpMem {
         const size_t o_tg = (PASS == PASS_JVP) ? take(sizeof(R4) * cap, 32) : 0;
         const size_t o_dp = take(sizeof(real) * NDP * cap, 16);
         const size_t o_d = take(sizeof(real) * cap, 16), o_fc = take(sizeof(real) * cap, 16), o_fcg = take(sizeof(real) * cap, 16);
-        size_t o_ax = 0, o_ay = 0, o_az = 0, o_dE = 0, o_jj = 0, o_img = 0;
+        size_t o_ax = 0, o_ay = 0, o_az = 0, o_dE = 0;
         if (PASS == PASS_FORCE) {
             o_ax = take(sizeof(real) * cap, 16); o_ay = take(sizeof(real) * cap, 16); o_az = take(sizeof(real) * cap, 16);
             o_dE = take(sizeof(real) * imax, 16);
-            o_jj = take(sizeof(int32_t) * cap, 16); o_img = take(sizeof(int32_t) * cap, 16);
         }
         const size_t o_sj = take(sizeof(int32_t) * cap, 16);
         const size_t o_sj2 = take(sizeof(int32_t) * cap, 16);
@@ -160,7 +160,6 @@ struct WarpMem {
             w->d = reinterpret_cast<real*>(base + o_d); w->fc = reinterpret_cast<real*>(base + o_fc); w->fcg = reinterpret_cast<real*>(base + o_fcg);
             w->ax = reinterpret_cast<real*>(base + o_ax); w->ay = reinterpret_cast<real*>(base + o_ay); w->az = reinterpret_cast<real*>(base + o_az);
             w->dE = reinterpret_cast<real*>(base + o_dE);
-            w->jj = reinterpret_cast<int32_t*>(base + o_jj); w->img = reinterpret_cast<int32_t*>(base + o_img);
             w->stagej = reinterpret_cast<int32_t*>(base + o_sj);
             w->stagej2 = reinterpret_cast<int32_t*>(base + o_sj2);
             w->bar = reinterpret_cast<uint64_t*>(base + o_bar);
@@ -421,8 +420,10 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 const int e = base_in + e0 + lane;
                 bool keep = false;
                 R4 r4;
-                if (e0 + lane < cin && e < nin) { r4 = w.geo[e]; keep = r4.w < rc; }   // in place: o <= e
+                int j = 0;
+                if (e0 + lane < cin && e < nin) { r4 = w.geo[e]; j = w.stagej[e]; keep = r4.w < rc; }
                 const unsigned msk = __ballot_sync(0xffffffffu, keep);
+                __syncwarp();   // records are compacted in place (o <= e): all reads of the chunk first
                 if (keep) {
                     const int o = pos + __popc(msk & lt);
                     const real dd = r4.w, idd = real(1) / dd;
@@ -440,11 +441,9 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                             w.dp[o * NDP + 2 * q + 1] = ex * (g - real(2) * dd * f * ie2[q]);
                         }
                     }
-                    const int j = w.stagej[e];
                     if (PASS == PASS_FORCE) {
-                        w.jj[o] = j;
+                        w.stagej[o] = (a.newton_untranslated && a.nimg[row + e] != 0) ? -1 : j;
                         w.ax[o] = real(0); w.ay[o] = real(0); w.az[o] = real(0);
-                        w.img[o] = a.newton_untranslated ? a.nimg[row + e] : 0;
                     }
                     if (PASS == PASS_JVP) {
                         const real lx = a.lam[3 * (size_t)i] - a.lam[3 * (size_t)j];
@@ -723,8 +722,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
                 W9[0] += rx * vx; W9[1] += rx * vy; W9[2] += rx * vz;
                 W9[3] += ry * vx; W9[4] += ry * vy; W9[5] += ry * vz;
                 W9[6] += rz * vx; W9[7] += rz * vy; W9[8] += rz * vz;
-                if (!a.newton_untranslated || w.img[e] == 0) {
-                    const int j = w.jj[e];
+                const int j = w.stagej[e];
+                if (j >= 0) {
                     atomicAdd(&a.F[3 * (size_t)j], -vx); atomicAdd(&a.F[3 * (size_t)j + 1], -vy); atomicAdd(&a.F[3 * (size_t)j + 2], -vz);
                 }
             }
