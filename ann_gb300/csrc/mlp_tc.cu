@@ -4,17 +4,19 @@
 // Reference: NN::ANN::fpbp (src/ml/nn.cpp:1343-1409), NN::DODZ::grad (nn.cpp:1801-1824) and
 // NNH::energy (src/nnp/nnh.cpp:118-121), the same computation as the SIMT kernel in mlp.cu.
 //
-// Per CTA (128 threads, thread t <-> atom row t <-> TMEM lane t), persistent over the type's tiles:
+// Per CTA (512 threads: 4 warps per TMEM lane quadrant; tile row r <-> TMEM lane r), persistent
+// over the type's tiles:
 //   weights   : one bulk asynchronous copy (cp.async.bulk + mbarrier) of the type's image
 //               (B operands W_l and W_l^T in the canonical K-major no-swizzle layout, BF16 hi/lo).
 //   per tile  : A0 = inpw*(G+inpb) split into BF16 hi+lo rows, then for every hidden layer
 //               D = A W_l^T (tcgen05.mma kind::f16, M=128, issued by one thread, completion via
-//               tcgen05.commit on an mbarrier), epilogue = tcgen05.ld of the thread's row, bias,
-//               activation, next A; the last hidden layer's epilogue forms the energy and
-//               delta = outw w_last f'(z); the backward GEMMs D = delta W_l multiply by f'(z_{l-1})
-//               recomputed from the forward accumulators kept in TMEM, down to dE/dG = D inpw.
-//   split     : A = A_hi + A_lo (and W = W_hi + W_lo when the image fits) accumulate 2 or 3
-//               MMAs per k-step, giving close to FP32 products from BF16 operands.
+//               tcgen05.commit on an mbarrier); the epilogue (tcgen05.ld, bias, activation, next A)
+//               is split by 16-column chunks over the warps sharing a quadrant, and f'(z) is
+//               written back over z (tcgen05.st). The last hidden layer's epilogue forms the
+//               energy and delta = outw w_last f'(z); the backward GEMMs D = delta W_l multiply by
+//               the stored f'(z_{l-1}), down to dE/dG = D inpw.
+//   split     : A = A_hi + A_lo and W = W_hi + W_lo accumulate 3 MMAs per k-step, giving close
+//               to FP32 products from BF16 operands.
 // Every wait is bounded; on a timeout the CTA records ST_TIMEOUT, drains, frees TMEM and returns.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
