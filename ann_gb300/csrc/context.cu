@@ -88,8 +88,10 @@ static void upload_ints(DevBuf& b, const std::vector<int>& v, cudaStream_t st) {
 }
 
 struct GraphKey {
-    int S, N, cap, prec, forces, nbins;
-    bool operator==(const GraphKey& o) const { return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins; }
+    int S, N, cap, prec, forces, nbins, nchunks;
+    bool operator==(const GraphKey& o) const {
+        return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins && nchunks == o.nchunks;
+    }
 };
 
 struct ann_ctx {
@@ -107,8 +109,8 @@ struct ann_ctx {
     // batch
     int S = 0, N = 0;
     bool have_batch = false;
-    std::vector<int32_t> off_h, sid_h;
-    DevBuf off, cell, pos, type, sid;
+    std::vector<int32_t> off_h, sid_h, rchunk_h, rschunk_h;
+    DevBuf off, cell, pos, type, sid, rchunk, rschunk, rpartial;
     // neighbour list
     int cap = 0, nbins_cap = 0;
     DevBuf geo, pos4, abin, abc, am, aslot, bcount, bstart, bidx, bm, bpos4, bposd, nbins_total, nn, ntc, nj, nimg, nr, scan_tmp, counter, status;
@@ -117,8 +119,9 @@ struct ann_ctx {
     int last_prec = -1;
     bool have_results = false, have_forces = false;
     // graphs
-    cudaGraphExec_t gexec = nullptr;
-    GraphKey gkey{-1, -1, -1, -1, -1, -1};
+    // graphs of the E+F sequence: [0] with the list build, [1] with the Verlet-list refresh (MD)
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    GraphKey gkey[2] = {{-1, -1, -1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1, -1, -1}};
     // training
     DevBuf Eref, Fref, loss3, ce, lam, U, grad;
     bool have_train = false;
@@ -135,7 +138,7 @@ struct ann_ctx {
     int md_rebuilds = 0;
     // instrumentation
     int64_t kernels = 0;            // kernels launched (graph replays add graph_kernels)
-    int64_t graph_kernels = 0;
+    int64_t graph_kernels[2] = {0, 0};
     bool profile = false;
     bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
     int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
@@ -168,8 +171,10 @@ static void upload_params(ann_ctx* c, ParamSet<real>& P) {
     upload_vec<real>(P.inpw, h.inpw, c->stream); upload_vec<real>(P.inpb, h.inpb, c->stream);
 }
 static void reset_graph(ann_ctx* c) {
-    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
-    c->gkey = GraphKey{-1, -1, -1, -1, -1, -1};
+    for (int k = 0; k < 2; ++k) {
+        if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
+        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1};
+    }
 }
 static void rebuild_plan(ann_ctx* c) {
     build_plan(c->pot, c->plan);
@@ -241,6 +246,16 @@ static void stage_offsets(ann_ctx* c, int nstruc, const int64_t* atom_offsets) {
     c->sid_h.assign(c->N, 0);
     for (int s = 0; s <= nstruc; ++s) c->off_h[s] = (int32_t)atom_offsets[s];
     for (int s = 0; s < nstruc; ++s) for (int i = c->off_h[s]; i < c->off_h[s + 1]; ++i) c->sid_h[i] = s;
+    // chunks of the per-structure reductions
+    c->rchunk_h.clear();
+    c->rschunk_h.assign(nstruc + 1, 0);
+    for (int s = 0; s < nstruc; ++s) {
+        c->rschunk_h[s] = (int32_t)(c->rchunk_h.size() / 3);
+        for (int a = c->off_h[s]; a < c->off_h[s + 1]; a += RED_CHUNK) {
+            c->rchunk_h.push_back(s); c->rchunk_h.push_back(a); c->rchunk_h.push_back(std::min(a + RED_CHUNK, c->off_h[s + 1]));
+        }
+    }
+    c->rschunk_h[nstruc] = (int32_t)(c->rchunk_h.size() / 3);
 }
 
 static void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell, bool device_src) {
@@ -262,6 +277,18 @@ static void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const doub
     ensure_batch_buffers(c);
     const cudaMemcpyKind k = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     ck(cudaMemcpyAsync(c->off.p, c->off_h.data(), 4 * (c->S + 1), cudaMemcpyHostToDevice, c->stream), "H2D offsets");
+    {
+        // sized by the bound S + N / RED_CHUNK + 1, so that a captured graph's pointers stay valid
+        // for every batch with the same S and N
+        const size_t nch = c->rchunk_h.size() / 3;
+        const size_t nmax = (size_t)c->S + (size_t)c->N / RED_CHUNK + 1;
+        c->rchunk.ensure(4 * 3 * nmax);
+        c->rschunk.ensure(4 * ((size_t)c->S + 1));
+        c->rpartial.ensure(sizeof(double) * 10 * nmax);
+        if (nch) ck(cudaMemcpyAsync(c->rchunk.p, c->rchunk_h.data(), 4 * c->rchunk_h.size(), cudaMemcpyHostToDevice, c->stream), "H2D chunks");
+        ck(cudaMemcpyAsync(c->rschunk.p, c->rschunk_h.data(), 4 * c->rschunk_h.size(), cudaMemcpyHostToDevice, c->stream), "H2D chunks");
+        ck(cudaStreamSynchronize(c->stream), "H2D chunks");   // the host tables are rebuilt by the next batch
+    }
     if (c->N > 0) {
         ck(cudaMemcpyAsync(c->sid.p, c->sid_h.data(), 4 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D sid");
         ck(cudaMemcpyAsync(c->pos.p, posn, sizeof(double) * 3 * (size_t)c->N, k, c->stream), "copy positions");
@@ -311,6 +338,13 @@ static void mark(ann_ctx* c, int k) {
     cudaEventRecord(c->ev[k], c->stream);
 }
 
+static RedTable red_table(ann_ctx* c) {
+    RedTable t;
+    t.nchunks = (int32_t)(c->rchunk_h.size() / 3);
+    t.chunk = c->rchunk.as<int32_t>(); t.schunk = c->rschunk.as<int32_t>(); t.partial = c->rpartial.as<double>();
+    return t;
+}
+
 // the MIXED network pass runs on the tensor cores unless the SIMT kernels are asked for
 static bool use_tc(const ann_ctx* c) { return c->opt.mlp_backend != 1 && c->tc.ok; }
 
@@ -358,7 +392,7 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     }
     check_phase(c, "forces");
     mark(c, 5);
-    launch_reduce_structures<real>(c->S, c->off.as<int32_t>(), c->Eatom.as<double>(), forces ? c->W.as<real>() : nullptr,
+    launch_reduce_structures<real>(c->S, red_table(c), c->Eatom.as<double>(), forces ? c->W.as<real>() : nullptr,
                                    c->F.as<real>(), c->Es.as<double>(), c->Ws.as<double>(), forces ? c->Fout.as<double>() : nullptr, st);
     check_phase(c, "reductions");
     mark(c, 6);
@@ -376,15 +410,16 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
                                               " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
     if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
-    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap};
-    const bool graphs = c->opt.use_graphs && build_list && c->N > 0 && !c->profile;
+    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3)};
+    const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
+    const int gs = build_list ? 0 : 1;
     if (graphs) {
-        if (!(c->gexec && c->gkey == key)) {
-            reset_graph(c);
+        if (!(c->gexec[gs] && c->gkey[gs] == key)) {
+            if (c->gexec[gs]) { cudaGraphExecDestroy(c->gexec[gs]); c->gexec[gs] = nullptr; }
             cudaGraph_t g = nullptr;
             const int64_t before = g_launch_counter;
             ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-            if (prec == ANN_FP64) enqueue_ef<double>(c, forces, true); else enqueue_ef<float>(c, forces, true);
+            if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
             const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
             if (ce != cudaSuccess) {
                 // locate the failing launch: replay the sequence eagerly with per-phase checks
@@ -393,18 +428,18 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
                 const bool d0 = c->debug;
                 c->debug = true;
                 try {
-                    if (prec == ANN_FP64) enqueue_ef<double>(c, forces, true); else enqueue_ef<float>(c, forces, true);
+                    if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
                 } catch (...) { c->debug = d0; throw; }
                 c->debug = d0;
                 throw ann_error(ANN_ERR_CUDA, std::string("graph capture failed (") + cudaGetErrorString(ce) + ") but the eager replay succeeded");
             }
-            c->graph_kernels = g_launch_counter - before;
-            ck(cudaGraphInstantiate(&c->gexec, g, 0), "graph instantiate");
+            c->graph_kernels[gs] = g_launch_counter - before;
+            ck(cudaGraphInstantiate(&c->gexec[gs], g, 0), "graph instantiate");
             cudaGraphDestroy(g);
-            c->gkey = key;
+            c->gkey[gs] = key;
         }
-        ck(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
-        c->kernels += c->graph_kernels;
+        ck(cudaGraphLaunch(c->gexec[gs], c->stream), "graph launch");
+        c->kernels += c->graph_kernels[gs];
     } else {
         const int64_t before = g_launch_counter;
         if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
@@ -488,7 +523,8 @@ int ann_destroy(ann_ctx* c) {
                       &c->bcount, &c->bstart, &c->bidx, &c->bm, &c->bpos4, &c->bposd, &c->nbins_total, &c->nn, &c->ntc, &c->nj, &c->nimg,
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
-                      &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d})
+                      &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
+                      &c->rchunk, &c->rschunk, &c->rpartial, &c->tcimg})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);

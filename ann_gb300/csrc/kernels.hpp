@@ -102,8 +102,16 @@ template <typename real> void launch_mlp_train_grad(const DevPot& pot, const Mlp
 // ---- small kernels (misc.cu) ---------------------------------------------------------------
 void launch_type_lists(int natoms, int ntypes, const int32_t* type, int32_t* tcount, int32_t* tstart, int32_t* tlist,
                        int32_t* status, cudaStream_t st);
+// chunk table of the per-structure reductions (built on the host with the batch)
+constexpr int RED_CHUNK = 256;
+struct RedTable {
+    int32_t nchunks;
+    const int32_t* chunk;            // [nchunks][3]: structure, first atom, end atom
+    const int32_t* schunk;           // [S+1] first chunk of each structure
+    double* partial;                 // [nchunks][10]
+};
 template <typename real>
-void launch_reduce_structures(int nstruc, const int32_t* off, const double* Eatom, const real* W, const real* F,
+void launch_reduce_structures(int nstruc, const RedTable& t, const double* Eatom, const real* W, const real* F,
                               double* Es, double* Ws, double* Fout, cudaStream_t st);
 void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st);
 size_t scan_tmp_ints(int n);

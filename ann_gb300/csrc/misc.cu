@@ -1,8 +1,8 @@
 // Small device kernels: exclusive scan, per-type atom lists, and the per-structure segmented
 // reductions (K5) that turn per-atom energies / virials / force accumulators into the FP64
 // per-structure results (the reference sums NNP energies per structure, nnp.cpp:436-447, and
-// MPI_Reduce-s them across ranks; here one block per structure sums in a fixed order, so the
-// result is deterministic).
+// MPI_Reduce-s them across ranks; here fixed-size chunks of each structure are summed in a
+// fixed order and the chunk partials added in chunk order, so the result is deterministic).
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "kernels.hpp"
@@ -114,12 +114,17 @@ void launch_type_lists(int natoms, int ntypes, const int32_t* type, int32_t* tco
 }
 
 // ---------------------------------------------------------------- per-structure reductions
+// Structures are cut into chunks of at most RED_CHUNK atoms (table built on the host with the
+// batch): one block per chunk sums E and W in a fixed order into a partial row, then one block
+// per structure adds its chunks' partials in a fixed order. The result does not depend on the
+// launch geometry, and a 262k-atom structure is spread over 1,024 blocks instead of one.
+constexpr int RED_THREADS = 128;
 template <typename real>
-__global__ void k_reduce_structures(const int32_t* off, const double* Eatom, const real* W, const real* F,
-                                    double* Es, double* Ws, double* Fout) {
-    const int s = blockIdx.x;
-    const int a0 = off[s], a1 = off[s + 1];
-    __shared__ double red[10][256];
+__global__ void k_reduce_chunks(const int32_t* chunk, const double* Eatom, const real* W, const real* F, double* partial,
+                                double* Fout) {
+    const int c = blockIdx.x;
+    const int a0 = chunk[3 * c + 1], a1 = chunk[3 * c + 2];
+    __shared__ double red[10][RED_THREADS];
     double acc[10];
 #pragma unroll
     for (int k = 0; k < 10; ++k) acc[k] = 0.0;
@@ -145,18 +150,42 @@ __global__ void k_reduce_structures(const int32_t* off, const double* Eatom, con
         }
         __syncthreads();
     }
+    if (threadIdx.x < 10) partial[10 * (size_t)c + threadIdx.x] = red[threadIdx.x][0];
+}
+// one block per structure: thread t adds chunks t, t + RED_THREADS, ... in order, then a fixed tree
+__global__ void k_reduce_partials(int nstruc, const int32_t* schunk, const double* partial, bool with_w, double* Es, double* Ws) {
+    const int s = blockIdx.x;
+    __shared__ double red[10][RED_THREADS];
+    double acc[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = 0.0;
+    for (int c = schunk[s] + threadIdx.x; c < schunk[s + 1]; c += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) acc[k] += partial[10 * (size_t)c + k];
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < 10; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
     if (threadIdx.x == 0) {
         Es[s] = red[0][0];
-        if (W && Ws) for (int k = 0; k < 9; ++k) Ws[9 * (size_t)s + k] = red[1 + k][0];
+        if (with_w && Ws) for (int k = 0; k < 9; ++k) Ws[9 * (size_t)s + k] = red[1 + k][0];
     }
 }
 template <typename real>
-void launch_reduce_structures(int nstruc, const int32_t* off, const double* Eatom, const real* W, const real* F,
+void launch_reduce_structures(int nstruc, const RedTable& t, const double* Eatom, const real* W, const real* F,
                               double* Es, double* Ws, double* Fout, cudaStream_t st) {
     if (nstruc <= 0) return;
-    ++::ann::g_launch_counter, k_reduce_structures<real><<<nstruc, 256, 0, st>>>(off, Eatom, W, F, Es, Ws, Fout);
+    if (t.nchunks > 0) ++::ann::g_launch_counter, k_reduce_chunks<real><<<t.nchunks, RED_THREADS, 0, st>>>(t.chunk, Eatom, W, F, t.partial, Fout);
+    ++::ann::g_launch_counter, k_reduce_partials<<<nstruc, RED_THREADS, 0, st>>>(nstruc, t.schunk, t.partial, W != nullptr, Es, Ws);
 }
-template void launch_reduce_structures<float>(int, const int32_t*, const double*, const float*, const float*, double*, double*, double*, cudaStream_t);
-template void launch_reduce_structures<double>(int, const int32_t*, const double*, const double*, const double*, double*, double*, double*, cudaStream_t);
+template void launch_reduce_structures<float>(int, const RedTable&, const double*, const float*, const float*, double*, double*, double*, cudaStream_t);
+template void launch_reduce_structures<double>(int, const RedTable&, const double*, const double*, const double*, double*, double*, double*, cudaStream_t);
 
 }  // namespace ann

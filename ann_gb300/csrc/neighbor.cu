@@ -353,17 +353,32 @@ __global__ void k_refresh(NbrArgs a) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.natoms) return;
     const StrucGeo& g = a.geo[a.sid[i]];
+    double R[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = g.R[k];
     const int cnt = a.nn[i];
     const size_t row = (size_t)i * a.cap;
     const double xid[3] = {a.pos[3 * i], a.pos[3 * i + 1], a.pos[3 * i + 2]};
+    float Rf[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Rf[k] = (float)R[k];
+    const float4 xi4 = FP64 ? float4{} : a.pos4[i];
     for (int e = lane; e < cnt; e += 32) {
         const int j = a.nj[row + e];
         int n0, n1, n2;
         unpack3(a.nimg[row + e], n0, n1, n2);
-        double r[3], d2;
-        pair_vec_d(xid, a.pos + 3 * (size_t)j, g.R, n0, n1, n2, r, d2);
-        if (FP64) reinterpret_cast<Vec4d*>(a.nr)[row + e] = Vec4d{r[0], r[1], r[2], sqrt(d2)};
-        else reinterpret_cast<Vec4f*>(a.nr)[row + e] = Vec4f{(float)r[0], (float)r[1], (float)r[2], (float)sqrt(d2)};
+        if (FP64) {   // the canonical FP64 pair vector of the list builder
+            double r[3], d2;
+            pair_vec_d(xid, a.pos + 3 * (size_t)j, R, n0, n1, n2, r, d2);
+            reinterpret_cast<Vec4d*>(a.nr)[row + e] = Vec4d{r[0], r[1], r[2], sqrt(d2)};
+        } else {      // FP32 from the FP32 position copy, as the list builder's mixed form
+            const float4 pj = a.pos4[j];
+            const float fn0 = (float)n0, fn1 = (float)n1, fn2 = (float)n2;
+            const float rx = (xi4.x - pj.x) - (fn0 * Rf[0] + fn1 * Rf[3] + fn2 * Rf[6]);
+            const float ry = (xi4.y - pj.y) - (fn0 * Rf[1] + fn1 * Rf[4] + fn2 * Rf[7]);
+            const float rz = (xi4.z - pj.z) - (fn0 * Rf[2] + fn1 * Rf[5] + fn2 * Rf[8]);
+            reinterpret_cast<Vec4f*>(a.nr)[row + e] = Vec4f{rx, ry, rz, sqrtf(rx * rx + ry * ry + rz * rz)};
+        }
     }
 }
 
@@ -390,10 +405,20 @@ void configure_nbr(int maxsmem) {
     set_max_dynamic_smem(k_neighbors<false>, maxsmem);
 }
 
+// FP32 copy of the current positions (the type bits in w are kept)
+__global__ void k_pos4(int n, const double* pos, float4* pos4) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos4[i];
+    p.x = (float)pos[3 * (size_t)i]; p.y = (float)pos[3 * (size_t)i + 1]; p.z = (float)pos[3 * (size_t)i + 2];
+    pos4[i] = p;
+}
+
 void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st) {
     const int threads = 256;
     const int grid = (int)(((long long)a.natoms * 32 + threads - 1) / threads);
     if (grid < 1) return;
+    if (!fp64) ++::ann::g_launch_counter, k_pos4<<<(a.natoms + 255) / 256, 256, 0, st>>>(a.natoms, a.pos, a.pos4);
     if (fp64) ++::ann::g_launch_counter, k_refresh<true><<<grid, threads, 0, st>>>(a);
     else ++::ann::g_launch_counter, k_refresh<false><<<grid, threads, 0, st>>>(a);
 }

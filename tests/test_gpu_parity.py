@@ -121,6 +121,20 @@ def test_generic_basis_variants(ctx, oracle, tmp_path):
     _check_mixed(ctx, offs, posn, types, cell, E, F)
 
 
+def test_large_structure_reductions(ctx, oracle, tmp_path):
+    """A structure of 2,600 atoms (eleven reduction chunks of at most 256 atoms) between two
+    small ones: energies and virials as the oracle's, also in the mixed form."""
+    big = cases.W.random_binary(1, 2600, 2600, seed=77)
+    structs = cases.small_binary(n_struc=1, seed=3) + big + cases.tiny_cells()[:1]
+    offs, posn, types, cell = cases.batch(structs)
+    text = cases.config_potential(ctx, 2, tmp_path)
+    pot = oracle.load_text(text)
+    E, F, Wv = ctx.compute(offs, posn, types, cell, precision=FP64)
+    Eo, Fo, Wo, _, _ = pot.compute(offs, posn, types, cell)
+    assert _rel_err(E, Eo) < REL and _rel_err(F, Fo) < REL and _rel_err(Wv, Wo) < REL
+    _check_mixed(ctx, offs, posn, types, cell, E, F)
+
+
 def test_empty_and_single_structures(ctx, oracle, tmp_path):
     text = cases.config_potential(ctx, 2, tmp_path)
     pot = oracle.load_text(text)
