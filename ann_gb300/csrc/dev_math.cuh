@@ -74,6 +74,9 @@ template <> struct M<double> {
     static __device__ __forceinline__ double tanh(double x) { return ::tanh(x); }
     static __device__ __forceinline__ double log1p(double x) { return ::log1p(x); }
     static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double log(double x) { return ::log(x); }
+    static __device__ __forceinline__ double atan(double x) { return ::atan(x); }
+    static __device__ __forceinline__ double erf(double x) { return ::erf(x); }
     static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
     static __device__ __forceinline__ double coscut(double x) { return d_coscut(x); }   // ~cos(x), x in [0,pi]
     static __device__ __forceinline__ double sincut(double x) { return d_sincut(x); }
@@ -86,6 +89,9 @@ template <> struct M<float> {
     static __device__ __forceinline__ float tanh(float x) { return ::tanhf(x); }
     static __device__ __forceinline__ float log1p(float x) { return ::log1pf(x); }
     static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
+    static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+    static __device__ __forceinline__ float atan(float x) { return ::atanf(x); }
+    static __device__ __forceinline__ float erf(float x) { return ::erff(x); }
     static __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
     static __device__ __forceinline__ float coscut(float x) { return __cosf(x); }
     static __device__ __forceinline__ float sincut(float x) { return __sinf(x); }
@@ -231,24 +237,123 @@ __device__ __forceinline__ void angular_damp(int name, real ie2, real r2s, real&
     }
 }
 
-// activation value, first and second derivative (nn.cpp:149-236 linear/sigmoid/tanh,
-// nn.cpp:676-720 softplus shifted by -ln2/c)
+// activation value, first and second derivative: a and d follow AFFPBP::af_* (nn.cpp:149-810),
+// d2 is the exact derivative of d (where AFFPBP2 sets 0 or an inexact form, nn.cpp:282-812); the
+// same formulas as the oracle's activate()
 template <typename real>
 __device__ __forceinline__ void act_fd(int neuron, real c, real z, real& a, real& d, real& d2) {
+    const real PI = real(3.141592653589793), RADPI = real(1.772453850905516), one = real(1), two = real(2), half = real(0.5);
     switch (neuron) {
         case N_SIGMOID: {
-            if (z >= real(0)) { const real e = M<real>::exp(-c * z); const real f = real(1) / (real(1) + e); a = f; d = c * e * f * f; d2 = -c * c * e * (real(1) - e) * f * f * f; }
-            else { const real e = M<real>::exp(c * z); const real f = real(1) / (real(1) + e); a = e * f; d = c * e * f * f; d2 = -c * c * e * (e - real(1)) * f * f * f; }
+            if (z >= real(0)) { const real e = M<real>::exp(-c * z); const real f = one / (one + e); a = f; d = c * e * f * f; d2 = -c * c * e * (one - e) * f * f * f; }
+            else { const real e = M<real>::exp(c * z); const real f = one / (one + e); a = e * f; d = c * e * f * f; d2 = -c * c * e * (e - one) * f * f * f; }
             return;
         }
-        case N_TANH: { const real t = M<real>::tanh(c * z); a = t; d = c * (real(1) - t * t); d2 = c * c * (real(-2) * t * (real(1) - t * t)); return; }
+        case N_TANH: { const real t = M<real>::tanh(c * z); a = t; d = c * (one - t * t); d2 = c * c * (-two * t * (one - t * t)); return; }
+        case N_ISRU: {
+            const real zz = c * z, isr = one / M<real>::sqrt(one + zz * zz), isr3 = isr * isr * isr;
+            if (zz < real(-100)) a = -one / (one + one / (zz * zz));
+            else if (zz > real(100)) a = one / (one + one / (zz * zz));
+            else a = zz * isr;
+            d = c * isr3; d2 = real(-3) * c * c * zz * isr3 * isr * isr;
+            return;
+        }
+        case N_ARCTAN: {
+            const real zz = c * z * PI / two, fr = one / (one + zz * zz);
+            a = (two / PI) * M<real>::atan(zz); d = c * fr; d2 = -PI * c * c * zz * fr * fr;
+            return;
+        }
+        case N_RELU: if (z > real(0)) { a = z; d = one; } else { a = real(0); d = real(0); } d2 = real(0); return;
+        case N_ELU: {
+            if (z >= real(0)) { a = z; d = one; d2 = real(0); }
+            else { const real e = M<real>::exp(c * z); a = e - one; d = c * e; d2 = c * c * e; }
+            return;
+        }
+        case N_TANHRE: {
+            if (z >= real(0)) { a = z; d = one; d2 = real(0); }
+            else { const real fe = M<real>::exp(two * c * z); a = (fe - one) / (fe + one); d = c * (one - a * a); d2 = -two * c * a * d; }
+            return;
+        }
+        case N_SQRE: {
+            if (z >= real(0)) { a = z; d = one; d2 = real(0); }
+            else { const real den = one / M<real>::sqrt(one + z * z), den3 = den * den * den; a = z * den; d = den3; d2 = real(-3) * z * den3 * den * den; }
+            return;
+        }
+        case N_SWISH: {
+            const real zz = c * z;
+            if (zz > real(0)) {
+                const real e = M<real>::exp(-zz), den = one / (one + e);
+                a = z * den; d = (one + e * (one + zz)) * den * den; d2 = c * e * (two - zz + e * (two + zz)) * den * den * den;
+            } else {
+                const real e = M<real>::exp(zz), den = one / (one + e);
+                a = z * e * den; d = e * (one + zz + e) * den * den; d2 = c * e * (two + zz + e * (two - zz)) * den * den * den;
+            }
+            return;
+        }
+        case N_GELU: {
+            const real zz = half * RADPI * c * z, erfp1 = one + M<real>::erf(zz), g = M<real>::exp(-zz * zz);
+            a = half * z * erfp1; d = half * (erfp1 + c * z * g); d2 = c * g * (one - zz * zz);
+            return;
+        }
+        case N_MISH: {
+            const real zz = c * z;
+            if (zz > real(0)) {
+                const real e = M<real>::exp(-zz), e2 = e * e, den = one / ((one + e) * (one + e) + e2);
+                a = z * (one - two * e2 * den);
+                d = one - two * e2 * den * (one - two * zz * (one + e) * den);
+                const real t1 = real(4) * e2 * (one + e) * den * den;
+                const real t2 = real(4) * e2 * den * den * den * (-two - real(3) * e + two * e2 + two * e2 * e);
+                d2 = c * (two * t1 + zz * t2);
+            } else {
+                const real e = M<real>::exp(zz), den = one / (e * (e + two) + two);
+                a = z * e * (e + two) * den;
+                d = one + two * den * (-one + two * zz * (one - (e + two) * den));
+                const real t1 = real(4) * e * (e + one) * den * den;
+                const real t2 = real(4) * den * den * den * e * (two + two * e - real(3) * e * e - two * e * e * e);
+                d2 = c * (two * t1 + zz * t2);
+            }
+            return;
+        }
+        case N_PFLU: {
+            const real zz = c * z, z2 = zz * zz, fs = one / M<real>::sqrt(z2 + one), fs3 = fs * fs * fs;
+            a = half * z * (one + zz * fs); d = half * (zz * (z2 + two) * fs3 + one); d2 = -half * c * (z2 - two) * fs3 * fs * fs;
+            return;
+        }
+        case N_SERF: {
+            const real fe = M<real>::exp(z), fl = M<real>::log1p(fe), ef = M<real>::erf(fl), g = M<real>::exp(-fl * fl), sg = one / (one + one / fe);
+            a = z * ef; d = ef + two / RADPI * g * z * sg; d2 = two / RADPI * g * sg * (two - two * z * fl * sg + z * (one - sg));
+            return;
+        }
+        case N_LOGISH: {
+            const real l2i = one / real(kLOG2), e = M<real>::exp(-z), lf = M<real>::log(one + one / (one + e));
+            const real q = e / ((one + e) * (two + e)), qp = e * (e * e - two) / ((one + e) * (one + e) * (two + e) * (two + e));
+            a = l2i * z * lf; d = l2i * (lf + z * q); d2 = l2i * (two * q + z * qp);
+            return;
+        }
         case N_SOFTPLUS: {
-            const real ci = real(1) / c;
-            if (z > real(0)) { const real e = M<real>::exp(-c * z); const real den = real(1) / (e + real(1)); a = z + ci * (M<real>::log1p(e) - real(kLOG2)); d = den; d2 = c * e * den * den; }
-            else { const real e = M<real>::exp(c * z); const real den = real(1) / (e + real(1)); a = ci * (M<real>::log1p(e) - real(kLOG2)); d = e * den; d2 = c * e * den * den; }
+            const real ci = one / c;
+            if (z > real(0)) { const real e = M<real>::exp(-c * z); const real den = one / (e + one); a = z + ci * (M<real>::log1p(e) - real(kLOG2)); d = den; d2 = c * e * den * den; }
+            else { const real e = M<real>::exp(c * z); const real den = one / (e + one); a = ci * (M<real>::log1p(e) - real(kLOG2)); d = e * den; d2 = c * e * den * den; }
             return;
         }
-        default: a = z; d = real(1); d2 = real(0); return;  // LINEAR
+        case N_SQPLUS: {
+            const real zz = c * z, fs = M<real>::sqrt(one + zz * zz);
+            a = half / c * (zz - one + fs); d = half * (zz / fs + one); d2 = half * c / (fs * fs * fs);
+            return;
+        }
+        case N_ATISH: {
+            const real zz = half * PI * z, fr = one / (one + zz * zz), at = M<real>::atan(zz);
+            a = z * half * (one + two / PI * at); d = half * (one + z * fr) + at / PI; d2 = fr * fr;
+            return;
+        }
+        case N_TEST: {
+            const real zz = c * z, z2 = zz * zz, z4 = z2 * z2, den = one / M<real>::sqrt(M<real>::sqrt(z4 + one));
+            const real den4 = den * den * den * den;
+            a = half * z * (one + zz * den); d = half * (zz * den * (one + one / (z4 + one)) + one);
+            d2 = half * c * (den + (one - z4) * den * den4 - real(5) * z4 * den * den4 * den4);
+            return;
+        }
+        default: a = z; d = one; d2 = real(0); return;  // LINEAR
     }
 }
 

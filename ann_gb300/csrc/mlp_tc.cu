@@ -95,8 +95,9 @@ static __device__ __forceinline__ void put8(uint8_t* hi, uint8_t* lo, int r, int
     if (lo) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// activation value and first derivative with the hardware approximations (exp2 / log2 / rcp);
-// absolute errors ~1e-7, far inside the FP32 path's tolerance (nn.cpp:149-236 forms)
+// activation value and first derivative: sigmoid, tanh and softplus with the hardware
+// approximations (exp2 / log2 / rcp; absolute errors ~1e-7, far inside the FP32 path's tolerance),
+// the other forms of nn.cpp:149-810 through act_fd
 static __device__ __forceinline__ void act_fast(int neuron, float c, float z, float& a, float& d) {
     switch (neuron) {
         case N_SIGMOID: {
@@ -118,7 +119,7 @@ static __device__ __forceinline__ void act_fast(int neuron, float c, float z, fl
             d = (z > 0.0f) ? r : e * r;
             return;
         }
-        default: a = z; d = 1.0f; return;
+        default: { float d2; act_fd<float>(neuron, c, z, a, d, d2); return; }   // the other forms, full-accuracy functions
     }
 }
 

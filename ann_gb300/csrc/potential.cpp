@@ -264,8 +264,8 @@ void Potential::validate() const {
     for (auto& x : sp) {
         if (x.nn.nodes.back() != 1) throw ann_error(ANN_ERR_UNSUPPORTED, "networks must have one output (type " + x.name + ")");
         const int act = x.nn.neuron;
-        if (act != N_LINEAR && act != N_SIGMOID && act != N_TANH && act != N_SOFTPLUS)
-            throw ann_error(ANN_ERR_UNSUPPORTED, std::string("activation ") + neuron_names[act] + " is not implemented on the GPU path");
+        if (act <= N_UNKNOWN || act > N_TEST)
+            throw ann_error(ANN_ERR_UNSUPPORTED, "activation " + std::to_string(act) + " is not implemented on the GPU path");
         for (int l = 0; l < x.nn.nlayer(); ++l)
             if (x.nn.nodes[l] > 256) throw ann_error(ANN_ERR_UNSUPPORTED, "layers wider than 256 nodes are not supported");
         if (x.nInput > 256) throw ann_error(ANN_ERR_UNSUPPORTED, "more than 256 inputs per atom are not supported");

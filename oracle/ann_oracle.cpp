@@ -353,8 +353,12 @@ static int neuron_read(const std::string& s) {  // nn.cpp:120-140
     for (int i = 1; i < 20; ++i) if (s == names[i]) return i;
     return N_UNKNOWN;
 }
-// activation value, first and second derivative (nn.cpp:149-236 lin/sigmoid/tanh, 676-720 softplus)
+// activation value, first and second derivative: a and d follow AFFPBP::af_* (nn.cpp:149-810);
+// d2 is the exact derivative of d (AFFPBP2 sets d2 = 0 for GELU, MISH, SERF, LOGISH, ATISH and
+// TEST and has inexact d2 for ARCTAN, TANHRE and SQRE, nn.cpp:282-444); SERF's d uses erf(fl) for
+// its a/z term so that it is finite at z = 0.
 static void activate(int neuron, double c, double z, double& a, double& d, double& d2) {
+    constexpr double PI = 3.141592653589793, RADPI = 1.772453850905516;   // math/const.hpp:9-10
     switch (neuron) {
         case N_LINEAR: a = z; d = 1.0; d2 = 0.0; return;
         case N_SIGMOID: {
@@ -363,11 +367,109 @@ static void activate(int neuron, double c, double z, double& a, double& d, doubl
             return;
         }
         case N_TANH: { const double t = std::tanh(c * z); a = t; d = c * (1.0 - t * t); d2 = c * c * (-2.0 * t * (1.0 - t * t)); return; }
+        case N_ISRU: {  // nn.cpp:254-266
+            const double zz = c * z, isr = 1.0 / std::sqrt(1.0 + zz * zz), isr3 = isr * isr * isr;
+            if (zz < -100.0) a = -1.0 / (1.0 + 1.0 / (zz * zz));
+            else if (zz > 100.0) a = 1.0 / (1.0 + 1.0 / (zz * zz));
+            else a = zz * isr;
+            d = c * isr3;
+            d2 = -3.0 * c * c * zz * isr3 * isr * isr;
+            return;
+        }
+        case N_ARCTAN: {  // nn.cpp:282-290
+            const double zz = c * z * PI / 2.0, fr = 1.0 / (1.0 + zz * zz);
+            a = (2.0 / PI) * std::atan(zz); d = c * fr; d2 = -PI * c * c * zz * fr * fr;
+            return;
+        }
+        case N_RELU: if (z > 0.0) { a = z; d = 1.0; } else { a = 0.0; d = 0.0; } d2 = 0.0; return;   // nn.cpp:315-328
+        case N_ELU: {  // nn.cpp:353-366
+            if (z >= 0.0) { a = z; d = 1.0; d2 = 0.0; }
+            else { const double e = std::exp(c * z); a = e - 1.0; d = c * e; d2 = c * c * e; }
+            return;
+        }
+        case N_TANHRE: {  // nn.cpp:393-405
+            if (z >= 0) { a = z; d = 1.0; d2 = 0.0; }
+            else { const double fe = std::exp(2.0 * c * z); a = (fe - 1.0) / (fe + 1.0); d = c * (1.0 - a * a); d2 = -2.0 * c * a * d; }
+            return;
+        }
+        case N_SQRE: {  // nn.cpp:432-444
+            if (z >= 0) { a = z; d = 1.0; d2 = 0.0; }
+            else { const double den = 1.0 / std::sqrt(1.0 + z * z), den3 = den * den * den; a = z * den; d = den3; d2 = -3.0 * z * den3 * den * den; }
+            return;
+        }
+        case N_SWISH: {  // nn.cpp:480-498
+            const double zz = c * z;
+            if (zz > 0.0) {
+                const double e = std::exp(-zz), den = 1.0 / (1.0 + e);
+                a = z * den; d = (1.0 + e * (1.0 + zz)) * den * den; d2 = c * e * (2.0 - zz + e * (2.0 + zz)) * den * den * den;
+            } else {
+                const double e = std::exp(zz), den = 1.0 / (1.0 + e);
+                a = z * e * den; d = e * (1.0 + zz + e) * den * den; d2 = c * e * (2.0 + zz + e * (2.0 - zz)) * den * den * den;
+            }
+            return;
+        }
+        case N_GELU: {  // nn.cpp:505-524
+            const double zz = 0.5 * RADPI * c * z, erfp1 = 1.0 + std::erf(zz), g = std::exp(-zz * zz);
+            a = 0.5 * z * erfp1; d = 0.5 * (erfp1 + c * z * g); d2 = c * g * (1.0 - zz * zz);
+            return;
+        }
+        case N_MISH: {  // nn.cpp:548-586 (AFFPBP form)
+            const double zz = c * z;
+            if (zz > 0.0) {
+                const double e = std::exp(-zz), e2 = e * e, den = 1.0 / ((1.0 + e) * (1.0 + e) + e2);
+                a = z * (1.0 - 2.0 * e2 * den);
+                d = 1.0 - 2.0 * e2 * den * (1.0 - 2.0 * zz * (1.0 + e) * den);
+                const double t1 = 4.0 * e2 * (1.0 + e) * den * den;
+                const double t2 = 4.0 * e2 * den * den * den * (-2.0 - 3.0 * e + 2.0 * e2 + 2.0 * e2 * e);
+                d2 = c * (2.0 * t1 + zz * t2);
+            } else {
+                const double e = std::exp(zz), den = 1.0 / (e * (e + 2.0) + 2.0);
+                a = z * e * (e + 2.0) * den;
+                d = 1.0 + 2.0 * den * (-1.0 + 2.0 * zz * (1.0 - (e + 2.0) * den));
+                const double t1 = 4.0 * e * (e + 1.0) * den * den;
+                const double t2 = 4.0 * den * den * den * e * (2.0 + 2.0 * e - 3.0 * e * e - 2.0 * e * e * e);
+                d2 = c * (2.0 * t1 + zz * t2);
+            }
+            return;
+        }
+        case N_PFLU: {  // nn.cpp:605-618
+            const double zz = c * z, z2 = zz * zz, fs = 1.0 / std::sqrt(z2 + 1.0), fs3 = fs * fs * fs;
+            a = 0.5 * z * (1.0 + zz * fs); d = 0.5 * (zz * (z2 + 2.0) * fs3 + 1.0); d2 = -0.5 * c * (z2 - 2.0) * fs3 * fs * fs;
+            return;
+        }
+        case N_SERF: {  // nn.cpp:634-646 (no c)
+            const double fe = std::exp(z), fl = std::log1p(fe), ef = std::erf(fl), g = std::exp(-fl * fl), s = 1.0 / (1.0 + 1.0 / fe);
+            a = z * ef; d = ef + 2.0 / RADPI * g * z * s; d2 = 2.0 / RADPI * g * s * (2.0 - 2.0 * z * fl * s + z * (1.0 - s));
+            return;
+        }
+        case N_LOGISH: {  // nn.cpp:662-680 (no c)
+            const double l2i = 1.0 / LOG2, e = std::exp(-z), lf = std::log(1.0 + 1.0 / (1.0 + e));
+            const double q = e / ((1.0 + e) * (2.0 + e)), qp = e * (e * e - 2.0) / ((1.0 + e) * (1.0 + e) * (2.0 + e) * (2.0 + e));
+            a = l2i * z * lf; d = l2i * (lf + z * q); d2 = l2i * (2.0 * q + z * qp);
+            return;
+        }
         case N_SOFTPLUS: {
             const double ci = 1.0 / c;
             // AFFPBP::af_softplus branches on z>0 (nn.cpp:694-708); AFFPBP2 on z>=0; identical values.
             if (z > 0.0) { const double e = std::exp(-c * z); const double den = 1.0 / (e + 1.0); a = z + ci * (std::log1p(e) - LOG2); d = 1.0 / (e + 1.0); d2 = c * e * den * den; }
             else { const double e = std::exp(c * z); const double den = 1.0 / (e + 1.0); a = ci * (std::log1p(e) - LOG2); d = e / (e + 1.0); d2 = c * e * den * den; }
+            return;
+        }
+        case N_SQPLUS: {  // nn.cpp:740-750
+            const double zz = c * z, fs = std::sqrt(1.0 + zz * zz);
+            a = 0.5 / c * (zz - 1.0 + fs); d = 0.5 * (zz / fs + 1.0); d2 = 0.5 * c / (fs * fs * fs);
+            return;
+        }
+        case N_ATISH: {  // nn.cpp:769-779 (no c)
+            const double zz = 0.5 * PI * z, fr = 1.0 / (1.0 + zz * zz), at = std::atan(zz);
+            a = z * 0.5 * (1.0 + 2.0 / PI * at); d = 0.5 * (1.0 + z * fr) + at / PI; d2 = fr * fr;
+            return;
+        }
+        case N_TEST: {  // nn.cpp:802-812
+            const double zz = c * z, z2 = zz * zz, z4 = z2 * z2, den = 1.0 / std::sqrt(std::sqrt(z4 + 1.0));
+            const double den4 = den * den * den * den;
+            a = 0.5 * z * (1.0 + zz * den); d = 0.5 * (zz * den * (1.0 + 1.0 / (z4 + 1.0)) + 1.0);
+            d2 = 0.5 * c * (den + (1.0 - z4) * den * den4 - 5.0 * z4 * den * den4 * den4);
             return;
         }
         default: throw std::invalid_argument("activation not supported by the oracle");
@@ -893,6 +995,9 @@ int orc_type_index(void* p, const char* name) { auto& m = ((NNP*)p)->index; auto
 void orc_get_params(void* p, double* out) { int c = 0; for (auto& h : ((NNP*)p)->h) { h.nn.pack(out + c); c += h.nn.size(); } }
 void orc_set_params(void* p, const double* in) { int c = 0; for (auto& h : ((NNP*)p)->h) { h.nn.unpack(in + c); c += h.nn.size(); } }
 
+int orc_activate(int neuron, double c, double z, double* a, double* d, double* d2) {
+    try { activate(neuron, c, z, *a, *d, *d2); return 0; } catch (std::exception& e) { return -1; }
+}
 double orc_fmexp(double x) { return fmexp(x); }
 double orc_coscut(double x) { return coscut(x); }
 double orc_sincut(double x) { return sincut(x); }

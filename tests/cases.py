@@ -99,6 +99,30 @@ def generic_potential_text(seed=7) -> str:
         v1=_fmt(rng.normal(0, 0.5, 6 * 10)), v2=_fmt(rng.normal(0, 0.5, 6)))
 
 
+NEURONS = ["LINEAR", "SIGMOID", "TANH", "ISRU", "ARCTAN", "RELU", "ELU", "TANHRE", "SQRE", "SWISH", "GELU", "MISH",
+           "PFLU", "SERF", "LOGISH", "SOFTPLUS", "SQPLUS", "ATISH", "TEST"]     # nn.hpp:84-103, enum values 1..19
+
+
+def activation_potential_text(neuron: str, c: float = 1.3, seed: int = 5) -> str:
+    """A small binary potential (4 radial per species, 2x8 angular per pair: 32 inputs, 32-12-10-1
+    networks) whose hidden layers use the given activation with scale c; Xavier weights, input
+    scaling that keeps the pre-activations near the activation's curved part."""
+    text = W.potential_text(["A", "B"], 6.5, 4, [0.003, 0.01], [12, 10, 1], neuron)
+    nin = 2 * 4 + 3 * 2 * 8
+    params = [W.xavier_network(seed + 100 * t, nin, [12, 10, 1]) for t in range(2)]
+    text = W.set_network_text(text, params, nin, [12, 10, 1])
+    text = text.replace(f"neuron {neuron} 1.000000", f"neuron {neuron} {c:f}")
+    rng = np.random.default_rng(seed)
+    out = []
+    for line in text.splitlines():
+        if line.startswith("inpw "):
+            line = "inpw " + _fmt(rng.uniform(0.02, 0.2, nin))
+        elif line.startswith("inpb "):
+            line = "inpb " + _fmt(rng.uniform(-2.0, 0.0, nin))
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
 def config_potential(ctx, cfg, tmp_path, precondition_batch=None):
     """Initialise the configuration potential in ctx, round-trip it through the 'ann' text format
     (what both sides read) and return that text."""

@@ -61,6 +61,7 @@ class Oracle:
             getattr(L, f).restype = C.c_double
             getattr(L, f).argtypes = [C.c_double]
         L.orc_cutoff.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D]
+        L.orc_activate.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D, _D]
         L.orc_basisR.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, C.c_double, _D, _D, _D, _D]
         L.orc_basisA.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, _I, C.c_double, C.c_double, C.c_double, _D, _D, _D, _D, _D]
         L.orc_neighbors.restype = C.c_longlong
@@ -84,6 +85,13 @@ class Oracle:
         return Potential(self, p)
 
     # ---- geometry
+    def activate(self, neuron: int, c: float, z: float):
+        """(a, d, d2) of the oracle's activation (the reference's AFFPBP forms)."""
+        a, d, d2 = np.zeros(1), np.zeros(1), np.zeros(1)
+        if self.L.orc_activate(neuron, c, z, _d(a), _d(d), _d(d2)) != 0:
+            raise ValueError(f"activation {neuron} not supported")
+        return float(a[0]), float(d[0]), float(d2[0])
+
     def neighbors(self, x, R, rc):
         x = np.ascontiguousarray(x, np.float64)
         Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))

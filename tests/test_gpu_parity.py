@@ -199,3 +199,17 @@ def test_errors_are_reported(ctx, tmp_path):
         ctx.load_text("ann\nntypes 0\n")
     # the context stays usable
     ctx.compute(offs, posn, types, cell)
+
+
+@pytest.mark.parametrize("neuron", cases.NEURONS)
+def test_every_activation(ctx, oracle, neuron):
+    """Hidden layers with each activation of nn.cpp:149-810: FP64 as the oracle, mixed (tensor-core
+    networks where they apply) within the mixed bars."""
+    text = cases.activation_potential_text(neuron)
+    ctx.load_text(text)
+    pot = oracle.load_text(text)
+    offs, posn, types, cell = cases.batch(cases.small_binary(n_struc=2, seed=6))
+    E, F, Wv = ctx.compute(offs, posn, types, cell, precision=FP64)
+    Eo, Fo, Wo, _, _ = pot.compute(offs, posn, types, cell)
+    assert _rel_err(E, Eo) < REL and _rel_err(F, Fo) < REL and _rel_err(Wv, Wo) < REL
+    _check_mixed(ctx, offs, posn, types, cell, E, F)

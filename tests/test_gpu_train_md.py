@@ -119,3 +119,17 @@ def test_md_energy_conservation(ctx, tmp_path, prec):
     drift = abs(pe + ke - e0) / len(t)          # eV/atom over 0.8 ps
     assert drift < 2e-4, drift
     assert rebuilds >= 0
+
+
+@pytest.mark.parametrize("neuron", ["GELU", "MISH", "SERF", "ARCTAN", "TEST"])
+def test_gradient_other_activations(ctx, oracle, neuron):
+    """the force-term adjoint through f'' of the other activations, FP64 vs the oracle"""
+    text = cases.activation_potential_text(neuron)
+    ctx.load_text(text)
+    pot = oracle.load_text(text)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    loss = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 0.3, 1.0, precision=FP64)
+    g = ctx.train_backward()
+    lo, go = pot.train(offs, posn, types, cell, Eref, Fref, 0.3, 1.0)
+    assert np.allclose(loss, lo, rtol=1e-10, atol=1e-14)
+    assert np.abs(g - go).max() <= 1e-9 * np.abs(go).max()

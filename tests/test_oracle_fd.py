@@ -180,3 +180,43 @@ def test_energy_gradient_matches_error_cost_o1(oracle):
     l2, g2 = pot.error_cost_o1(offs, posn, types, cell, Eref)
     assert abs(loss[1] - l2) < 1e-12 * max(1, abs(l2))
     assert np.allclose(g, g2, rtol=1e-10, atol=1e-14)
+
+
+@pytest.mark.parametrize("neuron", range(1, 20))
+def test_activation_derivatives_fd(oracle, neuron):
+    """d = da/dz and d2 = dd/dz for every activation of nn.cpp:149-810, away from the kinks at 0"""
+    h = 1e-5
+    for c in (0.7, 1.3):
+        for z in np.concatenate([np.linspace(-3.0, -0.05, 9), np.linspace(0.05, 3.0, 9)]):
+            a, d, d2 = oracle.activate(neuron, c, z)
+            ap, dp, _ = oracle.activate(neuron, c, z + h)
+            am, dm, _ = oracle.activate(neuron, c, z - h)
+            assert abs((ap - am) / (2 * h) - d) <= 1e-7 * max(1.0, abs(d)), (neuron, c, z, d)
+            assert abs((dp - dm) / (2 * h) - d2) <= 1e-6 * max(1.0, abs(d2)), (neuron, c, z, d2)
+
+
+@pytest.mark.parametrize("neuron", ["ISRU", "ARCTAN", "TANHRE", "SWISH", "GELU", "MISH", "PFLU", "SERF", "LOGISH",
+                                    "SQPLUS", "ATISH", "TEST"])
+def test_training_gradient_fd_activations(oracle, neuron):
+    """the force term of the training loss uses f'' of the hidden activations"""
+    pot = oracle.load_text(cases.activation_potential_text(neuron))
+    structs = cases.small_binary(n_struc=1, seed=4)
+    offs, posn, types, cell = pack_batch(structs)
+    Eref, Fref = W.lennard_jones(structs)
+    Fref = np.concatenate(Fref) * 0.01
+    Eref = Eref * 0.01
+    loss, g = pot.train(offs, posn, types, cell, Eref, Fref, 0.3, 1.0)
+    p0 = pot.get_params()
+    rng = np.random.default_rng(11)
+    gscale = np.abs(g).max()
+    for k in rng.choice(len(p0), 8, replace=False):
+        hh = 1e-5 * max(1.0, abs(p0[k]))
+        pp = p0.copy(); pp[k] += hh
+        pot.set_params(pp)
+        lp = pot.train(offs, posn, types, cell, Eref, Fref, 0.3, 1.0)[0][0]
+        pp[k] -= 2 * hh
+        pot.set_params(pp)
+        lm = pot.train(offs, posn, types, cell, Eref, Fref, 0.3, 1.0)[0][0]
+        pot.set_params(p0)
+        fd = (lp - lm) / (2 * hh)
+        assert abs(fd - g[k]) <= 1e-6 * max(abs(fd), abs(g[k])) + 1e-7 * gscale, (neuron, k, fd, g[k])
