@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -37,11 +38,16 @@ using namespace ann;
 static std::mutex g_err_mu;
 static std::string g_err;
 
+// every (re)allocation of a device buffer bumps this counter; captured graphs record it and are
+// recaptured when it moved (a graph holds raw buffer pointers)
+static std::atomic<uint64_t> g_alloc_gen{0};
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
     void ensure(size_t b) {
         if (b <= bytes && p) return;
+        ++g_alloc_gen;
         if (p) cudaFree(p);
         p = nullptr; bytes = 0;
         const size_t want = std::max<size_t>(b, 256);
@@ -89,8 +95,10 @@ static void upload_ints(DevBuf& b, const std::vector<int>& v, cudaStream_t st) {
 
 struct GraphKey {
     int S, N, cap, prec, forces, nbins, nchunks;
+    uint64_t gen;   // g_alloc_gen at capture
     bool operator==(const GraphKey& o) const {
-        return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins && nchunks == o.nchunks;
+        return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins && nchunks == o.nchunks &&
+               gen == o.gen;
     }
 };
 
@@ -109,8 +117,11 @@ struct ann_ctx {
     // batch
     int S = 0, N = 0;
     bool have_batch = false;
-    std::vector<int32_t> off_h, sid_h, rchunk_h, rschunk_h;
-    DevBuf off, cell, pos, type, sid, rchunk, rschunk, rpartial;
+    std::vector<int32_t> off_h, rchunk_h, rschunk_h, tables_h;
+    DevBuf tables, cell, pos, type, sid, rpartial;
+    const int32_t* off_d = nullptr;        // device offsets [S+1] (inside tables)
+    const int32_t* rchunk_d = nullptr;     // reduction chunks [3 * nchunks] (inside tables)
+    const int32_t* rschunk_d = nullptr;    // first chunk of each structure [S+1] (inside tables)
     // neighbour list
     int cap = 0, nbins_cap = 0;
     DevBuf geo, pos4, abin, abc, am, aslot, bcount, bstart, bidx, bm, bpos4, bposd, nbins_total, nn, ntc, nj, nimg, nr, scan_tmp, counter, status;
@@ -121,7 +132,7 @@ struct ann_ctx {
     // graphs
     // graphs of the E+F sequence: [0] with the list build, [1] with the Verlet-list refresh (MD)
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    GraphKey gkey[2] = {{-1, -1, -1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1, -1, -1}};
+    GraphKey gkey[2] = {{-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}};
     // training
     DevBuf Eref, Fref, loss3, ce, lam, U, grad;
     bool have_train = false;
@@ -173,7 +184,7 @@ static void upload_params(ann_ctx* c, ParamSet<real>& P) {
 static void reset_graph(ann_ctx* c) {
     for (int k = 0; k < 2; ++k) {
         if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
-        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1};
+        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, 0};
     }
 }
 static void rebuild_plan(ann_ctx* c) {
@@ -217,7 +228,7 @@ static int estimate_cap(ann_ctx* c, const double* cell) {
 static void ensure_batch_buffers(ann_ctx* c) {
     const int S = c->S, N = std::max(c->N, 1), T = c->pot.ntypes(), imax = c->pot.max_input();
     const size_t rb = sizeof(double);  // sized for the widest precision
-    c->off.ensure(sizeof(int32_t) * (S + 1)); c->cell.ensure(sizeof(double) * 9 * std::max(S, 1));
+    c->cell.ensure(sizeof(double) * 9 * std::max(S, 1));
     c->pos.ensure(sizeof(double) * 3 * N); c->type.ensure(sizeof(int32_t) * N); c->sid.ensure(sizeof(int32_t) * N);
     c->geo.ensure(sizeof(StrucGeo) * std::max(S, 1));
     c->nbins_cap = 2 * N + S + 2;
@@ -243,9 +254,7 @@ static void stage_offsets(ann_ctx* c, int nstruc, const int64_t* atom_offsets) {
     c->S = nstruc;
     c->N = (int)atom_offsets[nstruc];
     c->off_h.assign(nstruc + 1, 0);
-    c->sid_h.assign(c->N, 0);
     for (int s = 0; s <= nstruc; ++s) c->off_h[s] = (int32_t)atom_offsets[s];
-    for (int s = 0; s < nstruc; ++s) for (int i = c->off_h[s]; i < c->off_h[s + 1]; ++i) c->sid_h[i] = s;
     // chunks of the per-structure reductions
     c->rchunk_h.clear();
     c->rschunk_h.assign(nstruc + 1, 0);
@@ -263,9 +272,8 @@ static void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const doub
     stage_offsets(c, nstruc, offs);
     if (c->N > 0 && (!posn || !type)) throw ann_error(ANN_ERR_ARG, "posn/type is NULL");
     if (nstruc > 0 && !cell) throw ann_error(ANN_ERR_ARG, "cell is NULL");
+    // types and positions are checked on the device (ST_BAD_TYPE, ST_NONFINITE), cells here
     if (!device_src) {
-        for (int i = 0; i < c->N; ++i) if (type[i] < 0 || type[i] >= c->pot.ntypes()) throw ann_error(ANN_ERR_ARG, "type index out of range at atom " + std::to_string(i));
-        for (int64_t k = 0; k < 3 * (int64_t)c->N; ++k) if (!std::isfinite(posn[k])) throw ann_error(ANN_ERR_NUMERIC, "non-finite position");
         for (int64_t k = 0; k < 9 * (int64_t)nstruc; ++k) if (!std::isfinite(cell[k])) throw ann_error(ANN_ERR_NUMERIC, "non-finite cell");
         for (int s = 0; s < nstruc; ++s) {
             const double* R = cell + 9 * s;
@@ -276,21 +284,26 @@ static void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const doub
     if (c->cap == 0) c->cap = estimate_cap(c, device_src ? nullptr : cell);
     ensure_batch_buffers(c);
     const cudaMemcpyKind k = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    ck(cudaMemcpyAsync(c->off.p, c->off_h.data(), 4 * (c->S + 1), cudaMemcpyHostToDevice, c->stream), "H2D offsets");
     {
-        // sized by the bound S + N / RED_CHUNK + 1, so that a captured graph's pointers stay valid
-        // for every batch with the same S and N
-        const size_t nch = c->rchunk_h.size() / 3;
+        // offsets, the reduction chunks and the structures' first chunks in one copy (pageable
+        // copies return once the host data is staged). The chunk buffers are sized by the bound
+        // S + N / RED_CHUNK + 1, so that a captured graph's pointers stay valid for every batch
+        // with the same S and N.
         const size_t nmax = (size_t)c->S + (size_t)c->N / RED_CHUNK + 1;
-        c->rchunk.ensure(4 * 3 * nmax);
-        c->rschunk.ensure(4 * ((size_t)c->S + 1));
+        const size_t o_ch = (size_t)c->S + 1, o_sc = o_ch + 3 * nmax;
+        c->tables_h.assign(o_sc + c->S + 1, 0);
+        std::copy(c->off_h.begin(), c->off_h.end(), c->tables_h.begin());
+        std::copy(c->rchunk_h.begin(), c->rchunk_h.end(), c->tables_h.begin() + o_ch);
+        std::copy(c->rschunk_h.begin(), c->rschunk_h.end(), c->tables_h.begin() + o_sc);
+        c->tables.ensure(4 * c->tables_h.size());
         c->rpartial.ensure(sizeof(double) * 10 * nmax);
-        if (nch) ck(cudaMemcpyAsync(c->rchunk.p, c->rchunk_h.data(), 4 * c->rchunk_h.size(), cudaMemcpyHostToDevice, c->stream), "H2D chunks");
-        ck(cudaMemcpyAsync(c->rschunk.p, c->rschunk_h.data(), 4 * c->rschunk_h.size(), cudaMemcpyHostToDevice, c->stream), "H2D chunks");
-        ck(cudaStreamSynchronize(c->stream), "H2D chunks");   // the host tables are rebuilt by the next batch
+        ck(cudaMemcpyAsync(c->tables.p, c->tables_h.data(), 4 * c->tables_h.size(), cudaMemcpyHostToDevice, c->stream), "H2D offsets");
+        c->off_d = c->tables.as<int32_t>();
+        c->rchunk_d = c->off_d + o_ch;
+        c->rschunk_d = c->off_d + o_sc;
     }
     if (c->N > 0) {
-        ck(cudaMemcpyAsync(c->sid.p, c->sid_h.data(), 4 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D sid");
+        launch_fill_sid(c->S, c->off_d, c->sid.as<int32_t>(), c->stream);
         ck(cudaMemcpyAsync(c->pos.p, posn, sizeof(double) * 3 * (size_t)c->N, k, c->stream), "copy positions");
         ck(cudaMemcpyAsync(c->type.p, type, sizeof(int32_t) * (size_t)c->N, k, c->stream), "copy types");
     }
@@ -313,7 +326,7 @@ static BpArgs<real> bp_args(ann_ctx* c) {
 static NbrArgs nbr_args(ann_ctx* c, double rc) {
     NbrArgs a{};
     a.nstruc = c->S; a.natoms = c->N; a.ntypes = c->pot.ntypes(); a.cap = c->cap; a.rc = rc;
-    a.off = c->off.as<int32_t>(); a.cell = c->cell.as<double>(); a.pos = c->pos.as<double>(); a.type = c->type.as<int32_t>(); a.sid = c->sid.as<int32_t>();
+    a.off = c->off_d; a.cell = c->cell.as<double>(); a.pos = c->pos.as<double>(); a.type = c->type.as<int32_t>(); a.sid = c->sid.as<int32_t>();
     a.geo = c->geo.as<StrucGeo>(); a.pos4 = c->pos4.as<float4>(); a.abin = c->abin.as<int32_t>(); a.abc = c->abc.as<int32_t>(); a.am = c->am.as<int32_t>();
     a.aslot = c->aslot.as<int32_t>(); a.bcount = c->bcount.as<int32_t>(); a.bstart = c->bstart.as<int32_t>(); a.bidx = c->bidx.as<int32_t>();
     a.bm = c->bm.as<int32_t>(); a.bpos4 = c->bpos4.as<float4>(); a.bposd = c->bposd.as<double>(); a.nbins_cap = c->nbins_cap;
@@ -341,7 +354,7 @@ static void mark(ann_ctx* c, int k) {
 static RedTable red_table(ann_ctx* c) {
     RedTable t;
     t.nchunks = (int32_t)(c->rchunk_h.size() / 3);
-    t.chunk = c->rchunk.as<int32_t>(); t.schunk = c->rschunk.as<int32_t>(); t.partial = c->rpartial.as<double>();
+    t.chunk = c->rchunk_d; t.schunk = c->rschunk_d; t.partial = c->rpartial.as<double>();
     return t;
 }
 
@@ -410,7 +423,7 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
                                               " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
     if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
-    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3)};
+    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), g_alloc_gen.load()};
     const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
     const int gs = build_list ? 0 : 1;
     if (graphs) {
@@ -519,12 +532,12 @@ int ann_destroy(ann_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     reset_graph(c);
     c->pf.release(); c->pd.release();
-    for (DevBuf* b : {&c->poff, &c->off, &c->cell, &c->pos, &c->type, &c->sid, &c->geo, &c->pos4, &c->abin, &c->abc, &c->am, &c->aslot,
+    for (DevBuf* b : {&c->poff, &c->cell, &c->pos, &c->type, &c->sid, &c->geo, &c->pos4, &c->abin, &c->abc, &c->am, &c->aslot,
                       &c->bcount, &c->bstart, &c->bidx, &c->bm, &c->bpos4, &c->bposd, &c->nbins_total, &c->nn, &c->ntc, &c->nj, &c->nimg,
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
-                      &c->rchunk, &c->rschunk, &c->rpartial, &c->tcimg})
+                      &c->tables, &c->rpartial, &c->tcimg})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -830,7 +843,7 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
         if (c->S > 0) ck(cudaMemcpyAsync(c->Eref.p, Eref, 8 * (size_t)c->S, cudaMemcpyHostToDevice, c->stream), "H2D Eref");
         if (c->N > 0) ck(cudaMemcpyAsync(c->Fref.p, Fref, 8 * 3 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D Fref");
         ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
-        launch_train_loss(c->S, c->N, c->off.as<int32_t>(), c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
+        launch_train_loss(c->S, c->N, c->off_d, c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
                           c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->loss3.as<double>(), c->ce.as<double>(), c->lam.p,
                           prec == ANN_FP64, c->stream);
         ck(cudaGetLastError(), "loss kernel");

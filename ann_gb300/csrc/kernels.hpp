@@ -113,6 +113,7 @@ struct RedTable {
 template <typename real>
 void launch_reduce_structures(int nstruc, const RedTable& t, const double* Eatom, const real* W, const real* F,
                               double* Es, double* Ws, double* Fout, cudaStream_t st);
+void launch_fill_sid(int nstruc, const int32_t* off, int32_t* sid, cudaStream_t st);
 void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st);
 size_t scan_tmp_ints(int n);
 

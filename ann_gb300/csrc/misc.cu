@@ -71,6 +71,15 @@ void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp,
     ++::ann::g_launch_counter, k_scan_add<<<nb, SCAN_T, 0, st>>>(out, n, tmp);
 }
 
+// ---------------------------------------------------------------- structure of every atom
+__global__ void k_fill_sid(const int32_t* off, int32_t* sid) {
+    const int s = blockIdx.x;
+    for (int i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) sid[i] = s;
+}
+void launch_fill_sid(int nstruc, const int32_t* off, int32_t* sid, cudaStream_t st) {
+    if (nstruc > 0) ++::ann::g_launch_counter, k_fill_sid<<<nstruc, 128, 0, st>>>(off, sid);
+}
+
 // ---------------------------------------------------------------- per-type atom lists
 // slots within each type: lanes of a warp with the same type are counted together
 // (match + popc), the block's counts go to global memory with one atomic per type
