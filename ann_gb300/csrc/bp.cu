@@ -127,7 +127,7 @@ template <typename real, int NG, int PASS>
 struct WarpMem {
     typedef typename V4<real>::T R4;
     R4* geo;             // (ux, uy, uz, 1/d)
-    real* dp;            // [e][2*NG]: D_0, Dp_0, D_1, Dp_1, ...
+    real* dp;            // [e][2*NG]: D_0, D_1, ..., Dp_0, Dp_1, ...
     real *d, *fc, *fcg;
     real *ax, *ay, *az;  // force accumulators (FORCE)
     R4* tg;              // tangent of the pair vector (drx, dry, drz, dd) (JVP)
@@ -190,8 +190,8 @@ struct DampRec {
 #pragma unroll
         for (int q = 0; q < 2 * NG; ++q) v[q] = real(0);
     }
-    __device__ __forceinline__ real D(int g) const { return v[2 * g]; }
-    __device__ __forceinline__ real Dp(int g) const { return v[2 * g + 1]; }
+    __device__ __forceinline__ real D(int g) const { return v[g]; }        // record: D_0..D_{NG-1}, Dp_0..Dp_{NG-1}
+    __device__ __forceinline__ real Dp(int g) const { return v[NG + g]; }
 };
 
 // ---------------------------------------------------------------- force pass, fast path
@@ -200,6 +200,28 @@ struct DampRec {
 // The block's weighted sum over slots, A_g(cos) = sum_s dE/dG_s |1/2 + lambda_s cos/2|^zeta_s,
 // is a polynomial of degree 8 in cos (zeta = 1,2,4,8; the bases are never negative for
 // |cos| <= 1); al[g][p] holds its coefficients and Horner's rule gives A_g and dA_g/dcos together.
+// two FP32 lanes per register pair (packed FMA of sm_100+), used for the two damping groups
+static __device__ __forceinline__ uint64_t pk2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+static __device__ __forceinline__ float hsum2(uint64_t v) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return lo + hi;
+}
+static __device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+static __device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 template <typename real, int NG>
 __device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, const DampRec<real, NG>& dj,
                                               const typename V4<real>::T& gk, const DampRec<real, NG>& dk,
@@ -219,6 +241,28 @@ __device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, co
     const real idj = gj.w, idk = gk.w;
     const real cj = -phi * cs * idj + e0, bj = phi * idj;
     const real ck = -phi * cs * idk + e1, bk = phi * idk;
+    vj[0] = cj * gj.x + bj * gk.x; vj[1] = cj * gj.y + bj * gk.y; vj[2] = cj * gj.z + bj * gk.z;
+    vk[0] = ck * gk.x + bk * gj.x; vk[1] = ck * gk.y + bk * gj.y; vk[2] = ck * gk.z + bk * gj.z;
+}
+
+// the same for FP32 and two damping groups, both groups at once in packed FP32 pairs (group 0 in
+// the low half): alp[p] = (al[0][p], al[1][p])
+__device__ __forceinline__ void triplet_force2(const Vec4f& gj, const DampRec<float, 2>& dj, const Vec4f& gk, const DampRec<float, 2>& dk,
+                                               const uint64_t (&alp)[9], float (&vj)[3], float (&vk)[3]) {
+    const float cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
+    const uint64_t c2 = pk2(cs, cs);
+    uint64_t B = alp[8];
+    uint64_t A = fma2(B, c2, alp[7]);
+#pragma unroll
+    for (int p = 6; p >= 0; --p) { B = fma2(B, c2, A); A = fma2(A, c2, alp[p]); }
+    const uint64_t Dj = pk2(dj.v[0], dj.v[1]), Dpj = pk2(dj.v[2], dj.v[3]);
+    const uint64_t Dk = pk2(dk.v[0], dk.v[1]), Dpk = pk2(dk.v[2], dk.v[3]);
+    const float phi = -hsum2(mul2(B, mul2(Dj, Dk)));
+    const float e0 = -hsum2(mul2(mul2(A, Dpj), Dk));
+    const float e1 = -hsum2(mul2(mul2(A, Dj), Dpk));
+    const float idj = gj.w, idk = gk.w;
+    const float cj = -phi * cs * idj + e0, bj = phi * idj;
+    const float ck = -phi * cs * idk + e1, bk = phi * idk;
     vj[0] = cj * gj.x + bj * gk.x; vj[1] = cj * gj.y + bj * gk.y; vj[2] = cj * gj.z + bj * gk.z;
     vk[0] = ck * gk.x + bk * gj.x; vk[1] = ck * gk.y + bk * gj.y; vk[2] = ck * gk.z + bk * gj.z;
 }
@@ -266,6 +310,12 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
     else { ga.x = ga.y = ga.z = ga.w = real(0); da.zero(); }
     real sa[3] = {real(0), real(0), real(0)}, sb[3] = {real(0), real(0), real(0)};
+    constexpr bool PACKED = std::is_same<real, float>::value && NG == 2;
+    uint64_t alp[9];
+    if constexpr (PACKED) {
+#pragma unroll
+        for (int p = 0; p < 9; ++p) alp[p] = pk2(al[0][p], al[NG - 1][p]);
+    }
     const int n = np;
     const int steps = TRI ? np / 2 : np;      // triangle: steps 1..n/2, rectangle: 0..n-1
     const int qb = TRI ? p0 : q0;
@@ -281,7 +331,8 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
         DampRec<real, NG> db;
         db.load(w.dp + e * NDP);
         real vj[3], vk[3];
-        triplet_force<real, NG>(ga, da, gb, db, al, vj, vk);
+        if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, vj, vk);
+        else triplet_force<real, NG>(ga, da, gb, db, al, vj, vk);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             sa[c] += valid ? vj[c] : real(0);
@@ -437,8 +488,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ De
 #pragma unroll
                         for (int q = 0; q < NG; ++q) {
                             const real ex = M<real>::bexp(-dd * dd * ie2[q]);
-                            w.dp[o * NDP + 2 * q] = f * ex;
-                            w.dp[o * NDP + 2 * q + 1] = ex * (g - real(2) * dd * f * ie2[q]);
+                            w.dp[o * NDP + q] = f * ex;
+                            w.dp[o * NDP + NG + q] = ex * (g - real(2) * dd * f * ie2[q]);
                         }
                     }
                     if (PASS == PASS_FORCE) {
