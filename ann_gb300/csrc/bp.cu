@@ -386,7 +386,7 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
 
 // ---------------------------------------------------------------- the kernel
 template <typename real, int NG, bool FAST, int PASS>
-__global__ void __launch_bounds__(BP_WARPS * 32) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
+__global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
     typedef typename V4<real>::T R4;
     extern __shared__ __align__(128) unsigned char bsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
