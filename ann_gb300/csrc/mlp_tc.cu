@@ -95,9 +95,14 @@ static __device__ __forceinline__ void put8(uint8_t* hi, uint8_t* lo, int r, int
     if (lo) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// the other activation forms of nn.cpp:149-810 with full-accuracy functions, out of line so that
+// the epilogue code of the common forms stays compact
+static __device__ __noinline__ void act_other(int neuron, float c, float z, float& a, float& d) {
+    float d2;
+    act_fd<float>(neuron, c, z, a, d, d2);
+}
 // activation value and first derivative: sigmoid, tanh and softplus with the hardware
-// approximations (exp2 / log2 / rcp; absolute errors ~1e-7, far inside the FP32 path's tolerance),
-// the other forms of nn.cpp:149-810 through act_fd
+// approximations (exp2 / log2 / rcp; absolute errors ~1e-7, far inside the FP32 path's tolerance)
 static __device__ __forceinline__ void act_fast(int neuron, float c, float z, float& a, float& d) {
     switch (neuron) {
         case N_SIGMOID: {
@@ -119,7 +124,7 @@ static __device__ __forceinline__ void act_fast(int neuron, float c, float z, fl
             d = (z > 0.0f) ? r : e * r;
             return;
         }
-        default: { float d2; act_fd<float>(neuron, c, z, a, d, d2); return; }   // the other forms, full-accuracy functions
+        default: act_other(neuron, c, z, a, d); return;
     }
 }
 
