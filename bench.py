@@ -347,10 +347,19 @@ def main():
     sm_mhz = clk.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12           # TFLOP/s (FMA = 2 flop) at the sampled clock
     mufu_peak = 152 * 16 * sm_mhz * 1e6 / 1e12                 # T ops/s
+    # DRAM bytes of one force-pass launch: the per-atom figure of the committed ncu capture (small
+    # case of the same workload) times the atoms of this launch
+    traffic, traffic_src = None, None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        tr = json.loads(tf.read_text()).get("k_bp force pass (forces)")
+        if tr:
+            traffic = float(tr["dram_bytes_per_atom"]) * N
+            traffic_src = f"{tr['dram_bytes_per_atom']} B/atom x {N} atoms, from {tr['source']}"
     roofline = {"kernel": "k_bp force pass (" + names[4] + ")", "bound": "hbm",
                 "achieved": work["force_bytes"] / t_force / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": work["force_bytes"] / t_force / 1e9 / pk["hbm_gbs"], "traffic": None,
-                "peak_source": pk["source"], "dominant_phase": names[dom]}
+                "frac": work["force_bytes"] / t_force / 1e9 / pk["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
+                "algorithmic_bytes": work["force_bytes"], "peak_source": pk["source"], "dominant_phase": names[dom]}
     roofline_compute = {"kernel": roofline["kernel"], "bound": "fp32+mufu",
                         "fp32_tflops": work["force_flops"] / t_force / 1e12, "fp32_peak_tflops": fp32_peak,
                         "frac_fp32": work["force_flops"] / t_force / 1e12 / fp32_peak,
