@@ -85,6 +85,8 @@ _SIGS = {
     "ann_get_neighbors": (C.c_int, [_V, _I32, _I32, _I32, _D, C.c_int64]),
     "ann_train_forward": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, C.c_double, C.c_double, C.c_int32, _D]),
     "ann_train_backward": (C.c_int, [_V, C.c_double, _D, C.c_int64]),
+    "ann_adam_init": (C.c_int, [_V, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "ann_adam_step": (C.c_int, [_V, C.c_double]),
     "ann_md_init": (C.c_int, [_V, C.c_int64, _D, _D, _I32, _D, _D, C.c_double, C.c_double, C.c_int32]),
     "ann_md_run": (C.c_int, [_V, C.c_int32, _D, _D, _I32]),
     "ann_md_get_state": (C.c_int, [_V, _D, _D, _D]),
@@ -364,6 +366,14 @@ class Context:
         g = np.zeros(self.nparams)
         self._ck(self.lib.ann_train_backward(self.h, scale, _d(g), len(g)))
         return g
+
+    def adam_init(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-16):
+        """Adam on the device (NN::ADAM; eps defaults to the reference's 1e-16)."""
+        self._ck(self.lib.ann_adam_init(self.h, lr, beta1, beta2, eps))
+
+    def adam_step(self, scale=1.0):
+        """One Adam step with the gradient of the last train_backward (times scale)."""
+        self._ck(self.lib.ann_adam_step(self.h, scale))
 
     # ---- MD
     def md_init(self, posn, vel, types, cell, masses, dt_fs=2.0, skin=0.5, precision=None):

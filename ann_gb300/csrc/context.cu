@@ -30,6 +30,11 @@ void launch_md_kick_drift(int natoms, double* pos, double* vel, const void* F, b
                           double dt, const double* R, const double* Ri, double* disp_ref, int32_t* maxdisp_flag, double half_skin2,
                           int stage, cudaStream_t st);
 void launch_md_ke(int natoms, const double* vel, const double* mass, const int32_t* type, double* ke, cudaStream_t st);
+// optimiser and parameter refresh (optim.cu)
+void launch_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2, double b1ii,
+                 double b2ii, double eps, cudaStream_t st);
+void launch_param_refresh(int64_t n, const double* p, const int32_t* map, double* w64, double* wt64, double* b64, float* w32, float* wt32,
+                          float* b32, uint8_t* img, cudaStream_t st);
 void configure_kernels();
 }
 
@@ -111,6 +116,14 @@ struct ann_ctx {
     PlanHost plan;
     TcPlan tc;                      // tensor-core network images (MIXED precision)
     DevBuf tcimg;
+    // packed FP64 parameters on the device and where each one is copied to
+    DevBuf p64, pmap;
+    bool params_dev_newer = false;  // an optimiser step changed p64 after the host copy
+    // Adam state (NN::ADAM, opt/algo.cpp:272-296)
+    DevBuf adam_m, adam_v;
+    bool adam_ready = false, have_grad = false;
+    int64_t adam_t = 0;
+    double adam_lr = 0, adam_b1 = 0, adam_b2 = 0, adam_eps = 0;
     ParamSet<float> pf;
     ParamSet<double> pd;
     DevBuf poff;
@@ -201,10 +214,34 @@ static void rebuild_plan(ann_ctx* c) {
     int64_t acc = 0;
     for (auto& s : c->pot.sp) { po.push_back((int)acc); acc += s.nn.size(); }
     upload_ints(c->poff, po, c->stream);
+    {
+        std::vector<int32_t> map;
+        build_param_map(c->plan.pot, c->tc, map);
+        std::vector<double> p((size_t)std::max<int64_t>(acc, 1), 0.0);
+        c->pot.get_params(p.data());
+        c->p64.ensure(8 * p.size());
+        c->pmap.ensure(4 * std::max<size_t>(map.size(), 1));
+        ck(cudaMemcpyAsync(c->p64.p, p.data(), 8 * p.size(), cudaMemcpyHostToDevice, c->stream), "upload params");
+        if (!map.empty()) ck(cudaMemcpyAsync(c->pmap.p, map.data(), 4 * map.size(), cudaMemcpyHostToDevice, c->stream), "upload params");
+        ck(cudaStreamSynchronize(c->stream), "upload params");
+        c->params_dev_newer = false;
+        c->have_grad = false;
+    }
     c->have_pot = true;
     c->have_results = false;
     c->have_train = false;
     reset_graph(c);
+}
+
+// after optimiser steps on the device the host copy of the parameters is brought up to date
+// before anything reads or rebuilds from it
+static void sync_params_from_device(ann_ctx* c) {
+    if (!c->params_dev_newer) return;
+    std::vector<double> p((size_t)c->pot.nparams());
+    ck(cudaMemcpyAsync(p.data(), c->p64.p, 8 * p.size(), cudaMemcpyDeviceToHost, c->stream), "D2H params");
+    ck(cudaStreamSynchronize(c->stream), "D2H params");
+    c->pot.set_params(p.data());
+    c->params_dev_newer = false;
 }
 
 // ---------------------------------------------------------------- batch buffers
@@ -265,6 +302,14 @@ static void stage_offsets(ann_ctx* c, int nstruc, const int64_t* atom_offsets) {
         }
     }
     c->rschunk_h[nstruc] = (int32_t)(c->rchunk_h.size() / 3);
+}
+
+// a batch staged by the compute or training calls replaces the MD system: the MD state (list skin,
+// velocities) no longer applies, and ann_md_init starts a new one
+static void leave_md(ann_ctx* c) {
+    if (!c->md_ready) return;
+    c->md_ready = false;
+    c->cap = 0;   // re-estimated without the skin
 }
 
 static void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell, bool device_src) {
@@ -537,7 +582,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
-                      &c->tables, &c->rpartial, &c->tcimg})
+                      &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->adam_m, &c->adam_v})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -559,6 +604,7 @@ int ann_load_potential_text(ann_ctx* c, const char* text) {
         p.read_text(text);
         p.validate();
         c->pot = p;
+        c->adam_ready = false;
         rebuild_plan(c);
     })
 }
@@ -575,6 +621,7 @@ int ann_write_potential(ann_ctx* c, const char* path) {
     if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
     std::ofstream f(path);
     if (!f) return fail(c, ANN_ERR_IO, std::string("could not write potential file: \"") + path + "\"");
+    try { set_device(c); sync_params_from_device(c); } catch (ann_error& e) { return fail(c, e.code, e.what()); }
     f << c->pot.write_text();
     return f.good() ? ANN_OK : fail(c, ANN_ERR_IO, "write failed");
 }
@@ -622,8 +669,7 @@ int ann_get_params(ann_ctx* c, double* p, int64_t n) {
     if (!c || !p) return fail(c, ANN_ERR_ARG, "NULL argument");
     if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
     if (n != c->pot.nparams()) return fail(c, ANN_ERR_ARG, "parameter count mismatch");
-    c->pot.get_params(p);
-    return ANN_OK;
+    ANN_TRY(c, { set_device(c); sync_params_from_device(c); c->pot.get_params(p); })
 }
 int ann_set_params(ann_ctx* c, const double* p, int64_t n) {
     if (!c || !p) return fail(c, ANN_ERR_ARG, "NULL argument");
@@ -638,6 +684,7 @@ int ann_set_input_scaling(ann_ctx* c, int32_t t, const double* w, const double* 
     if (n != c->pot.sp[t].nInput) return fail(c, ANN_ERR_ARG, "input count mismatch");
     ANN_TRY(c, {
         set_device(c);
+        sync_params_from_device(c);
         c->pot.sp[t].nn.inpw.assign(w, w + n);
         c->pot.sp[t].nn.inpb.assign(b, b + n);
         rebuild_plan(c);
@@ -647,16 +694,16 @@ int ann_init_network(ann_ctx* c, int32_t t, int32_t seed, int32_t dist, int32_t 
     if (!c) return fail(c, ANN_ERR_ARG, "NULL argument");
     if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
     if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
-    ANN_TRY(c, { set_device(c); init_network(c->pot.sp[t].nn, seed, dist, init, sb, sw); rebuild_plan(c); })
+    ANN_TRY(c, { set_device(c); sync_params_from_device(c); init_network(c->pot.sp[t].nn, seed, dist, init, sb, sw); rebuild_plan(c); })
 }
 
 int ann_batch_upload(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
-    ANN_TRY(c, { set_device(c); upload_batch(c, nstruc, offs, posn, type, cell, false); })
+    ANN_TRY(c, { set_device(c); leave_md(c); upload_batch(c, nstruc, offs, posn, type, cell, false); })
 }
 int ann_batch_set_device(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* d_posn, const int32_t* d_type, const double* d_cell) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
-    ANN_TRY(c, { set_device(c); upload_batch(c, nstruc, offs, d_posn, d_type, d_cell, true); })
+    ANN_TRY(c, { set_device(c); leave_md(c); upload_batch(c, nstruc, offs, d_posn, d_type, d_cell, true); })
 }
 int ann_batch_compute(ann_ctx* c, int32_t prec, int32_t want_forces) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
@@ -722,6 +769,7 @@ int ann_compute(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* p
     if (!energy) return fail(c, ANN_ERR_ARG, "energy is NULL");
     ANN_TRY(c, {
         set_device(c);
+        leave_md(c);
         upload_batch(c, nstruc, offs, posn, type, cell, false);
         run_batch(c, prec, forces != nullptr || virial != nullptr);
         finish_batch(c);
@@ -834,6 +882,7 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
     if (!Eref || !Fref || !loss3) return fail(c, ANN_ERR_ARG, "NULL argument");
     ANN_TRY(c, {
         set_device(c);
+        leave_md(c);
         upload_batch(c, nstruc, offs, posn, type, cell, false);
         run_batch(c, prec, true);
         finish_batch(c);
@@ -880,6 +929,47 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
         ck(cudaMemcpy(st, c->status.p, sizeof(st), cudaMemcpyDeviceToHost), "D2H status");
         if (st[0] != 0) throw ann_error(ANN_ERR_CUDA, "device status " + std::to_string(st[0]) + " in backward pass");
         for (int64_t k = 0; k < n; ++k) grad[k] *= scale;
+        c->have_grad = true;
+    })
+}
+
+int ann_adam_init(ann_ctx* c, double lr, double beta1, double beta2, double eps) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        if (!c->have_pot) throw ann_error(ANN_ERR_STATE, "no potential loaded");
+        if (!(lr > 0) || !(beta1 >= 0 && beta1 < 1) || !(beta2 >= 0 && beta2 < 1) || !(eps >= 0))
+            throw ann_error(ANN_ERR_ARG, "invalid Adam settings (lr > 0, 0 <= beta < 1, eps >= 0)");
+        set_device(c);
+        const size_t n = (size_t)std::max<int64_t>(c->pot.nparams(), 1);
+        c->adam_m.ensure(8 * n); c->adam_v.ensure(8 * n);
+        ck(cudaMemsetAsync(c->adam_m.p, 0, 8 * n, c->stream), "memset");
+        ck(cudaMemsetAsync(c->adam_v.p, 0, 8 * n, c->stream), "memset");
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+        c->adam_lr = lr; c->adam_b1 = beta1; c->adam_b2 = beta2; c->adam_eps = eps; c->adam_t = 0;
+        c->adam_ready = true;
+    })
+}
+int ann_adam_step(ann_ctx* c, double scale) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        if (!c->adam_ready) throw ann_error(ANN_ERR_STATE, "ann_adam_init first");
+        if (!c->have_grad) throw ann_error(ANN_ERR_STATE, "ann_adam_step needs the gradient of a preceding ann_train_backward");
+        set_device(c);
+        const int64_t n = c->pot.nparams();
+        ++c->adam_t;
+        const double b1ii = 1.0 / (1.0 - std::pow(c->adam_b1, (double)c->adam_t));
+        const double b2ii = 1.0 / (1.0 - std::pow(c->adam_b2, (double)c->adam_t));
+        const int64_t before = g_launch_counter;
+        launch_adam(n, c->grad.as<double>(), scale, c->adam_m.as<double>(), c->adam_v.as<double>(), c->p64.as<double>(), c->adam_lr, c->adam_b1,
+                    c->adam_b2, b1ii, b2ii, c->adam_eps, c->stream);
+        launch_param_refresh(n, c->p64.as<double>(), c->pmap.as<int32_t>(), c->pd.w.as<double>(), c->pd.wt.as<double>(), c->pd.b.as<double>(),
+                             c->pf.w.as<float>(), c->pf.wt.as<float>(), c->pf.b.as<float>(), c->tc.ok ? c->tcimg.as<uint8_t>() : nullptr,
+                             c->stream);
+        c->kernels += g_launch_counter - before;
+        ck(cudaGetLastError(), "Adam step");
+        c->params_dev_newer = true;
+        c->have_results = false;
+        c->have_grad = false;
     })
 }
 

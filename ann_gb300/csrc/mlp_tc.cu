@@ -266,7 +266,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
                 float e = 0.0f;
 #pragma unroll
                 for (int g = 0; g < TC_GROUPS; ++g) e += ered[g * TC_M + r];
-                a.Eatom[at] = (double)(tt.outb + tt.outw * (e + tt.blast)) + tt.evac;
+                const float blast = *reinterpret_cast<const float*>(img + tt.blast);
+                a.Eatom[at] = (double)(tt.outb + tt.outw * (e + blast)) + tt.evac;
             }
             for (int c0 = grp * 16; c0 < Nout; c0 += 16 * TC_GROUPS) {
                 float gv[16];

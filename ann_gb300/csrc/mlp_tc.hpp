@@ -29,9 +29,10 @@ struct TcType {
     uint32_t bias[TC_MAXH];          // byte offset of the FP32 bias of hidden layer l (padded width)
     uint32_t wlast;                  // FP32 weights of the last layer (padded width of the last hidden layer)
     uint32_t inpw, inpb;             // FP32 input scaling (K0 entries)
+    uint32_t blast;                  // FP32 bias of the last layer (one entry, padded to 16 B)
     uint32_t img_bytes;              // size of the image (multiple of 16)
     uint32_t img_off;                // offset of this type's image in the device buffer
-    float blast, outw, outb, c;
+    float outw, outb, c;
     double evac;
     int32_t neuron;
     int32_t wmax;                    // widest padded operand width (K0 or any hidden width)
@@ -52,6 +53,17 @@ struct TcPlan {
 // builds the images from the row-major FP64 weights of the plan (w[l][n*ni+m], b[l][n])
 void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::vector<double>& b,
                    const std::vector<double>& inpw, const std::vector<double>& inpb, int max_smem, TcPlan& out);
+
+// Where every network parameter lives on the device, in the packing order of ann_get_params
+// (per type: biases layer by layer, then weights layer by layer with the input index outer,
+// nn.cpp:846-859): 8 ints per parameter, -1 where a destination does not apply.
+enum ParamSlot { PM_KIND = 0, PM_I64, PM_IT, PM_F32, PM_FH, PM_FL, PM_BH, PM_BL, PM_N };
+enum ParamKind { PK_BIAS = 0, PK_WEIGHT = 1 };
+// PM_I64: index into the FP64/FP32 bias or row-major weight arrays; PM_IT: index into the
+// transposed weights; PM_F32: byte offset of an FP32 copy in the tensor-core images (hidden bias,
+// last-layer weight or bias); PM_FH/FL, PM_BH/BL: byte offsets of the BF16 hi/lo entries of the
+// forward (W) and backward (W^T) operands
+void build_param_map(const DevPot& pot, const TcPlan& tc, std::vector<int32_t>& map);
 
 struct TcArgs {
     int32_t natoms, imax, type;

@@ -71,7 +71,6 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
         tt.outw = (float)net.outw;
         tt.outb = (float)net.outb;
         tt.evac = pot.t[ty].evac;
-        tt.blast = (float)b[net.boff[L - 1]];
         // operand sizes
         size_t bf = 0;
         for (int l = 0; l < tt.nhidden; ++l) {
@@ -82,7 +81,7 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
         for (int l = 0; l < tt.nhidden; ++l) vec += (size_t)tt.width[l] * 4;
         vec += (size_t)tt.width[tt.nhidden - 1] * 4 + (size_t)tt.K0 * 8;
         auto total = [&](int split) {
-            const size_t img = bf * (split == 3 ? 2 : 1) + vec + 16 * (4 * TC_MAXH + 4);
+            const size_t img = bf * (split == 3 ? 2 : 1) + vec + 16 * (4 * TC_MAXH + 5);
             return (img + 127) / 128 * 128 + (size_t)TC_M * tt.wmax * 2 * (split >= 2 ? 2 : 1) + TC_TAIL_BYTES;
         };
         // both operands split (three MMAs per k-step) keep the products within ~1e-5 relative of
@@ -135,6 +134,7 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
             const double* WL = w.data() + net.woff[L - 1];   // 1 x nl
             tt.wlast = put_floats(tt.width[tt.nhidden - 1], [&](int k) { return k < nl ? WL[k] : 0.0; });
         }
+        tt.blast = put_floats(1, [&](int) { return b[net.boff[L - 1]]; });
         tt.inpw = put_floats(tt.K0, [&](int k) { return k < net.nin ? inpw[net.inoff + k] : 0.0; });
         tt.inpb = put_floats(tt.K0, [&](int k) { return k < net.nin ? inpb[net.inoff + k] : 0.0; });
         align16();
@@ -144,6 +144,44 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
         out.image.insert(out.image.end(), img.begin(), img.end());
     }
     if (out.image.empty()) out.image.resize(128, 0);
+}
+
+void build_param_map(const DevPot& pot, const TcPlan& tc, std::vector<int32_t>& map) {
+    map.clear();
+    auto put = [&](int kind, int i64, int iT, int64_t f32, int64_t fh, int64_t fl, int64_t bh, int64_t bl) {
+        const int64_t v[PM_N] = {kind, i64, iT, f32, fh, fl, bh, bl};
+        for (int k = 0; k < PM_N; ++k) map.push_back((int32_t)v[k]);
+    };
+    for (int ty = 0; ty < pot.ntypes; ++ty) {
+        const DevNet& net = pot.t[ty].net;
+        const int L = net.nlayer;
+        const bool img = tc.ok;
+        const TcType& tt = tc.t[ty];
+        const int64_t base = img ? (int64_t)tt.img_off : 0;
+        for (int l = 0; l < L; ++l)
+            for (int n = 0; n < net.nodes[l]; ++n) {
+                int64_t f32 = -1;
+                if (img) f32 = base + ((l < tt.nhidden) ? tt.bias[l] + 4 * n : tt.blast);
+                put(PK_BIAS, net.boff[l] + n, -1, f32, -1, -1, -1, -1);
+            }
+        for (int l = 0; l < L; ++l) {
+            const int ni = (l == 0) ? net.nin : net.nodes[l - 1], no = net.nodes[l];
+            for (int m = 0; m < ni; ++m)
+                for (int n = 0; n < no; ++n) {
+                    int64_t f32 = -1, fh = -1, fl = -1, bh = -1, bl = -1;
+                    if (img && l < tt.nhidden) {
+                        const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
+                        fh = base + tt.fwd_hi[l] + canon(n, m, Kin);
+                        fl = base + tt.fwd_lo[l] + canon(n, m, Kin);
+                        bh = base + tt.bwd_hi[l] + canon(m, n, tt.width[l]);
+                        bl = base + tt.bwd_lo[l] + canon(m, n, tt.width[l]);
+                    } else if (img) {
+                        f32 = base + tt.wlast + 4 * m;   // last layer: one output
+                    }
+                    put(PK_WEIGHT, net.woff[l] + n * ni + m, net.woff[l] + m * no + n, f32, fh, fl, bh, bl);
+                }
+        }
+    }
 }
 
 }  // namespace ann

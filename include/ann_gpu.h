@@ -159,6 +159,13 @@ int ann_train_forward(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets,
                       double* loss3);
 /* dL/dp (reference packing, types in NNP order) scaled by dl_scale. Requires ann_train_forward.  */
 int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t nparams);
+/* Adam optimiser on the device (NN::ADAM::step, opt/algo.cpp:272-296): ann_adam_init sets the
+ * step size (gamma), beta1, beta2, eps and zeroes the moments; each ann_adam_step applies one
+ * step with the gradient of the preceding ann_train_backward times scale, to the parameters held
+ * on the device (FP64 master and every FP32 / tensor-core copy), so that a training loop needs no
+ * parameter transfer. ann_get_params / ann_write_potential read the updated parameters.       */
+int ann_adam_init(ann_ctx* ctx, double lr, double beta1, double beta2, double eps);
+int ann_adam_step(ann_ctx* ctx, double scale);
 
 /* ---- molecular dynamics: velocity Verlet (integrator.cpp:177-200) --------------------------- */
 /* One structure; masses per type in Dalton. list_skin adds to rc for the Verlet list; the list is

@@ -133,3 +133,58 @@ def test_gradient_other_activations(ctx, oracle, neuron):
     lo, go = pot.train(offs, posn, types, cell, Eref, Fref, 0.3, 1.0)
     assert np.allclose(loss, lo, rtol=1e-10, atol=1e-14)
     assert np.abs(g - go).max() <= 1e-9 * np.abs(go).max()
+
+
+def test_adam_steps_on_device(ctx, tmp_path):
+    """Adam (NN::ADAM::step, opt/algo.cpp:280-296) applied on the device to the resident parameters:
+    the parameters after three steps equal the same update done in numpy, and the refreshed device
+    copies (FP64, FP32 and the tensor-core images) give the energies of a context loaded with them."""
+    text = cases.config_potential(ctx, 3, tmp_path)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    p = ctx.get_params()
+    lr, b1, b2, eps = 1e-3, 0.9, 0.999, 1e-16
+    ctx.adam_init(lr, b1, b2, eps)
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for t in range(1, 4):
+        ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+        g = ctx.train_backward()
+        ctx.adam_step()
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        p = p - lr / (1 - b1 ** t) * m / (np.sqrt(v / (1 - b2 ** t)) + eps)
+    pd = ctx.get_params()
+    assert np.allclose(pd, p, rtol=1e-12, atol=1e-15)
+    other = Context()
+    try:
+        other.load_text(text)
+        other.set_params(pd)
+        for prec in (FP64, MIXED):
+            E1, F1, _ = ctx.compute(offs, posn, types, cell, precision=prec)
+            E2, F2, _ = other.compute(offs, posn, types, cell, precision=prec)
+            # forces: Newton-3rd shares are added atomically, so their order (and the last FP32 bit) varies
+            assert np.allclose(E1, E2, rtol=1e-12, atol=1e-12)
+            assert np.abs(F1 - F2).max() <= (1e-12 if prec == FP64 else 1e-5)
+    finally:
+        other.close()
+
+
+def test_compute_after_md_leaves_md(ctx, tmp_path):
+    """A batch computed after an MD run replaces the MD system: same results as a fresh context."""
+    text = cases.config_potential(ctx, 5, tmp_path)
+    x, v, t, R = _md_case()
+    ctx.md_init(x, v, t, R, np.array([39.948]), dt_fs=2.0, skin=0.5, precision=MIXED)
+    ctx.md_run(3)
+    offs, posn, types, cell = pack_batch([(x, t, R)])
+    other = Context()
+    try:
+        other.load_text(text)
+        for prec in (FP64, MIXED):
+            a = ctx.compute(offs, posn, types, cell, precision=prec)
+            b = other.compute(offs, posn, types, cell, precision=prec)
+            assert np.array_equal(a[0], b[0])
+            assert np.abs(a[1] - b[1]).max() <= (1e-12 if prec == FP64 else 1e-5)
+        with pytest.raises(Exception):
+            ctx.md_run(1)
+    finally:
+        other.close()
