@@ -163,8 +163,9 @@ def cpu_reference(offs, posn, types, cell, pot_text, budget_s=12.0, steps=1, war
 
 def training_leg(dev, steps=10, warmup=3):
     """Training throughput on the 64-structure binary batch with Lennard-Jones labels: one
-    ann_train_forward + ann_train_backward (loss, adjoint, parameter gradient) per step, host
-    arrays in and the gradient out, wall-clock per step."""
+    ann_train_forward + ann_train_backward (loss, adjoint, parameter gradient) + ann_adam_step
+    (optimiser step on the resident parameters) per step, host arrays in and the gradient out,
+    wall-clock per step."""
     from ann_gb300 import FP64, MIXED, Context
     from ann_gb300 import workloads as WL
     from ann_gb300.api import pack_batch
@@ -176,16 +177,22 @@ def training_leg(dev, steps=10, warmup=3):
     WL.make_potential(ctx, 3)
     WL.precondition(ctx, offs, posn, types, cell)
     out = {"workload": f"{len(structs)} binary structures, N~U{{32..256}} ({int(offs[-1])} atoms), LJ labels, "
-                       "loss = mean (dE/N)^2 + 0.1 mean |dF|^2/3",
+                       "loss = mean (dE/N)^2 + 0.1 mean |dF|^2/3, Adam step on the device",
            "unit": "structures/s", "nparams": int(ctx.nparams)}
+    p0 = ctx.get_params()
     for name, prec in (("mixed", MIXED), ("fp64", FP64)):
+        ctx.set_params(p0)
+        ctx.adam_init(1e-4, 0.9, 0.999, 1e-16)
         for _ in range(warmup):
             ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
             ctx.train_backward()
+            ctx.adam_step()
         t0 = time.perf_counter()
         for _ in range(steps):
             loss = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
             ctx.train_backward()
+            ctx.adam_step()
+        ctx.synchronize()
         dt = (time.perf_counter() - t0) / steps
         out[name] = len(structs) / dt
         out[name + "_ms_per_step"] = dt * 1e3
