@@ -150,3 +150,34 @@ def test_two_rank_gloo_sharding():
     for rank, mine, t, tmax in out:
         assert mine == [1] * 24          # every structure owned by exactly one rank
         assert tmax >= t
+
+
+def test_xyz_round_trip_and_wrapping(tmp_path):
+    """Extended XYZ as XYZ::read / XYZ::write (format/xyz_struc.cpp): properties, energy, lattice
+    columns, forces, wrapping into the cell, and the batch packing by type names."""
+    from ann_gb300.io import XYZStructure, batch_from_xyz, read_xyz, write_xyz
+    rng = np.random.default_rng(2)
+    R = np.array([[5.0, 1.0, 0.5], [0.0, 6.0, 0.7], [0.0, 0.0, 7.0]])     # columns = lattice vectors
+    x = rng.uniform(-3.0, 12.0, (5, 3))
+    f = rng.normal(size=(5, 3))
+    s = XYZStructure(["Ar", "Ne", "Ar", "Ar", "Ne"], x, R, -12.345678, f)
+    write_xyz(tmp_path / "a.xyz", s)
+    r = read_xyz(tmp_path / "a.xyz")
+    assert r.names == s.names and abs(r.energy - s.energy) < 1e-6
+    assert np.allclose(r.cell, R, atol=1e-6) and np.allclose(r.forces, f, atol=1e-9)
+    frac = np.linalg.solve(R, r.posn.T).T
+    assert np.all(frac >= 0) and np.all(frac < 1)
+    d = np.linalg.solve(R, (r.posn - x).T).T                            # wrapped by whole cell vectors
+    assert np.allclose(d, np.round(d), atol=1e-6)
+    # header tags in any case, extra columns, no forces
+    (tmp_path / "b.xyz").write_text('2\nlattice="4 0 0 0 4 0 0 0 4" properties=species:S:1:pos:R:3:Z:I:1 Potential_Energy=-1.5\n'
+                                    "Ar 0.5 0.5 0.5 18\nAr 4.5 1.0 1.0 18\n")
+    b = read_xyz(tmp_path / "b.xyz")
+    assert b.forces is None and b.energy == -1.5 and np.allclose(b.posn[1], [0.5, 1.0, 1.0])
+
+    class Names:
+        def type_index(self, n):
+            return {"Ar": 0, "Ne": 1}[n]
+    offs, posn, types, cell = batch_from_xyz(Names(), [r, b])
+    assert list(offs) == [0, 5, 7] and list(types) == [0, 1, 0, 0, 1, 0, 0]
+    assert np.allclose(cell[0].reshape(3, 3).T, R, atol=1e-6)
