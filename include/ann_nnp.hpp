@@ -29,7 +29,7 @@ inline void check(ann_ctx* c, int rc) {
 
 class NNP {
 public:
-    explicit NNP(int device = 0, int precision = ANN_FP64) {
+    explicit NNP(int device = 0, int precision = ANN_FP64) : prec_(precision) {
         ann_options o;
         ann_default_options(&o);
         o.device = device;
@@ -72,10 +72,8 @@ private:
         for (int c = 0; c < 3; ++c) for (int r = 0; r < 3; ++r) cell[3 * c + r] = struc.R()(r, c);
         const int64_t off[2] = {0, n};
         double e = 0.0;
-        ann_options o;
-        ann_default_options(&o);
         check(nnp.ctx_, ann_compute(nnp.ctx_, 1, off, x.data(), t.data(), cell, &e, forces ? f.data() : nullptr, nullptr,
-                                    precision < 0 ? ANN_FP64 : precision));
+                                    precision < 0 ? nnp.prec_ : precision));
         if (forces) {
             for (int i = 0; i < n; ++i) for (int c = 0; c < 3; ++c) struc.force(i)[c] = f[3 * i + c];
             struc.pe() = e;
@@ -83,6 +81,7 @@ private:
         return e;
     }
     ann_ctx* ctx_ = nullptr;
+    int prec_ = ANN_FP64;   // precision of calls that do not name one
 };
 
 // ptnl::PotNNPE-shaped plugin (torch/pot_nnpe.cpp:169-288): compute() returns the energy, adds it
