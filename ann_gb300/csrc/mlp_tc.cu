@@ -218,12 +218,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
         const int at = (row < cnt) ? a.tlist[a0 + row] : -1;
         const float* Grow = a.G + (size_t)(at >= 0 ? at : 0) * a.imax;
         // ---- A0 = inpw * (G + inpb), 8-column chunks shared out over the groups
+        // rows 16-byte aligned (row length and base pointers): vector loads / stores of full chunks
+        const bool vec = (a.imax & 3) == 0 && ((reinterpret_cast<uintptr_t>(a.G) | reinterpret_cast<uintptr_t>(a.dEdG)) & 15) == 0;
         for (int c0 = grp * 8; c0 < tt.K0; c0 += 8 * TC_GROUPS) {
             float v[8];
+            if (vec && at >= 0 && c0 + 8 <= tt.nin) {
+                const float4 g0 = *reinterpret_cast<const float4*>(Grow + c0), g1 = *reinterpret_cast<const float4*>(Grow + c0 + 4);
+                const float gg[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int k = c0 + q;
-                v[q] = (at >= 0 && k < tt.nin) ? inpw[k] * (Grow[k] + inpb[k]) : 0.0f;
+                for (int q = 0; q < 8; ++q) v[q] = inpw[c0 + q] * (gg[q] + inpb[c0 + q]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int k = c0 + q;
+                    v[q] = (at >= 0 && k < tt.nin) ? inpw[k] * (Grow[k] + inpb[k]) : 0.0f;
+                }
             }
             put8(Ahi, Alo, r, c0, asbo, v);
         }
@@ -281,10 +290,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
                     put8(Ahi, Alo, r, c0 + 8, asbo, o + 8);
                 } else if (at >= 0) {
                     float* drow = a.dEdG + (size_t)at * a.imax;
+                    if (vec && c0 + 16 <= a.imax) {
+                        float o[16];
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const int col = c0 + q;
-                        if (col < a.imax) drow[col] = (col < tt.nin) ? gv[q] * inpw[col] : 0.0f;
+                        for (int q = 0; q < 16; ++q) o[q] = (c0 + q < tt.nin) ? gv[q] * inpw[c0 + q] : 0.0f;
+#pragma unroll
+                        for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4*>(drow + c0 + q) = make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            const int col = c0 + q;
+                            if (col < a.imax) drow[col] = (col < tt.nin) ? gv[q] * inpw[col] : 0.0f;
+                        }
                     }
                 }
             }
