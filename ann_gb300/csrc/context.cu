@@ -156,11 +156,6 @@ struct ann_ctx {
     int md_prec = 0;
     double md_dt = 0, md_skin = 0;
     DevBuf vel, minv, mass, disp_ref, mdflag, ke;
-    DevBuf md_snap;                 // window start state (positions, velocities, forces, reference, flags)
-    cudaGraphExec_t md_gexec = nullptr;
-    int64_t md_graph_kernels = 0;
-    int md_gkey[6] = {-1, -1, -1, -1, -1, -1};
-    uint64_t md_ggen = 0;
     std::vector<double> md_mass_t;
     double md_R[9], md_Ri[9];
     DevBuf md_R_d, md_Ri_d;
@@ -199,12 +194,7 @@ static void upload_params(ann_ctx* c, ParamSet<real>& P) {
     upload_vec<real>(P.w, h.w, c->stream); upload_vec<real>(P.wt, h.wt, c->stream); upload_vec<real>(P.b, h.b, c->stream);
     upload_vec<real>(P.inpw, h.inpw, c->stream); upload_vec<real>(P.inpb, h.inpb, c->stream);
 }
-static void reset_md_graph(ann_ctx* c) {
-    if (c->md_gexec) { cudaGraphExecDestroy(c->md_gexec); c->md_gexec = nullptr; }
-    for (int& k : c->md_gkey) k = -1;
-}
 static void reset_graph(ann_ctx* c) {
-    reset_md_graph(c);
     for (int k = 0; k < 2; ++k) {
         if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
         c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, 0};
@@ -417,17 +407,12 @@ static RedTable red_table(ann_ctx* c) {
 static bool use_tc(const ann_ctx* c) { return c->opt.mlp_backend != 1 && c->tc.ok; }
 
 template <typename real>
-static void enqueue_ef(ann_ctx* c, bool forces, bool build_list, const int32_t* gate = nullptr) {
+static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     cudaStream_t st = c->stream;
     const bool fp64 = std::is_same<real, double>::value;
     const DevPot& pot = c->plan.pot;
     mark(c, 0);
-    if (gate) {   // MD step in a graph: the list is rebuilt or refreshed as *gate decides on the device
-        NbrArgs a = nbr_args(c, c->pot.rc + c->md_skin);
-        a.gate = gate;
-        launch_neighbors(a, fp64, st);
-        launch_refresh_geometry(a, fp64, st);
-    } else if (build_list) launch_neighbors(nbr_args(c, c->pot.rc + (c->md_ready ? c->md_skin : 0.0)), fp64, st);
+    if (build_list) launch_neighbors(nbr_args(c, c->pot.rc + (c->md_ready ? c->md_skin : 0.0)), fp64, st);
     else launch_refresh_geometry(nbr_args(c, c->pot.rc + c->md_skin), fp64, st);
     check_phase(c, "neighbour list");
     mark(c, 1);
@@ -471,7 +456,10 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list, const int32_t* 
     mark(c, 6);
 }
 
-static void check_smem(ann_ctx* c, int prec) {
+static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true) {
+    if (!c->have_batch) throw ann_error(ANN_ERR_STATE, "no batch staged");
+    if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
+    ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
     // shared-memory needs of this batch (neighbour rows are staged per warp)
     const size_t need_bp = bp_smem_bytes(c->plan.pot, c->cap, prec == ANN_FP64) + 1024;
     const size_t need_mlp = mlp_smem_bytes(c->plan.pot, prec == ANN_FP64, false) + 1024;
@@ -480,13 +468,6 @@ static void check_smem(ann_ctx* c, int prec) {
                                               " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
     if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
-}
-
-static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true) {
-    if (!c->have_batch) throw ann_error(ANN_ERR_STATE, "no batch staged");
-    if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
-    ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
-    check_smem(c, prec);
     const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), g_alloc_gen.load()};
     const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
     const int gs = build_list ? 0 : 1;
@@ -601,7 +582,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
-                      &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->adam_m, &c->adam_v, &c->md_snap})
+                      &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->adam_m, &c->adam_v})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1031,8 +1012,6 @@ int ann_md_init(ann_ctx* c, int64_t natoms, const double* posn, const double* ve
         ck(cudaMemcpy(c->mass.p, mass_t, 8 * T, cudaMemcpyHostToDevice), "H2D");
         c->vel.ensure(8 * 3 * (size_t)std::max<int64_t>(natoms, 1)); c->disp_ref.ensure(8 * 3 * (size_t)std::max<int64_t>(natoms, 1));
         c->mdflag.ensure(16); c->ke.ensure(16);
-        ck(cudaMemsetAsync(c->mdflag.p, 0, 16, c->stream), "memset");
-        c->md_snap.ensure(4 * ((8 * 3 * (size_t)std::max<int64_t>(natoms, 1) + 255) / 256 * 256) + 256);
         ck(cudaMemcpy(c->vel.p, vel, 8 * 3 * (size_t)natoms, cudaMemcpyHostToDevice), "H2D");
         // initial list + forces
         run_batch(c, prec, true, true);
@@ -1042,111 +1021,6 @@ int ann_md_init(ann_ctx* c, int64_t natoms, const double* posn, const double* ve
     })
 }
 
-}  // extern "C"
-
-// MD steps per captured graph: between two windows the host checks the device status once
-constexpr int MD_WINDOW = 25;
-
-// one captured graph of K velocity-Verlet steps; the Verlet-list rebuild is decided on the device
-// (k_md stage 0 sets the flag, the list-build and refresh kernels read it)
-template <typename real>
-static void md_capture(ann_ctx* c, int K) {
-    const double half_skin2 = 0.25 * c->md_skin * c->md_skin;
-    const bool fp64 = std::is_same<real, double>::value;
-    int32_t* flag = c->mdflag.as<int32_t>();
-    cudaGraph_t g = nullptr;
-    const int64_t before = g_launch_counter;
-    ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
-    for (int k = 0; k < K; ++k) {
-        cudaMemsetAsync(flag, 0, 4, c->stream);
-        for (int stage : {0, 3}) {
-            launch_md_kick_drift(c->N, c->pos.as<double>(), c->vel.as<double>(), c->F.p, fp64, c->minv.as<double>(), c->type.as<int32_t>(),
-                                 c->md_dt, c->md_R_d.as<double>(), c->md_Ri_d.as<double>(), c->disp_ref.as<double>(), flag, half_skin2,
-                                 stage, c->stream);
-        }
-        enqueue_ef<real>(c, true, true, flag);
-        launch_md_kick_drift(c->N, c->pos.as<double>(), c->vel.as<double>(), c->F.p, fp64, c->minv.as<double>(), c->type.as<int32_t>(),
-                             c->md_dt, c->md_R_d.as<double>(), c->md_Ri_d.as<double>(), c->disp_ref.as<double>(), flag, half_skin2, 1,
-                             c->stream);
-    }
-    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-    if (ce != cudaSuccess) {
-        cudaGetLastError();
-        if (g) cudaGraphDestroy(g);
-        throw ann_error(ANN_ERR_CUDA, std::string("MD graph capture failed: ") + cudaGetErrorString(ce));
-    }
-    c->md_graph_kernels = g_launch_counter - before;
-    ck(cudaGraphInstantiate(&c->md_gexec, g, 0), "graph instantiate");
-    cudaGraphDestroy(g);
-}
-
-// window start state <-> snapshot (positions, velocities, forces, displacement reference, flags)
-static void md_snapshot(ann_ctx* c, bool restore) {
-    const size_t n3 = 3 * (size_t)c->N, rb = (c->md_prec == ANN_FP64) ? 8 : 4;
-    uint8_t* s = c->md_snap.as<uint8_t>();
-    struct Part { void* buf; size_t bytes; } parts[] = {{c->pos.p, 8 * n3}, {c->vel.p, 8 * n3}, {c->F.p, rb * n3}, {c->disp_ref.p, 8 * n3},
-                                                        {c->mdflag.p, 16}};
-    size_t off = 0;
-    for (auto& p : parts) {
-        if (restore) ck(cudaMemcpyAsync(p.buf, s + off, p.bytes, cudaMemcpyDeviceToDevice, c->stream), "restore MD state");
-        else ck(cudaMemcpyAsync(s + off, p.buf, p.bytes, cudaMemcpyDeviceToDevice, c->stream), "save MD state");
-        off += (p.bytes + 255) / 256 * 256;
-    }
-}
-
-static int md_run_graphs(ann_ctx* c, int32_t nsteps) {
-    ck(cudaMemsetAsync(c->mdflag.as<int32_t>() + 1, 0, 4, c->stream), "memset");   // rebuild counter
-    int done = 0, attempts = 0;
-    while (done < nsteps) {
-        const int K = std::min(MD_WINDOW, nsteps - done);
-        check_smem(c, c->md_prec);
-        md_snapshot(c, false);
-        const int key[6] = {K, c->N, c->cap, c->nbins_cap, c->md_prec, (int)(c->rchunk_h.size() / 3)};
-        if (!(c->md_gexec && std::equal(key, key + 6, c->md_gkey) && c->md_ggen == g_alloc_gen.load())) {
-            reset_md_graph(c);
-            if (c->md_prec == ANN_FP64) md_capture<double>(c, K); else md_capture<float>(c, K);
-            std::copy(key, key + 6, c->md_gkey);
-            c->md_ggen = g_alloc_gen.load();
-        }
-        ck(cudaGraphLaunch(c->md_gexec, c->stream), "graph launch");
-        c->kernels += c->md_graph_kernels;
-        int32_t st[8];
-        ck(cudaMemcpyAsync(st, c->status.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream), "D2H status");
-        ck(cudaStreamSynchronize(c->stream), "synchronize");
-        if (st[0] == 0) { done += K; attempts = 0; continue; }
-        if ((st[0] & ST_NBR_OVERFLOW) && !(st[0] & ~ST_NBR_OVERFLOW) && attempts < 6) {
-            // a rebuild in this window overflowed the list capacity: grow it and redo the window
-            // from its start state with a rebuild forced at its first step
-            md_snapshot(c, true);
-            const int32_t one = 1;
-            ck(cudaMemcpyAsync(c->mdflag.as<int32_t>() + 2, &one, 4, cudaMemcpyHostToDevice, c->stream), "H2D flag");
-            const int need = std::max(st[1], c->cap + 1);
-            const int ncap = ((int)(need * 1.25) + 31) / 32 * 32;
-            if (ncap > 8192) throw ann_error(ANN_ERR_CAPACITY, "more than 8192 neighbours per atom");
-            c->cap = ncap;
-            ensure_batch_buffers(c);
-            reset_graph(c);
-            ck(cudaStreamSynchronize(c->stream), "synchronize");
-            ++attempts;
-            continue;
-        }
-        if (st[0] & ST_BAD_TYPE) throw ann_error(ANN_ERR_ARG, "type index out of range");
-        if (st[0] & ST_NONFINITE) throw ann_error(ANN_ERR_NUMERIC, "non-finite position or singular cell");
-        if (st[0] & ST_IMAGE_RANGE) throw ann_error(ANN_ERR_ARG, "an atom lies more than 500 cell lengths outside its cell");
-        if (st[0] & ST_TIMEOUT) throw ann_error(ANN_ERR_TIMEOUT, "a bounded device wait gave up");
-        throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity could not be grown (status " + std::to_string(st[0]) + ")");
-    }
-    int32_t f[4];
-    ck(cudaMemcpyAsync(f, c->mdflag.p, 16, cudaMemcpyDeviceToHost, c->stream), "D2H flags");
-    ck(cudaStreamSynchronize(c->stream), "synchronize");
-    c->last_prec = c->md_prec;
-    c->have_results = true;
-    c->have_forces = true;
-    return f[1];
-}
-
-extern "C" {
 int ann_md_run(ann_ctx* c, int32_t nsteps, double* pe, double* ke, int32_t* rebuilds) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
     ANN_TRY(c, {
@@ -1155,9 +1029,7 @@ int ann_md_run(ann_ctx* c, int32_t nsteps, double* pe, double* ke, int32_t* rebu
         const bool fp64 = c->md_prec == ANN_FP64;
         const double half_skin2 = 0.25 * c->md_skin * c->md_skin;
         int reb = 0;
-        const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile && !c->debug;
-        if (graphs) reb = md_run_graphs(c, nsteps);
-        for (int step = 0; !graphs && step < nsteps; ++step) {
+        for (int step = 0; step < nsteps; ++step) {
             // first half kick + drift + wrap; flags an atom that moved more than skin/2 since the last build
             ck(cudaMemsetAsync(c->mdflag.p, 0, 4, c->stream), "memset");
             launch_md_kick_drift(c->N, c->pos.as<double>(), c->vel.as<double>(), c->F.p, fp64, c->minv.as<double>(), c->type.as<int32_t>(),
@@ -1181,7 +1053,7 @@ int ann_md_run(ann_ctx* c, int32_t nsteps, double* pe, double* ke, int32_t* rebu
                                  c->md_dt, c->md_R_d.as<double>(), c->md_Ri_d.as<double>(), c->disp_ref.as<double>(), c->mdflag.as<int32_t>(),
                                  half_skin2, 1, c->stream);
         }
-        if (!graphs) finish_batch(c);
+        finish_batch(c);
         c->md_rebuilds += reb;
         if (rebuilds) *rebuilds = reb;
         if (pe) ck(cudaMemcpy(pe, c->Es.p, 8, cudaMemcpyDeviceToHost), "D2H pe");

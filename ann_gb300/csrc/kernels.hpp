@@ -50,12 +50,7 @@ struct NbrArgs {
     int32_t* scan_tmp;               // scratch for the bin scan
     uint32_t* counter;               // [1] work counter
     int32_t* status;                 // [8]
-    // optional device-side condition (MD steps captured in one graph): the list-build kernels run
-    // only when *gate != 0, the refresh kernels only when *gate == 0; no gate: always run
-    const int32_t* gate;
 };
-__device__ __forceinline__ bool nbr_build_skipped(const NbrArgs& a) { return a.gate && *a.gate == 0; }
-__device__ __forceinline__ bool nbr_refresh_skipped(const NbrArgs& a) { return a.gate && *a.gate != 0; }
 void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st);
 // recompute nr from positions and stored images (Verlet-list refresh between rebuilds)
 void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st);
@@ -119,7 +114,7 @@ template <typename real>
 void launch_reduce_structures(int nstruc, const RedTable& t, const double* Eatom, const real* W, const real* F,
                               double* Es, double* Ws, double* Fout, cudaStream_t st);
 void launch_fill_sid(int nstruc, const int32_t* off, int32_t* sid, cudaStream_t st);
-void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st, const int32_t* gate = nullptr);
+void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st);
 size_t scan_tmp_ints(int n);
 
 // raise the dynamic shared-memory limit of a kernel to what the device allows beside its static

@@ -14,9 +14,7 @@ thread_local int64_t g_launch_counter = 0;
 // ---------------------------------------------------------------- exclusive scan (3 phases)
 constexpr int SCAN_T = 1024, SCAN_PER = 4, SCAN_BLK = SCAN_T * SCAN_PER;
 
-// gate (optional): the scan runs only when *gate != 0 (a list rebuild inside a captured MD step)
-__global__ void k_scan_blocks(const int32_t* in, int32_t* out, int n, int32_t* bsum, const int32_t* gate) {
-    if (gate && *gate == 0) return;
+__global__ void k_scan_blocks(const int32_t* in, int32_t* out, int n, int32_t* bsum) {
     __shared__ int32_t s[SCAN_T];
     const int base = blockIdx.x * SCAN_BLK + threadIdx.x * SCAN_PER;
     int32_t v[SCAN_PER];
@@ -36,8 +34,7 @@ __global__ void k_scan_blocks(const int32_t* in, int32_t* out, int n, int32_t* b
     for (int k = 0; k < SCAN_PER; ++k) { if (base + k < n) out[base + k] = run; run += v[k]; }
     if (threadIdx.x == SCAN_T - 1) bsum[blockIdx.x] = s[SCAN_T - 1];
 }
-__global__ void k_scan_sums(int32_t* bsum, int nb, const int32_t* gate) {  // single block, serial over chunks
-    if (gate && *gate == 0) return;
+__global__ void k_scan_sums(int32_t* bsum, int nb) {  // single block, serial over chunks
     __shared__ int32_t s[SCAN_T];
     int32_t carry = 0;
     for (int c0 = 0; c0 < nb; c0 += SCAN_T) {
@@ -57,8 +54,7 @@ __global__ void k_scan_sums(int32_t* bsum, int nb, const int32_t* gate) {  // si
         carry += last;
     }
 }
-__global__ void k_scan_add(int32_t* out, int n, const int32_t* bsum, const int32_t* gate) {
-    if (gate && *gate == 0) return;
+__global__ void k_scan_add(int32_t* out, int n, const int32_t* bsum) {
     const int i = blockIdx.x * SCAN_BLK + threadIdx.x;
     const int32_t add = bsum[blockIdx.x];
     for (int k = 0; k < SCAN_PER; ++k) {
@@ -67,12 +63,12 @@ __global__ void k_scan_add(int32_t* out, int n, const int32_t* bsum, const int32
     }
 }
 size_t scan_tmp_ints(int n) { return (size_t)(n + SCAN_BLK - 1) / SCAN_BLK + 1; }
-void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st, const int32_t* gate) {
+void launch_exclusive_scan(const int32_t* in, int32_t* out, int n, int32_t* tmp, cudaStream_t st) {
     if (n <= 0) return;
     const int nb = (n + SCAN_BLK - 1) / SCAN_BLK;
-    ++::ann::g_launch_counter, k_scan_blocks<<<nb, SCAN_T, 0, st>>>(in, out, n, tmp, gate);
-    ++::ann::g_launch_counter, k_scan_sums<<<1, SCAN_T, 0, st>>>(tmp, nb, gate);
-    ++::ann::g_launch_counter, k_scan_add<<<nb, SCAN_T, 0, st>>>(out, n, tmp, gate);
+    ++::ann::g_launch_counter, k_scan_blocks<<<nb, SCAN_T, 0, st>>>(in, out, n, tmp);
+    ++::ann::g_launch_counter, k_scan_sums<<<1, SCAN_T, 0, st>>>(tmp, nb);
+    ++::ann::g_launch_counter, k_scan_add<<<nb, SCAN_T, 0, st>>>(out, n, tmp);
 }
 
 // ---------------------------------------------------------------- structure of every atom

@@ -32,7 +32,6 @@ static __device__ __forceinline__ int floordiv(int a, int b) { int q = a / b; if
 // bounded by 2*natoms+1 so that the bin arrays can be sized from the atom count alone.
 constexpr int SETUP_T = 256;
 __global__ void __launch_bounds__(SETUP_T) k_struc_setup(NbrArgs a) {
-    if (nbr_build_skipped(a)) return;
     __shared__ int32_t part[SETUP_T];
     const int S = a.nstruc;
     const int per = (S + blockDim.x - 1) / blockDim.x;
@@ -87,7 +86,6 @@ __global__ void __launch_bounds__(SETUP_T) k_struc_setup(NbrArgs a) {
 
 // ---------------------------------------------------------------- atom -> bin
 __global__ void k_atom_bin(NbrArgs a) {
-    if (nbr_build_skipped(a)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.natoms) return;
     const int s = a.sid[i];
@@ -118,7 +116,6 @@ __global__ void k_atom_bin(NbrArgs a) {
 }
 
 __global__ void k_bin_scatter(NbrArgs a) {
-    if (nbr_build_skipped(a)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.natoms) return;
     a.bidx[a.bstart[a.abin[i]] + a.aslot[i]] = i;
@@ -126,7 +123,6 @@ __global__ void k_bin_scatter(NbrArgs a) {
 
 // deterministic order inside each bin (atom index), then the bin-ordered copies
 __global__ void k_bin_sort(NbrArgs a, int nbins) {
-    if (nbr_build_skipped(a)) return;
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbins) return;
     const int st = a.bstart[b], en = a.bstart[b + 1];
@@ -204,7 +200,6 @@ constexpr int MAX_RANGES = 512;   // atom ranges per centre atom in the flattene
 
 template <bool FP64>
 __global__ void __launch_bounds__(NBR_WARPS * 32) k_neighbors(NbrArgs a) {
-    if (nbr_build_skipped(a)) return;
     extern __shared__ int32_t nsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int cap = a.cap;
@@ -354,7 +349,6 @@ __global__ void __launch_bounds__(NBR_WARPS * 32) k_neighbors(NbrArgs a) {
 // Verlet-list refresh: r from current positions and the stored images
 template <bool FP64>
 __global__ void k_refresh(NbrArgs a) {
-    if (nbr_refresh_skipped(a)) return;
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.natoms) return;
@@ -393,7 +387,7 @@ void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st) {
     cudaMemsetAsync(a.bcount, 0, sizeof(int32_t) * (a.nbins_cap + 1), st);
     const int nb = (a.natoms + 255) / 256;
     if (a.natoms > 0) ++::ann::g_launch_counter, k_atom_bin<<<nb, 256, 0, st>>>(a);
-    launch_exclusive_scan(a.bcount, a.bstart, a.nbins_cap + 1, a.scan_tmp, st, a.gate);
+    launch_exclusive_scan(a.bcount, a.bstart, a.nbins_cap + 1, a.scan_tmp, st);
     if (a.natoms > 0) ++::ann::g_launch_counter, k_bin_scatter<<<nb, 256, 0, st>>>(a);
     ++::ann::g_launch_counter, k_bin_sort<<<(a.nbins_cap + 255) / 256, 256, 0, st>>>(a, a.nbins_cap);
     cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), st);
@@ -412,8 +406,7 @@ void configure_nbr(int maxsmem) {
 }
 
 // FP32 copy of the current positions (the type bits in w are kept)
-__global__ void k_pos4(int n, const double* pos, float4* pos4, const int32_t* gate) {
-    if (gate && *gate != 0) return;
+__global__ void k_pos4(int n, const double* pos, float4* pos4) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 p = pos4[i];
@@ -425,7 +418,7 @@ void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st) {
     const int threads = 256;
     const int grid = (int)(((long long)a.natoms * 32 + threads - 1) / threads);
     if (grid < 1) return;
-    if (!fp64) ++::ann::g_launch_counter, k_pos4<<<(a.natoms + 255) / 256, 256, 0, st>>>(a.natoms, a.pos, a.pos4, a.gate);
+    if (!fp64) ++::ann::g_launch_counter, k_pos4<<<(a.natoms + 255) / 256, 256, 0, st>>>(a.natoms, a.pos, a.pos4);
     if (fp64) ++::ann::g_launch_counter, k_refresh<true><<<grid, threads, 0, st>>>(a);
     else ++::ann::g_launch_counter, k_refresh<false><<<grid, threads, 0, st>>>(a);
 }

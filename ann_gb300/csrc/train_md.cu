@@ -47,28 +47,19 @@ void launch_train_loss(int nstruc, int natoms, const int32_t* off, const int32_t
     ++::ann::g_launch_counter, k_train_loss_final<<<1, 1, 0, st>>>(loss3);
 }
 
-// stage 0: v += dt/2 F/m; x += v dt; flag[0] = 1 when an atom moved more than skin/2 since the
-//          last build, or when a rebuild was requested (flag[2])
+// stage 0: v += dt/2 F/m; x += v dt; flag atoms that moved more than skin/2 since the last build
 // stage 1: v += dt/2 F/m
 // stage 2: wrap x into the cell (Cell::returnToCell)
-// stage 3: only when flag[0] is set: wrap x, make it the new displacement reference, count the
-//          rebuild in flag[1] and clear the request (the device-side rebuild decision of MD steps
-//          captured in one graph)
 template <typename real>
 __global__ void k_md(int n, double* x, double* v, const real* F, const double* minv, const int32_t* type, double dt,
                      const double* R, const double* Ri, const double* xref, int32_t* flag, double half_skin2, int stage) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (stage == 3) {
-        if (flag[0] == 0) return;
-        if (i == 0) { flag[1] += 1; flag[2] = 0; }
-    }
     if (i >= n) return;
-    if (stage == 2 || stage == 3) {
+    if (stage == 2) {
         double s[3];
         for (int d = 0; d < 3; ++d) s[d] = Ri[d] * x[3 * i] + Ri[3 + d] * x[3 * i + 1] + Ri[6 + d] * x[3 * i + 2];
         for (int d = 0; d < 3; ++d) s[d] -= floor(s[d]);
         for (int c = 0; c < 3; ++c) x[3 * i + c] = R[c] * s[0] + R[3 + c] * s[1] + R[6 + c] * s[2];
-        if (stage == 3) for (int c = 0; c < 3; ++c) const_cast<double*>(xref)[3 * i + c] = x[3 * i + c];
         return;
     }
     const double hm = 0.5 * dt * minv[type[i]];
@@ -80,7 +71,7 @@ __global__ void k_md(int n, double* x, double* v, const real* F, const double* m
             const double dd = x[3 * i + c] - xref[3 * i + c];
             d2 += dd * dd;
         }
-        if (d2 > half_skin2 || (i == 0 && flag[2] != 0)) atomicOr(flag, 1);
+        if (d2 > half_skin2) atomicOr(flag, 1);
     }
 }
 void launch_md_kick_drift(int natoms, double* pos, double* vel, const void* F, bool fp64, const double* minv, const int32_t* type,
