@@ -196,7 +196,7 @@ struct Cand {
 };
 
 constexpr int NBR_WARPS = 4;
-constexpr int MAX_RANGES = 512;   // atom ranges per centre atom in the flattened stencil walk
+constexpr int MAX_RANGES = 128;   // atom ranges per centre atom in the flattened stencil walk (else per-bin walk)
 
 template <bool FP64>
 __global__ void __launch_bounds__(NBR_WARPS * 32) k_neighbors(NbrArgs a) {
