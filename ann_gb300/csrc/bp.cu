@@ -782,7 +782,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
 #pragma unroll
             for (int q = 0; q < 9; ++q) W9[q] = warp_sum(W9[q]);
             if (lane == 0) {
-                atomicAdd(&a.F[3 * (size_t)i], fx); atomicAdd(&a.F[3 * (size_t)i + 1], fy); atomicAdd(&a.F[3 * (size_t)i + 2], fz);
+                const size_t ic = a.self ? (size_t)a.self[i] : (size_t)i;
+                atomicAdd(&a.F[3 * ic], fx); atomicAdd(&a.F[3 * ic + 1], fy); atomicAdd(&a.F[3 * ic + 2], fz);
 #pragma unroll
                 for (int q = 0; q < 9; ++q) a.W[9 * (size_t)i + q] = W9[q];
             }

@@ -71,6 +71,7 @@ struct BpArgs {
     real* W;                         // [9N] per-atom virial (force pass)
     const real* lam;                 // [3N] tangent field (jvp pass)
     real* U;                         // [N*imax] tangent of G (jvp pass)
+    const int32_t* self;             // [N] force index of each row's centre atom (NULL: the row index)
     DevParams<real> prm;
     uint32_t* counter;
     int32_t* status;
@@ -78,6 +79,26 @@ struct BpArgs {
 template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_force(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_jvp(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
+
+// ---- rows from a caller's neighbour list (extlist.cu) ----------------------------------------
+struct ListArgs {
+    int32_t nrows, nall, ntypes, cap;
+    double rc2;                      // square of the potential's cutoff: entries at or beyond it are dropped
+    int32_t hint;                    // largest row seen so far: longer rows record their length
+    const int32_t* ilist;            // [nrows] centre atom of each row (NULL: row index)
+    const int64_t* noff;             // [nrows+1] first entry of each row in neigh
+    const int32_t* neigh;            // [noff[nrows]] neighbour atoms, indices into [0, nall)
+    const double* x;                 // [3*nall] positions of local and ghost atoms
+    const int32_t* type;             // [nall]
+    int32_t* rtype;                  // [nrows] centre type of each row
+    int32_t* nn;                     // [nrows]
+    int32_t* ntc;                    // [nrows*T]
+    int32_t* nj;                     // [nrows*cap]
+    void* nr;                        // [nrows*cap] real4 (rx, ry, rz, d), r = x_centre - x_neighbour
+    int32_t* status;                 // [8]: [1] longest row on overflow, [2] longest row above hint
+};
+void launch_list_rows(const ListArgs& a, bool fp64, cudaStream_t st);
+template <typename real> void launch_to_double(size_t n, const real* in, double* out, cudaStream_t st);
 
 // ---- networks (mlp.cu) -----------------------------------------------------------------------
 template <typename real>

@@ -24,6 +24,7 @@ enum StatusBits {
     ST_BAD_TYPE = 4,        // type index out of range
     ST_TIMEOUT = 8,         // a bounded mbarrier wait gave up
     ST_NONFINITE = 16,      // non-finite position
+    ST_BAD_INDEX = 32,      // a caller's neighbour list names an atom outside [0, nall)
 };
 
 struct DevRadial {          // BasisR block (I,J)

@@ -106,6 +106,30 @@ int ann_compute(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets, const
                 double* forces /* 3N or NULL */, double* virial /* 9*nstruc or NULL */,
                 int32_t precision);
 
+/* ---- compute from the caller's neighbour list: an MD engine's domain with ghost atoms ---------
+ * The shape of LAMMPS `pair_style nn <rc>` / `pair_coeff * * <ann file> <elements>` (the
+ * reference runs it at examples/Ar/Ar_md_npt.in:22-23; that pair style's source is not part of
+ * the reference) and of NNP::compute(nnp, struc, nlist) (src/nnp/nnp.cpp:601-665), where the
+ * caller owns the neighbour list.
+ *  - nall atoms (local then ghost, as LAMMPS orders them): x[3*nall] positions, ghosts already
+ *    shifted to their image; type[nall] potential type indices (ann_type_index).
+ *  - inum rows, one per centre atom: ilist[inum] the centre atom of each row (NULL: row r is
+ *    atom r); numneigh[inum] the row lengths; neigh[] the rows back to back, atom indices in
+ *    [0, nall) (LAMMPS: firstneigh[i][k] & NEIGHMASK). The list must be FULL (every neighbour of
+ *    every centre). Entries at or beyond the potential's cutoff are ignored, so a list built with
+ *    a skin may be passed as it is.
+ *  - energy[1]: sum over the rows of the atomic energies (incl. vacuum energies); eatom[inum]
+ *    (or NULL): the energy of each row's atom, in row order.
+ *  - forces[3*nall] (or NULL) is overwritten with -dE/dx of every local AND ghost atom; with
+ *    newton_pair on the engine adds the ghost forces to their owners (LAMMPS reverse_comm).
+ *  - virial[9] (or NULL): sum over rows and entries of r[a] * v[b] as for ann_compute (LAMMPS
+ *    virial[0..5] = W[0], W[4], W[8], W[1], W[2], W[5]).
+ * Index, type or non-finite position errors return ANN_ERR_ARG / ANN_ERR_NUMERIC.                 */
+int ann_compute_list(ann_ctx* ctx, int32_t inum, const int32_t* ilist, const int32_t* numneigh,
+                     const int32_t* neigh, int32_t nall, const double* x, const int32_t* type,
+                     double* energy, double* eatom /* inum or NULL */, double* forces /* 3*nall or NULL */,
+                     double* virial /* 9 or NULL */, int32_t precision);
+
 /* ---- compute with device-resident batches -------------------------------------------------- */
 /* Stage a batch (host pointers; copied to the context's device buffers).                        */
 int ann_batch_upload(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets, const double* posn,
