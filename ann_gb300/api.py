@@ -68,6 +68,11 @@ _SIGS = {
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
     "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
     "ann_compute_list": (C.c_int, [_V, C.c_int32, _I32, _I32, _I32, C.c_int32, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_stats_reset": (C.c_int, [_V]),
+    "ann_stats_accumulate": (C.c_int, [_V]),
+    "ann_stats_get": (C.c_int, [_V, C.c_int32, _I64, _D]),
+    "ann_precondition": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_double, C.c_double]),
+    "ann_get_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_batch_upload": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D]),
     "ann_batch_set_device": (C.c_int, [_V, C.c_int32, _I64, _V, _V, _V]),
     "ann_batch_compute": (C.c_int, [_V, C.c_int32, C.c_int32]),
@@ -290,6 +295,37 @@ class Context:
         self._ck(self.lib.ann_compute_list(self.h, inum, _i32(il), _i32(nn), _i32(nb), nall, _d(x), _i32(t), _d(e), _d(ea), _d(f),
                                            _d(w), prec))
         return e[0], f, w, ea
+
+    # ---- input statistics and pre-conditioning (nnptefr2.cpp:686-858)
+    PREBIAS = {"IDENTITY": 0, "MEAN": 1, "HAR": 2, "RMS": 3, "MID": 4, "MIN": 5}
+    PRESCALE = {"IDENTITY": 0, "DEV": 1, "MINMAX": 2, "MAX": 3}
+
+    def stats_reset(self):
+        self._ck(self.lib.ann_stats_reset(self.h))
+
+    def stats_accumulate(self):
+        """Add the symmetry functions of the last computed batch to the statistics."""
+        self._ck(self.lib.ann_stats_accumulate(self.h))
+
+    def stats(self, t: int):
+        """(count, stats[6, nInput]) of type t: rows max, min, har, avg, dev, rms."""
+        n = self.num_inputs(t)
+        out = np.zeros(6 * n)
+        cnt = C.c_int64()
+        self._ck(self.lib.ann_stats_get(self.h, t, C.byref(cnt), _d(out)))
+        return cnt.value, out.reshape(6, n)
+
+    def precondition(self, prebias="MEAN", prescale="DEV", inbias=0.0, inscale=1.0):
+        pb = self.PREBIAS[prebias] if isinstance(prebias, str) else int(prebias)
+        ps = self.PRESCALE[prescale] if isinstance(prescale, str) else int(prescale)
+        self._ck(self.lib.ann_precondition(self.h, pb, ps, inbias, inscale))
+
+    def input_scaling(self, t: int):
+        """(inpw, inpb) of type t's network."""
+        n = self.num_inputs(t)
+        w, b = np.zeros(n), np.zeros(n)
+        self._ck(self.lib.ann_get_input_scaling(self.h, t, _d(w), _d(b), n))
+        return w, b
 
     def upload(self, offs, posn, types, cell):
         self._keep = [np.ascontiguousarray(offs, np.int64), np.ascontiguousarray(posn, np.float64),

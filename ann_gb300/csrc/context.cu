@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -164,6 +165,10 @@ struct ann_ctx {
     DevBuf lx, ltype, lilist, lnoff, lneigh, lrtype, lnn, lntc, lnj, lnr, lG, ldEdG, lEatom, lF, lW, lFout, ltcount, ltstart, ltlist,
         ltables, lpartial, lEs, lWs;
     int list_hint = 0;              // longest row within rc seen so far
+    // input statistics of a training set (ann_stats_*): accumulators [T][6][imax] and counts [T]
+    DevBuf st_acc, st_n, st_part, st_pcount;
+    bool st_ready = false;
+    int st_T = 0, st_imax = 0;
     // instrumentation
     int64_t kernels = 0;            // kernels launched (graph replays add graph_kernels)
     int64_t graph_kernels[2] = {0, 0};
@@ -597,7 +602,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->adam_m, &c->adam_v,
                       &c->lx, &c->ltype, &c->lilist, &c->lnoff, &c->lneigh, &c->lrtype, &c->lnn, &c->lntc, &c->lnj, &c->lnr, &c->lG,
                       &c->ldEdG, &c->lEatom, &c->lF, &c->lW, &c->lFout, &c->ltcount, &c->ltstart, &c->ltlist, &c->ltables, &c->lpartial,
-                      &c->lEs, &c->lWs})
+                      &c->lEs, &c->lWs, &c->st_acc, &c->st_n, &c->st_part, &c->st_pcount})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -620,6 +625,7 @@ int ann_load_potential_text(ann_ctx* c, const char* text) {
         p.validate();
         c->pot = p;
         c->adam_ready = false;
+        c->st_ready = false;   // statistics belong to the previous potential's inputs
         rebuild_plan(c);
     })
 }
@@ -933,6 +939,128 @@ int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32
         if (virial) ck(cudaMemcpyAsync(virial, c->lWs.p, sizeof(double) * 9, cudaMemcpyDeviceToHost, st), "D2H virial");
         ck(cudaStreamSynchronize(st), "synchronize");
     })
+}
+
+// ---- input statistics and pre-conditioning of a training set (nnptefr2.cpp:686-858)
+static void stats_reset(ann_ctx* c) {
+    const int T = c->pot.ntypes(), imax = std::max(c->pot.max_input(), 1);
+    std::vector<double> a((size_t)T * 6 * imax, 0.0);
+    for (int t = 0; t < T; ++t)
+        for (int k = 0; k < imax; ++k) { a[((size_t)t * 6) * imax + k] = -DBL_MAX; a[((size_t)t * 6 + 1) * imax + k] = DBL_MAX; }
+    c->st_acc.ensure(8 * a.size()); c->st_n.ensure(8 * (size_t)std::max(T, 1));
+    ck(cudaMemcpyAsync(c->st_acc.p, a.data(), 8 * a.size(), cudaMemcpyHostToDevice, c->stream), "H2D statistics");
+    ck(cudaMemsetAsync(c->st_n.p, 0, 8 * (size_t)std::max(T, 1), c->stream), "memset statistics");
+    ck(cudaStreamSynchronize(c->stream), "synchronize");
+    c->st_ready = true; c->st_T = T; c->st_imax = imax;
+}
+// host form of one type's statistics: rows max, min, har, avg, dev, rms of its n inputs
+static std::vector<double> stats_host(ann_ctx* c, int t, int64_t* count) {
+    const int imax = c->st_imax, n = c->pot.sp[t].nInput;
+    std::vector<double> a((size_t)6 * imax), out((size_t)6 * n);
+    double N = 0.0;
+    ck(cudaMemcpyAsync(a.data(), c->st_acc.as<double>() + (size_t)t * 6 * imax, 8 * a.size(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    ck(cudaMemcpyAsync(&N, c->st_n.as<double>() + t, 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    ck(cudaStreamSynchronize(c->stream), "synchronize");
+    for (int k = 0; k < n; ++k) {
+        out[k] = a[k];
+        out[n + k] = a[imax + k];
+        out[2 * n + k] = N / a[2 * imax + k];
+        out[3 * n + k] = a[3 * imax + k] / N;
+        out[4 * n + k] = N > 1.0 ? std::sqrt(a[4 * imax + k] / (N - 1.0)) : 0.0;
+        out[5 * n + k] = std::sqrt(a[5 * imax + k] / N);
+    }
+    if (count) *count = (int64_t)N;
+    return out;
+}
+
+int ann_stats_reset(ann_ctx* c) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    ANN_TRY(c, { set_device(c); stats_reset(c); })
+}
+int ann_stats_accumulate(ann_ctx* c) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->have_results) throw ann_error(ANN_ERR_STATE, "no computed batch");
+        finish_batch(c);   // a batch still in flight (ann_batch_compute) completes, list overflows recomputed
+        if (!c->st_ready || c->st_T != c->pot.ntypes() || c->st_imax != std::max(c->pot.max_input(), 1)) stats_reset(c);
+        const int T = c->pot.ntypes(), imax = c->pot.max_input(), maxch = stats_chunks_per_type(c->N);
+        if (c->N > 0 && imax > 0) {
+            c->st_part.ensure(8 * (size_t)T * maxch * 6 * imax); c->st_pcount.ensure(4 * (size_t)T * maxch);
+            const int64_t before = g_launch_counter;
+            if (c->last_prec == ANN_FP64)
+                launch_input_stats<double>(c->N, T, imax, c->G.as<double>(), c->tstart.as<int32_t>(), c->tlist.as<int32_t>(),
+                                           c->st_part.as<double>(), c->st_pcount.as<int32_t>(), c->st_acc.as<double>(), c->st_n.as<double>(), c->stream);
+            else
+                launch_input_stats<float>(c->N, T, imax, c->G.as<float>(), c->tstart.as<int32_t>(), c->tlist.as<int32_t>(),
+                                          c->st_part.as<double>(), c->st_pcount.as<int32_t>(), c->st_acc.as<double>(), c->st_n.as<double>(), c->stream);
+            c->kernels += g_launch_counter - before;
+            ck(cudaGetLastError(), "statistics kernels");
+        }
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+    })
+}
+int ann_stats_get(ann_ctx* c, int32_t t, int64_t* count, double* stats) {
+    if (!c || !stats) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->st_ready || c->st_T != c->pot.ntypes()) throw ann_error(ANN_ERR_STATE, "no statistics accumulated");
+        const std::vector<double> h = stats_host(c, t, count);
+        std::copy(h.begin(), h.end(), stats);
+    })
+}
+int ann_precondition(ann_ctx* c, int32_t prebias, int32_t prescale, double inbias, double inscale) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (prebias < ANN_PREBIAS_IDENTITY || prebias > ANN_PREBIAS_MIN) return fail(c, ANN_ERR_ARG, "Invalid input bias.");
+    if (prescale < ANN_PRESCALE_IDENTITY || prescale > ANN_PRESCALE_MAX) return fail(c, ANN_ERR_ARG, "Invalid input scaling.");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->st_ready || c->st_T != c->pot.ntypes()) throw ann_error(ANN_ERR_STATE, "no statistics accumulated");
+        sync_params_from_device(c);
+        for (int t = 0; t < c->pot.ntypes(); ++t) {
+            int64_t N = 0;
+            const std::vector<double> h = stats_host(c, t, &N);
+            if (N == 0) continue;   // a type without atoms keeps its scaling
+            const int n = c->pot.sp[t].nInput;
+            const double *mx = h.data(), *mn = mx + n, *har = mx + 2 * n, *avg = mx + 3 * n, *dev = mx + 4 * n, *rms = mx + 5 * n;
+            auto& nn = c->pot.sp[t].nn;
+            for (int k = 0; k < n; ++k) {
+                double b = 0.0, w = 1.0;
+                switch (prebias) {
+                    case ANN_PREBIAS_MEAN: b = -1.0 * avg[k]; break;
+                    case ANN_PREBIAS_HAR: b = -1.0 * har[k]; break;
+                    case ANN_PREBIAS_RMS: b = -1.0 * rms[k]; break;
+                    case ANN_PREBIAS_MID: b = -0.5 * (mx[k] + mn[k]); break;
+                    case ANN_PREBIAS_MIN: b = -1.0 * mn[k]; break;
+                    default: b = 0.0; break;
+                }
+                switch (prescale) {
+                    case ANN_PRESCALE_DEV: w = (dev[k] == 0) ? 1.0 : 1.0 / dev[k]; break;
+                    case ANN_PRESCALE_MINMAX: { const double s = mx[k] - mn[k]; w = (s > 0) ? 1.0 / s : 1.0; } break;
+                    case ANN_PRESCALE_MAX: w = (mx[k] > 0) ? 1.0 / mx[k] : 1.0; break;
+                    default: w = 1.0; break;
+                }
+                nn.inpb[k] = b + inbias;
+                nn.inpw[k] = w * inscale;
+            }
+            nn.outb.assign(nn.outb.size(), 0.0);
+            nn.outw.assign(nn.outw.size(), 1.0);
+        }
+        rebuild_plan(c);
+    })
+}
+int ann_get_input_scaling(ann_ctx* c, int32_t t, double* w, double* b, int32_t n) {
+    if (!c || !w || !b) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    if (n != c->pot.sp[t].nInput) return fail(c, ANN_ERR_ARG, "input count mismatch");
+    std::copy(c->pot.sp[t].nn.inpw.begin(), c->pot.sp[t].nn.inpw.end(), w);
+    std::copy(c->pot.sp[t].nn.inpb.begin(), c->pot.sp[t].nn.inpb.end(), b);
+    return ANN_OK;
 }
 
 // ---- inspection

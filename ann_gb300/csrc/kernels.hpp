@@ -100,6 +100,12 @@ struct ListArgs {
 void launch_list_rows(const ListArgs& a, bool fp64, cudaStream_t st);
 template <typename real> void launch_to_double(size_t n, const real* in, double* out, cudaStream_t st);
 
+// ---- input statistics of a training set (stats.cu) -------------------------------------------
+int stats_chunks_per_type(int natoms);
+template <typename real>
+void launch_input_stats(int natoms, int ntypes, int imax, const real* G, const int32_t* tstart, const int32_t* tlist, double* part,
+                        int32_t* pcount, double* acc, double* accn, cudaStream_t st);
+
 // ---- networks (mlp.cu) -----------------------------------------------------------------------
 template <typename real>
 struct MlpArgs {

@@ -191,6 +191,28 @@ int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t npar
 int ann_adam_init(ann_ctx* ctx, double lr, double beta1, double beta2, double eps);
 int ann_adam_step(ann_ctx* ctx, double scale);
 
+/* ---- input statistics and pre-conditioning of a training set (nnptefr2.cpp:686-858) ----------
+ * The trainer's set-up: statistics of every input over all atoms of each type in the training
+ * set, then inpb / inpw of each network from them. Accumulated on the device batch by batch:
+ * ann_stats_accumulate adds the symmetry functions of the last computed batch (ann_compute,
+ * ann_batch_compute or ann_train_forward; in that call's precision, FP64 to match the reference).
+ * ann_stats_get gives, for type t, count = atoms accumulated and stats[6 * nInput(t)] = rows max,
+ * min, harmonic mean N/sum(1/G), mean, standard deviation (N-1 normalised; 0 for N < 2) and rms.
+ * ann_precondition sets, for every type with atoms, inpb = bias(prebias) + inbias and
+ * inpw = scale(prescale) * inscale, and outb = 0, outw = 1, as the trainer does. Enum values are
+ * those of PreBias / PreScale (nnptefr2.hpp:59-97).                                              */
+enum ann_prebias {
+    ANN_PREBIAS_IDENTITY = 0, ANN_PREBIAS_MEAN = 1, ANN_PREBIAS_HAR = 2, ANN_PREBIAS_RMS = 3, ANN_PREBIAS_MID = 4,
+    ANN_PREBIAS_MIN = 5
+};
+enum ann_prescale { ANN_PRESCALE_IDENTITY = 0, ANN_PRESCALE_DEV = 1, ANN_PRESCALE_MINMAX = 2, ANN_PRESCALE_MAX = 3 };
+int ann_stats_reset(ann_ctx* ctx);
+int ann_stats_accumulate(ann_ctx* ctx);
+int ann_stats_get(ann_ctx* ctx, int32_t type, int64_t* count, double* stats);
+int ann_precondition(ann_ctx* ctx, int32_t prebias, int32_t prescale, double inbias, double inscale);
+/* the input scaling of type t's network (inpw, inpb; n = nInput(t))                               */
+int ann_get_input_scaling(ann_ctx* ctx, int32_t type, double* w, double* b, int32_t n);
+
 /* ---- molecular dynamics: velocity Verlet (integrator.cpp:177-200) --------------------------- */
 /* One structure; masses per type in Dalton. list_skin adds to rc for the Verlet list; the list is
  * rebuilt when an atom has moved more than skin/2 since the last build.                          */

@@ -22,6 +22,7 @@
 // The canonical arithmetic (no fused multiply-add, fixed association) is shared with the GPU
 // FP64 path so that the two lists agree bit for bit.
 // ============================================================================================
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <climits>
@@ -1223,6 +1224,89 @@ int orc_md_step(void* pp, int N, double* x, double* v, const int* type, const do
         *ke = 0.5 * k * mvv;
         return 0;
     } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+// Input statistics of a training set (nnptefr2.cpp:686-775), per type t over its N_t atoms and per
+// input k: max, min, harmonic mean N/sum(1/G), mean, standard deviation sqrt(sum (mean-G)^2 /
+// (N-1)) and rms sqrt(sum G^2 / N), each a separate pass over the atoms as in the reference.
+// G is natoms x imax (the first nin[t] entries of a row are the atom's inputs).
+// out[t * 6 * imax + q * imax + k] for q = max, min, har, avg, dev, rms; count[t] = N_t.
+// Deviation kept from the reference: a type with fewer than two atoms gets dev = 0 (the
+// reference divides by N-1 = 0).
+void orc_input_stats(int ntypes, const int* nin, long long natoms, const int* type, const double* G, int imax, double* out,
+                     long long* count) {
+    for (int t = 0; t < ntypes; ++t) {
+        double* o = out + (size_t)t * 6 * imax;
+        for (int k = 0; k < 6 * imax; ++k) o[k] = 0.0;
+        for (int k = 0; k < nin[t]; ++k) { o[k] = -DBL_MAX; o[imax + k] = DBL_MAX; }
+        count[t] = 0;
+    }
+    for (long long i = 0; i < natoms; ++i) ++count[type[i]];
+    for (long long i = 0; i < natoms; ++i) {                       // max / min (702-713)
+        double* o = out + (size_t)type[i] * 6 * imax;
+        for (int k = 0; k < nin[type[i]]; ++k) {
+            const double g = G[i * imax + k];
+            if (g > o[k]) o[k] = g;
+            if (g < o[imax + k]) o[imax + k] = g;
+        }
+    }
+    for (long long i = 0; i < natoms; ++i) {                       // harmonic mean (720-730)
+        double* o = out + (size_t)type[i] * 6 * imax;
+        for (int k = 0; k < nin[type[i]]; ++k) o[2 * imax + k] += 1.0 / G[i * imax + k];
+    }
+    for (long long i = 0; i < natoms; ++i) {                       // mean (732-740)
+        double* o = out + (size_t)type[i] * 6 * imax;
+        for (int k = 0; k < nin[type[i]]; ++k) o[3 * imax + k] += G[i * imax + k];
+    }
+    for (int t = 0; t < ntypes; ++t) {
+        double* o = out + (size_t)t * 6 * imax;
+        for (int k = 0; k < nin[t]; ++k) { o[2 * imax + k] = count[t] / o[2 * imax + k]; o[3 * imax + k] /= count[t]; }
+    }
+    for (long long i = 0; i < natoms; ++i) {                       // deviation (742-754), rms (756-766)
+        double* o = out + (size_t)type[i] * 6 * imax;
+        for (int k = 0; k < nin[type[i]]; ++k) {
+            const double d = o[3 * imax + k] - G[i * imax + k];
+            o[4 * imax + k] += d * d;
+            o[5 * imax + k] += G[i * imax + k] * G[i * imax + k];
+        }
+    }
+    for (int t = 0; t < ntypes; ++t) {
+        double* o = out + (size_t)t * 6 * imax;
+        for (int k = 0; k < nin[t]; ++k) {
+            o[4 * imax + k] = count[t] > 1 ? std::sqrt(o[4 * imax + k] / (count[t] - 1.0)) : 0.0;
+            o[5 * imax + k] = std::sqrt(o[5 * imax + k] / count[t]);
+        }
+    }
+}
+
+// Input pre-conditioning from those statistics (nnptefr2.cpp:777-858): inpb by PreBias
+// (0 IDENTITY, 1 MEAN, 2 HAR, 3 RMS, 4 MID, 5 MIN; nnptefr2.hpp:87-97) plus inbias, inpw by PreScale
+// (0 IDENTITY, 1 DEV, 2 MINMAX, 3 MAX; nnptefr2.hpp:59-67) times inscale. Returns 1 for an enum value
+// outside those (the reference's "Invalid input bias." / "Invalid input scaling.").
+int orc_precondition(int n, const double* st /* 6 x n rows of one type, row stride imax */, int imax, int prebias,
+                     int prescale, double inbias, double inscale, double* inpb, double* inpw) {
+    const double *mx = st, *mn = st + imax, *har = st + 2 * imax, *avg = st + 3 * imax, *dev = st + 4 * imax, *rms = st + 5 * imax;
+    for (int k = 0; k < n; ++k) {
+        switch (prebias) {
+            case 0: inpb[k] = 0.0; break;
+            case 1: inpb[k] = -1.0 * avg[k]; break;
+            case 2: inpb[k] = -1.0 * har[k]; break;
+            case 3: inpb[k] = -1.0 * rms[k]; break;
+            case 4: inpb[k] = -0.5 * (mx[k] + mn[k]); break;
+            case 5: inpb[k] = -1.0 * mn[k]; break;
+            default: g_err = "Invalid input bias."; return 1;
+        }
+        inpb[k] += inbias;
+        switch (prescale) {
+            case 0: inpw[k] = 1.0; break;
+            case 1: inpw[k] = (dev[k] == 0) ? 1.0 : 1.0 / dev[k]; break;
+            case 2: { const double s = mx[k] - mn[k]; inpw[k] = (s > 0) ? 1.0 / s : 1.0; } break;
+            case 3: inpw[k] = (mx[k] > 0) ? 1.0 / mx[k] : 1.0; break;
+            default: g_err = "Invalid input scaling."; return 1;
+        }
+        inpw[k] *= inscale;
+    }
+    return 0;
 }
 
 }  // extern "C"

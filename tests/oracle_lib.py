@@ -73,6 +73,9 @@ class Oracle:
         L.orc_lj.restype = C.c_double
         L.orc_lj.argtypes = [C.c_int, _D, _D, C.c_double, C.c_double, C.c_double, _D]
         L.orc_md_step.argtypes = [C.c_void_p, C.c_int, _D, _D, _I, _D, _D, C.c_double, _D, _D, _D]
+        L.orc_input_stats.restype = None
+        L.orc_input_stats.argtypes = [C.c_int, _I, C.c_longlong, _I, _D, C.c_int, _D, C.POINTER(C.c_longlong)]
+        L.orc_precondition.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _D, _D]
 
     def err(self):
         return self.L.orc_last_error().decode()
@@ -104,6 +107,25 @@ class Oracle:
             if k >= 0:
                 return i[:k], j[:k], img[:3 * k].reshape(-1, 3), r[:3 * k].reshape(-1, 3), d[:k]
             cap = -k
+
+    def input_stats(self, nin, types, G):
+        """Per-type input statistics (nnptefr2.cpp:686-775): (stats[T, 6, imax] with rows max, min,
+        har, avg, dev, rms; counts[T])."""
+        G = np.ascontiguousarray(G, np.float64)
+        T, imax = len(nin), G.shape[1]
+        out = np.zeros((T, 6, imax))
+        cnt = np.zeros(T, np.int64)
+        self.L.orc_input_stats(T, _i(np.ascontiguousarray(nin, np.int32)), len(types), _i(np.ascontiguousarray(types, np.int32)),
+                               _d(G), imax, _d(out), cnt.ctypes.data_as(C.POINTER(C.c_longlong)))
+        return out, cnt
+
+    def precondition(self, stats_t, n, prebias, prescale, inbias=0.0, inscale=1.0):
+        """(inpb, inpw) of one type from its statistics (nnptefr2.cpp:777-858)."""
+        st = np.ascontiguousarray(stats_t, np.float64)
+        b, w = np.zeros(n), np.zeros(n)
+        if self.L.orc_precondition(n, _d(st), st.shape[1], prebias, prescale, inbias, inscale, _d(b), _d(w)) != 0:
+            raise ValueError(self.err())
+        return b, w
 
     def lj(self, x, R, eps=0.0104, sig=3.4, rcut=8.5):
         x = np.ascontiguousarray(x, np.float64)
