@@ -164,3 +164,48 @@ def tiny_cells():
 
 def batch(structs):
     return pack_batch(structs)
+
+
+# ---- the reference's argon example (examples/Ar): basis_Ar restated in the current file format
+AR_RS = [0.00, 0.16, 0.31, 0.47, 0.63, 0.78, 0.94, 1.10, 1.25, 1.41]
+AR_ETA = [0.016, 0.032, 0.054, 0.084, 0.126, 0.190, 0.287, 0.455, 0.760, 1.400]
+AR_AETA = [0.120, 0.060, 0.030]
+
+
+def argon_example_potential(rc=8.0, nodes=(7, 4, 2, 1), neuron="TANH", evac=-574.641, seed=3, sigma_w=0.5):
+    """The example's argon potential: examples/Ar/basis_Ar (10 radial G2 (rs, eta), 3 angular G4
+    (eta, zeta 5, lambda -1)) written in the current 'ann' format (BasisR GAUSSIAN takes
+    exp(-(eta'(r-rs))^2), so eta' = sqrt(eta); BasisA GAUSS takes exp(-(rij^2+rik^2)/eta'^2), so
+    eta' = 1/sqrt(eta)); nh 7 4 2 and the vacuum energy of nn_pot_train_init.txt; XAVIER normal
+    weights. rc is 8 A rather than the example's 10 A: the FP64 rows of the densest training cell
+    at 10 A exceed a block's shared memory."""
+    nin = len(AR_RS) + len(AR_AETA)
+    out = ["ann", "ntypes 1", f"name Ar mass 39.948000 energy {evac:f} ", f"rc {rc:f}", "basis Ar", "basis_radial Ar",
+           f"BasisR COS {rc:f} GAUSSIAN {len(AR_RS)}"]
+    out += [f"\t{r:f} {np.sqrt(e):f}" for r, e in zip(AR_RS, AR_ETA)]
+    out += ["basis_angular Ar Ar", f"BasisA COS {rc:f} GAUSS {len(AR_AETA)}"]
+    out += [f"\t{1 / np.sqrt(e):f} 5.000000 -1 0" for e in AR_AETA]
+    out += ["nn Ar", "nn " + " ".join(map(str, [nin] + list(nodes))) + " ", f"neuron {neuron} 1.000000",
+            "inpw " + " ".join(["1.000000000000000"] * nin) + " ", "outw 1.000000000000000 ",
+            "inpb " + " ".join(["0.000000000000000"] * nin) + " ", "outb 0.000000000000000 "]
+    prev = nin
+    for l, n in enumerate(nodes):
+        out.append(f"bias[{l + 1}] " + " ".join(["0.0"] * n) + " ")
+    for l, n in enumerate(nodes):
+        out.append(f"weight[{l},{l + 1}] " + " ".join(["0.0"] * (n * prev)) + " ")
+        prev = n
+    text = "\n".join(out) + "\n"
+    return W.set_network_text(text, [W.xavier_network(seed, nin, list(nodes), 0.001, sigma_w)], nin, list(nodes))
+
+
+def argon_example_data():
+    """(train, val) batches of the fixture built from the example's QE outputs:
+    each (offs, posn, types, cell, energies, forces)."""
+    from pathlib import Path
+    d = np.load(Path(__file__).resolve().parent / "golden" / "ar_qe.npz")
+    out = []
+    for k in ("train", "val"):
+        X, C = d[k + "_posn"], d[k + "_cell"]
+        b = pack_batch([(X[s], np.zeros(X.shape[1], np.int32), C[s]) for s in range(len(X))])
+        out.append((*b, d[k + "_energy"], d[k + "_forces"].reshape(-1, 3)))
+    return out
