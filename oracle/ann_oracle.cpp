@@ -31,6 +31,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <random>
 #include <vector>
 #include <map>
 #include <thread>
@@ -1307,6 +1308,88 @@ int orc_precondition(int n, const double* st /* 6 x n rows of one type, row stri
         inpw[k] *= inscale;
     }
     return 0;
+}
+
+// Taylor-perturbed copies of structures with forces (nnptefr2.cpp:2409-2479): every structure is
+// kept; one whose mean |F| exceeds 1e-12 gets nadd copies in which each atom j moves by
+// dr = vr (sin t cos p, sin t sin p, cos t), cos t and p/pi uniform in [-1, 1)
+// (std::uniform_real_distribution), vr from the radial distribution rdist with scale rdelta
+// (rand/rng.cpp:64-146: 1 UNIFORM, 2 LAPLACE, 3 NORMAL, 5 SECH, 6 LOGISTIC, 7 COSINE) times
+// rcov[j] when given (Perturb::COVALENT), and the energy becomes E - sum_j dr_j . F_j. Draws come
+// from one std::mt19937(seed) in the order vr, cos t, p per atom. Writes the new structures'
+// atom offsets, positions, energies and source structure when the output pointers are not NULL;
+// returns the number of structures (-1 for an unknown distribution).
+long long orc_taylor_perturb(int nstruc, const long long* off, const double* x, const double* F, const double* E, int nadd, int rdist,
+                             double rdelta, unsigned seed, const double* rcov, long long* out_off, double* out_x, double* out_E,
+                             int* out_src) {
+    const double PI = 3.14159265358979323846;
+    std::mt19937 gen(seed);
+    const double gmax = (double)gen.max();
+    std::uniform_real_distribution<double> dista(-1.0, 1.0);
+    int ncache = 0;
+    double cache_y = 0.0;
+    auto unit_nonzero = [&]() { double p = 0; while (p == 0) p = (double)gen() / gmax; return p; };
+    auto radial = [&]() -> double {
+        switch (rdist) {
+            case 1: return (double)gen() / gmax * rdelta;
+            case 2: { double p = unit_nonzero() - 0.5; const double s = (p > 0) - (p < 0); return -1.0 * rdelta * s * std::log(1.0 - 2.0 * std::fabs(p)); }
+            case 3: {
+                if (ncache++ % 2 == 0) {
+                    const double r1 = unit_nonzero(), r2 = (double)gen() / gmax;
+                    const double mag = rdelta * std::sqrt(-2.0 * std::log(r1)), ang = 2.0 * PI * r2;
+                    cache_y = mag * std::sin(ang);
+                    return mag * std::cos(ang);
+                }
+                return cache_y;
+            }
+            case 5: { const double p = unit_nonzero(); return rdelta * 2.0 / PI * std::log(std::tan(0.5 * PI * p)); }
+            case 6: { const double p = unit_nonzero(); return rdelta * std::log(p / (1.0 - p)); }
+            case 7: {
+                const double p = unit_nonzero();
+                if (p < 0.5) { const double t = std::sqrt(-2.0 * std::log(p)); return rdelta * (0.820251 - 0.806770 * t + 0.093247 * t * t); }
+                const double t = std::sqrt(-2.0 * std::log(1.0 - p));
+                return -rdelta * (0.820251 - 0.806770 * t + 0.093247 * t * t);
+            }
+        }
+        return NAN;
+    };
+    if (rdist != 1 && rdist != 2 && rdist != 3 && rdist != 5 && rdist != 6 && rdist != 7) return -1;
+    long long ns = 0, na = 0;
+    auto emit = [&](int s, const double* xs, double e) {
+        const long long n = off[s + 1] - off[s];
+        if (out_off) { out_off[ns] = na; out_off[ns + 1] = na + n; }
+        if (out_x) std::memcpy(out_x + 3 * na, xs, sizeof(double) * 3 * n);
+        if (out_E) out_E[ns] = e;
+        if (out_src) out_src[ns] = s;
+        ++ns; na += n;
+    };
+    std::vector<double> xp;
+    for (int s = 0; s < nstruc; ++s) {
+        const long long a0 = off[s], n = off[s + 1] - off[s];
+        emit(s, x + 3 * a0, E[s]);
+        double favg = 0;
+        for (long long j = 0; j < n; ++j) {
+            const double* f = F + 3 * (a0 + j);
+            favg += std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+        }
+        favg /= n;
+        if (!(favg > 1.0e-12)) continue;
+        for (int m = 0; m < nadd; ++m) {
+            xp.assign(x + 3 * a0, x + 3 * (a0 + n));
+            double e = E[s];
+            for (long long j = 0; j < n; ++j) {
+                double vr = radial();
+                if (rcov) vr *= rcov[a0 + j];
+                const double ct = dista(gen), st = std::sqrt(1.0 - ct * ct), ph = dista(gen) * PI;
+                const double dr[3] = {vr * st * std::cos(ph), vr * st * std::sin(ph), vr * ct};
+                const double* f = F + 3 * (a0 + j);
+                for (int c = 0; c < 3; ++c) xp[3 * j + c] += dr[c];
+                e -= dr[0] * f[0] + dr[1] * f[1] + dr[2] * f[2];
+            }
+            emit(s, xp.data(), e);
+        }
+    }
+    return ns;
 }
 
 }  // extern "C"

@@ -76,6 +76,8 @@ class Oracle:
         L.orc_input_stats.restype = None
         L.orc_input_stats.argtypes = [C.c_int, _I, C.c_longlong, _I, _D, C.c_int, _D, C.POINTER(C.c_longlong)]
         L.orc_precondition.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _D, _D]
+        L.orc_taylor_perturb.restype = C.c_longlong
+        L.orc_taylor_perturb.argtypes = [C.c_int, _L, _D, _D, _D, C.c_int, C.c_int, C.c_double, C.c_uint, _D, _L, _D, _D, _I]
 
     def err(self):
         return self.L.orc_last_error().decode()
@@ -126,6 +128,23 @@ class Oracle:
         if self.L.orc_precondition(n, _d(st), st.shape[1], prebias, prescale, inbias, inscale, _d(b), _d(w)) != 0:
             raise ValueError(self.err())
         return b, w
+
+    def taylor_perturb(self, offs, posn, forces, energy, nadd, dist, rdelta, seed, rcov=None):
+        """Perturbed training set (nnptefr2.cpp:2409-2479) with std::mt19937: (offs, posn, energy, src)."""
+        offs = np.ascontiguousarray(offs, np.int64)
+        x = np.ascontiguousarray(posn, np.float64)
+        f = np.ascontiguousarray(forces, np.float64)
+        e = np.ascontiguousarray(energy, np.float64)
+        rc = None if rcov is None else np.ascontiguousarray(rcov, np.float64)
+        args = (len(offs) - 1, _l(offs), _d(x), _d(f), _d(e), nadd, dist, rdelta, seed, _d(rc))
+        ns = self.L.orc_taylor_perturb(*args, None, None, None, None)
+        if ns < 0:
+            raise ValueError("Invalid position distribution.")
+        o = np.zeros(ns + 1, np.int64)
+        self.L.orc_taylor_perturb(*args, _l(o), None, None, None)
+        X = np.zeros((int(o[-1]), 3)); E = np.zeros(ns); S = np.zeros(ns, np.int32)
+        self.L.orc_taylor_perturb(*args, _l(o), _d(X), _d(E), _i(S))
+        return o, X, E, S
 
     def lj(self, x, R, eps=0.0104, sig=3.4, rcut=8.5):
         x = np.ascontiguousarray(x, np.float64)
