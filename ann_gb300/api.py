@@ -67,7 +67,7 @@ _SIGS = {
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
     "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
-    "ann_compute_list": (C.c_int, [_V, C.c_int32, _I32, _I32, _I32, C.c_int32, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_compute_list": (C.c_int, [_V, C.c_int32, _I32, _I32, _I32, C.c_int32, _D, _I32, _D, _D, _D, _D, C.c_int32, C.c_int32]),
     "ann_stats_reset": (C.c_int, [_V]),
     "ann_stats_accumulate": (C.c_int, [_V]),
     "ann_stats_get": (C.c_int, [_V, C.c_int32, _I64, _D]),
@@ -277,23 +277,27 @@ class Context:
                                       _d(e), _d(f), _d(w), prec))
         return e, f, w
 
-    def compute_list(self, x, types, numneigh, neigh, ilist=None, forces=True, virial=True, eatom=False, precision=None):
+    def compute_list(self, x, types, numneigh, neigh, ilist=None, forces=True, virial=True, eatom=False, precision=None,
+                     keep=False, inum=None):
         """E (+F of all nall atoms, virial, per-row energies) from a full neighbour list over local and
-        ghost atoms (the LAMMPS pair style shape, ann_compute_list). Returns (energy, forces[nall,3]
-        or None, virial[3,3] or None, eatom[inum] or None)."""
+        ghost atoms (the LAMMPS pair style shape, ann_compute_list). keep=True reuses the list, ilist
+        and types of the previous call (ANN_LIST_KEEP; types / numneigh / neigh may be None and inum
+        must then be given). Returns (energy, forces[nall,3] or None, virial[3,3] or None,
+        eatom[inum] or None)."""
         prec = self.precision if precision is None else precision
         x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
-        t = np.ascontiguousarray(types, np.int32)
-        nn = np.ascontiguousarray(numneigh, np.int32)
-        nb = np.ascontiguousarray(neigh, np.int32)
+        t = None if types is None else np.ascontiguousarray(types, np.int32)
+        nn = None if numneigh is None else np.ascontiguousarray(numneigh, np.int32)
+        nb = None if neigh is None else np.ascontiguousarray(neigh, np.int32)
         il = None if ilist is None else np.ascontiguousarray(ilist, np.int32)
-        nall, inum = len(x), len(nn)
+        nall = len(x)
+        inum = len(nn) if inum is None else int(inum)
         e = np.zeros(1)
         f = np.zeros((nall, 3)) if forces else None
         w = np.zeros((3, 3)) if virial else None
         ea = np.zeros(inum) if eatom else None
         self._ck(self.lib.ann_compute_list(self.h, inum, _i32(il), _i32(nn), _i32(nb), nall, _d(x), _i32(t), _d(e), _d(ea), _d(f),
-                                           _d(w), prec))
+                                           _d(w), prec, 1 if keep else 0))
         return e[0], f, w, ea
 
     # ---- input statistics and pre-conditioning (nnptefr2.cpp:686-858)

@@ -165,6 +165,8 @@ struct ann_ctx {
     DevBuf lx, ltype, lilist, lnoff, lneigh, lrtype, lnn, lntc, lnj, lnr, lG, ldEdG, lEatom, lF, lW, lFout, ltcount, ltstart, ltlist,
         ltables, lpartial, lEs, lWs;
     int list_hint = 0;              // longest row within rc seen so far
+    bool list_staged = false, list_have_ilist = false;   // a list on the device that ANN_LIST_KEEP may reuse
+    int list_inum = 0, list_nall = 0, list_maxnn = 0;
     // input statistics of a training set (ann_stats_*): accumulators [T][6][imax] and counts [T]
     DevBuf st_acc, st_n, st_part, st_pcount;
     bool st_ready = false;
@@ -837,42 +839,55 @@ static void enqueue_list(ann_ctx* c, int nrows, int nall, int cap, int nchunks, 
 
 extern "C" {
 int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32_t* numneigh, const int32_t* neigh, int32_t nall,
-                     const double* x, const int32_t* type, double* energy, double* eatom, double* forces, double* virial, int32_t prec) {
+                     const double* x, const int32_t* type, double* energy, double* eatom, double* forces, double* virial, int32_t prec,
+                     int32_t flags) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
     if (!energy) return fail(c, ANN_ERR_ARG, "energy is NULL");
     ANN_TRY(c, {
         set_device(c);
         if (!c->have_pot) throw ann_error(ANN_ERR_STATE, "no potential loaded");
         if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
+        if (flags & ~ANN_LIST_KEEP) throw ann_error(ANN_ERR_ARG, "unknown flags");
         if (inum < 0 || nall < 0) throw ann_error(ANN_ERR_ARG, "inum and nall must be >= 0");
-        if (inum > 0 && (!numneigh || !x || !type || nall == 0)) throw ann_error(ANN_ERR_ARG, "numneigh, x or type is NULL, or nall is 0");
-        if (!ilist && inum > nall) throw ann_error(ANN_ERR_ARG, "inum > nall without ilist");
-        std::vector<int64_t> noff((size_t)inum + 1, 0);
-        int maxnn = 0;
-        for (int r = 0; r < inum; ++r) {
-            if (numneigh[r] < 0) throw ann_error(ANN_ERR_ARG, "numneigh[" + std::to_string(r) + "] < 0");
-            noff[r + 1] = noff[r] + numneigh[r];
-            maxnn = std::max(maxnn, numneigh[r]);
+        const bool keep = (flags & ANN_LIST_KEEP) != 0;
+        if (inum > 0 && (!x || nall == 0)) throw ann_error(ANN_ERR_ARG, "x is NULL, or nall is 0");
+        cudaStream_t st = c->stream;
+        if (keep) {
+            // the list, ilist and types of the previous call stay on the device: only x is new
+            if (!c->list_staged) throw ann_error(ANN_ERR_STATE, "ANN_LIST_KEEP without a list staged by a previous call");
+            if (inum != c->list_inum || nall != c->list_nall)
+                throw ann_error(ANN_ERR_ARG, "ANN_LIST_KEEP: inum / nall differ from the staged list's");
+        } else {
+            c->list_staged = false;
+            if (inum > 0 && (!numneigh || !type)) throw ann_error(ANN_ERR_ARG, "numneigh or type is NULL");
+            if (!ilist && inum > nall) throw ann_error(ANN_ERR_ARG, "inum > nall without ilist");
+            std::vector<int64_t> noff((size_t)inum + 1, 0);
+            int maxnn = 0;
+            for (int r = 0; r < inum; ++r) {
+                if (numneigh[r] < 0) throw ann_error(ANN_ERR_ARG, "numneigh[" + std::to_string(r) + "] < 0");
+                noff[r + 1] = noff[r] + numneigh[r];
+                maxnn = std::max(maxnn, numneigh[r]);
+            }
+            const int64_t M = noff[inum];
+            if (M > 0 && !neigh) throw ann_error(ANN_ERR_ARG, "neigh is NULL");
+            c->ltype.ensure(4 * (size_t)std::max(nall, 1));
+            c->lnoff.ensure(8 * ((size_t)inum + 1)); c->lneigh.ensure(4 * (size_t)std::max<int64_t>(M, 1));
+            if (ilist) c->lilist.ensure(4 * (size_t)std::max(inum, 1));
+            if (nall > 0) ck(cudaMemcpyAsync(c->ltype.p, type, 4 * (size_t)nall, cudaMemcpyHostToDevice, st), "H2D type");
+            ck(cudaMemcpyAsync(c->lnoff.p, noff.data(), 8 * noff.size(), cudaMemcpyHostToDevice, st), "H2D list offsets");
+            if (M > 0) ck(cudaMemcpyAsync(c->lneigh.p, neigh, 4 * (size_t)M, cudaMemcpyHostToDevice, st), "H2D neighbours");
+            if (ilist && inum > 0) ck(cudaMemcpyAsync(c->lilist.p, ilist, 4 * (size_t)inum, cudaMemcpyHostToDevice, st), "H2D ilist");
+            c->list_inum = inum; c->list_nall = nall; c->list_maxnn = maxnn; c->list_have_ilist = ilist != nullptr;
         }
-        const int64_t M = noff[inum];
-        if (M > 0 && !neigh) throw ann_error(ANN_ERR_ARG, "neigh is NULL");
+        const bool have_ilist = c->list_have_ilist;
+        const int maxnn = c->list_maxnn;
         const bool fp64 = prec == ANN_FP64, want_f = forces != nullptr || virial != nullptr;
         const DevPot& pot = c->plan.pot;
         const int T = c->pot.ntypes(), imax = c->pot.max_input();
         const size_t rb = fp64 ? sizeof(double) : sizeof(float);
-        cudaStream_t st = c->stream;
         const int64_t launches0 = g_launch_counter;
-        // inputs
-        c->lx.ensure(sizeof(double) * 3 * (size_t)std::max(nall, 1)); c->ltype.ensure(4 * (size_t)std::max(nall, 1));
-        c->lnoff.ensure(8 * ((size_t)inum + 1)); c->lneigh.ensure(4 * (size_t)std::max<int64_t>(M, 1));
-        if (ilist) c->lilist.ensure(4 * (size_t)std::max(inum, 1));
-        if (nall > 0) {
-            ck(cudaMemcpyAsync(c->lx.p, x, sizeof(double) * 3 * (size_t)nall, cudaMemcpyHostToDevice, st), "H2D x");
-            ck(cudaMemcpyAsync(c->ltype.p, type, 4 * (size_t)nall, cudaMemcpyHostToDevice, st), "H2D type");
-        }
-        ck(cudaMemcpyAsync(c->lnoff.p, noff.data(), 8 * noff.size(), cudaMemcpyHostToDevice, st), "H2D list offsets");
-        if (M > 0) ck(cudaMemcpyAsync(c->lneigh.p, neigh, 4 * (size_t)M, cudaMemcpyHostToDevice, st), "H2D neighbours");
-        if (ilist && inum > 0) ck(cudaMemcpyAsync(c->lilist.p, ilist, 4 * (size_t)inum, cudaMemcpyHostToDevice, st), "H2D ilist");
+        c->lx.ensure(sizeof(double) * 3 * (size_t)std::max(nall, 1));
+        if (nall > 0) ck(cudaMemcpyAsync(c->lx.p, x, sizeof(double) * 3 * (size_t)nall, cudaMemcpyHostToDevice, st), "H2D x");
         // reduction chunks of the rows: {0, nchunks} then (structure 0, first row, end row) per chunk
         const int nch = (inum + RED_CHUNK - 1) / RED_CHUNK;
         std::vector<int32_t> tab{0, nch};
@@ -905,12 +920,12 @@ int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32
             ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, st), "memset status");
             ListArgs la{};
             la.nrows = inum; la.nall = nall; la.ntypes = T; la.cap = cap; la.rc2 = c->pot.rc * c->pot.rc; la.hint = c->list_hint;
-            la.ilist = ilist ? c->lilist.as<int32_t>() : nullptr; la.noff = c->lnoff.as<int64_t>(); la.neigh = c->lneigh.as<int32_t>();
+            la.ilist = have_ilist ? c->lilist.as<int32_t>() : nullptr; la.noff = c->lnoff.as<int64_t>(); la.neigh = c->lneigh.as<int32_t>();
             la.x = c->lx.as<double>(); la.type = c->ltype.as<int32_t>(); la.rtype = c->lrtype.as<int32_t>(); la.nn = c->lnn.as<int32_t>();
             la.ntc = c->lntc.as<int32_t>(); la.nj = c->lnj.as<int32_t>(); la.nr = c->lnr.p; la.status = c->status.as<int32_t>();
             launch_list_rows(la, fp64, st);
-            if (fp64) enqueue_list<double>(c, inum, nall, cap, nch, want_f, ilist != nullptr);
-            else enqueue_list<float>(c, inum, nall, cap, nch, want_f, ilist != nullptr);
+            if (fp64) enqueue_list<double>(c, inum, nall, cap, nch, want_f, have_ilist);
+            else enqueue_list<float>(c, inum, nall, cap, nch, want_f, have_ilist);
             ck(cudaGetLastError(), "kernel launch");
             int32_t sw[8];
             ck(cudaMemcpyAsync(sw, c->status.p, sizeof(sw), cudaMemcpyDeviceToHost, st), "D2H status");
@@ -932,6 +947,7 @@ int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32
             throw ann_error(ANN_ERR_CUDA, "unknown device status " + std::to_string(sw[0]));
         }
         if (!done) throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity could not be grown");
+        c->list_staged = true;
         c->kernels += g_launch_counter - launches0;
         ck(cudaMemcpyAsync(energy, c->lEs.p, sizeof(double), cudaMemcpyDeviceToHost, st), "D2H energy");
         if (eatom && inum > 0) ck(cudaMemcpyAsync(eatom, c->lEatom.p, sizeof(double) * inum, cudaMemcpyDeviceToHost, st), "D2H eatom");

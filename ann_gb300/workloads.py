@@ -299,6 +299,50 @@ def config5(seed: int = SEED0 + 5, cells=(64, 32, 32), T=80.0):
     return x, v, np.zeros(len(x), np.int32), R
 
 
+def ghost_domain(x, types, R, rcomm):
+    """What an MD engine (LAMMPS, one domain, newton_pair on) passes a pair style for a periodic
+    structure: local atoms (x wrapped into the cell R, lattice vectors as columns) followed by ghost
+    atoms (images x_j + R n, n != 0, inside the cell padded by rcomm on every face) and a FULL
+    neighbour list of every local atom within rcomm (self excluded). Returns (x_all, type_all,
+    owner, numneigh, neigh); rows are in increasing neighbour index."""
+    from scipy.spatial import cKDTree
+    R = np.asarray(R, np.float64)
+    Ri = np.linalg.inv(R)
+    s = np.asarray(x, np.float64) @ Ri.T
+    s -= np.floor(s)
+    s[s >= 1.0] = 0.0
+    xl = s @ R.T
+    n = len(xl)
+    vol = abs(np.linalg.det(R))
+    h = np.array([vol / np.linalg.norm(np.cross(R[:, (d + 1) % 3], R[:, (d + 2) % 3])) for d in range(3)])
+    pad = rcomm / h
+    k = np.ceil(pad).astype(int)
+    gx, go = [xl], [np.arange(n)]
+    for n0 in range(-k[0], k[0] + 1):
+        for n1 in range(-k[1], k[1] + 1):
+            for n2 in range(-k[2], k[2] + 1):
+                if n0 == n1 == n2 == 0:
+                    continue
+                sn = s + np.array([n0, n1, n2], np.float64)
+                keep = np.all((sn > -pad) & (sn < 1.0 + pad), axis=1)
+                if keep.any():
+                    gx.append(xl[keep] + R @ np.array([n0, n1, n2], np.float64))
+                    go.append(np.nonzero(keep)[0])
+    X = np.concatenate(gx)
+    owner = np.concatenate(go).astype(np.int64)
+    T = np.asarray(types, np.int32)[owner]
+    pairs = cKDTree(X).query_pairs(rcomm, output_type="ndarray")
+    a, b = pairs[:, 0], pairs[:, 1]
+    strict = np.einsum("ij,ij->i", X[a] - X[b], X[a] - X[b]) < rcomm * rcomm    # |r| < rcomm, as the list builders
+    a, b = a[strict], b[strict]
+    src = np.concatenate([a[a < n], b[b < n]])
+    dst = np.concatenate([b[a < n], a[b < n]])
+    order = np.lexsort((dst, src))
+    src, dst = src[order], dst[order]
+    numneigh = np.bincount(src, minlength=n).astype(np.int32)
+    return X, T, owner, numneigh, dst.astype(np.int32)
+
+
 def lennard_jones(structures, eps=0.0104, sig=3.4, rcut=8.5):
     """Unshifted, truncated LJ energies and forces (pot_lj_cut.cpp:73-90: 1/2 sum over the full
     periodic-image list) for synthetic training labels."""

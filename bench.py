@@ -224,6 +224,46 @@ def md_leg(dev, steps=1000, warmup=20):
             "drift_mev_atom_ps": float((pe + ke - pe0 - ke0) / n * 1e3 / ps), "precision": "mixed"}
 
 
+def lammps_leg(dev, steps=20, warmup=3, skin=2.0):
+    """The LAMMPS pair-style path (ann_compute_list) on the 262,144-atom FCC argon box (16-32-32-1
+    tanh networks, mixed precision) as one MD domain: local atoms plus ghosts within rc + skin
+    (LAMMPS's default metal-units skin, 2 A), a full list of the same radius. Times, end to end
+    from host arrays to host forces of all local and ghost atoms: a reneighbouring step (list, types
+    and positions sent) and a step between reneighbourings (ANN_LIST_KEEP: positions only)."""
+    from ann_gb300 import MIXED, Context
+    from ann_gb300 import workloads as WL
+    x, _, t, R = WL.config5()
+    ctx = Context(device=dev)
+    WL.make_potential(ctx, 5)
+    X, T, owner, nn, nb = WL.ghost_domain(x, t, R, ctx.rc + skin)
+    n, nall = len(t), len(X)
+
+    def run(keep, k):
+        ts = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            if keep:
+                E, F, _, _ = ctx.compute_list(X, None, None, None, precision=MIXED, keep=True, inum=n, virial=False)
+            else:
+                E, F, _, _ = ctx.compute_list(X, T, nn, nb, precision=MIXED, virial=False)
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts)), E, F
+
+    run(False, warmup)
+    t_full, E, F = run(False, steps)
+    run(True, warmup)
+    t_keep, E2, _ = run(True, steps)
+    folded = np.zeros((n, 3))
+    np.add.at(folded, owner, F)
+    ctx.close()
+    h2d_full = X.nbytes + T.nbytes + nn.nbytes + nb.nbytes + 8 * (n + 1)
+    return {"workload": f"FCC Ar {n} local + {nall - n} ghost atoms, full list rc + {skin} A ({len(nb) / n:.1f} entries per atom)",
+            "precision": "mixed", "reneighbour_step_ms": t_full * 1e3, "keep_step_ms": t_keep * 1e3,
+            "atom_evals_per_s_keep": n / t_keep, "atom_evals_per_s_reneighbour": n / t_full,
+            "h2d_bytes_reneighbour": int(h2d_full), "h2d_bytes_keep": int(X.nbytes), "d2h_bytes": int(24 * nall + 8),
+            "energy_equal_keep_vs_full": bool(E == E2), "net_force_after_fold": float(np.abs(folded.sum(axis=0)).max())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -403,6 +443,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_extras:
         line["training"] = training_leg(dev)
         line["md"] = md_leg(dev)
+        line["lammps"] = lammps_leg(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(offs, posn, types, cell, pot_text)
     if rank == 0:

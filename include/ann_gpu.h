@@ -124,11 +124,17 @@ int ann_compute(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets, const
  *    newton_pair on the engine adds the ghost forces to their owners (LAMMPS reverse_comm).
  *  - virial[9] (or NULL): sum over rows and entries of r[a] * v[b] as for ann_compute (LAMMPS
  *    virial[0..5] = W[0], W[4], W[8], W[1], W[2], W[5]).
+ *  - flags: 0, or ANN_LIST_KEEP when the list, ilist, types and nall are those of the previous
+ *    call on this context and only x changed (an MD engine between two reneighbourings; LAMMPS:
+ *    neighbor->ago != 0). ilist, numneigh, neigh and type may then be NULL; only x is copied to
+ *    the device. The cutoff filter still runs on the new positions, so a list with a skin stays
+ *    exact while atoms move within it.
  * Index, type or non-finite position errors return ANN_ERR_ARG / ANN_ERR_NUMERIC.                 */
+#define ANN_LIST_KEEP 1
 int ann_compute_list(ann_ctx* ctx, int32_t inum, const int32_t* ilist, const int32_t* numneigh,
                      const int32_t* neigh, int32_t nall, const double* x, const int32_t* type,
                      double* energy, double* eatom /* inum or NULL */, double* forces /* 3*nall or NULL */,
-                     double* virial /* 9 or NULL */, int32_t precision);
+                     double* virial /* 9 or NULL */, int32_t precision, int32_t flags);
 
 /* ---- compute with device-resident batches -------------------------------------------------- */
 /* Stage a batch (host pointers; copied to the context's device buffers).                        */

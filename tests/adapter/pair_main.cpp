@@ -58,5 +58,9 @@ int main(int argc, char** argv) {
     for (int i = 0; i < nall; ++i) std::printf("%.17g %.17g %.17g\n", fs[3 * i] - 1.0, fs[3 * i + 1] - 1.0, fs[3 * i + 2] - 1.0);
     std::printf("%.17g %.17g %.17g %.17g %.17g %.17g\n", virial[0], virial[1], virial[2], virial[3], virial[4], virial[5]);
     for (int i = 0; i < nall; ++i) std::printf("%.17g\n", eatom[i]);
+    // a second step with the list kept (no reneighbouring): same positions, same energy
+    const double e2 = pair.compute(inum, ilist.data(), numneigh.data(), firstneigh.data(), nall, x.data(), type.data(), f.data(),
+                                   nullptr, nullptr, nullptr, 0x1FFFFFFF, /*list_changed=*/false);
+    std::printf("%.17g\n", e2);
     return 0;
 }

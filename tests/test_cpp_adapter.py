@@ -114,4 +114,6 @@ def test_pair_style_adapter_matches_list_call(tmp_path, gpu_lib):
     fd = dom.x.T @ F
     assert np.max(np.abs(np.array([fd[0, 0], fd[1, 1], fd[2, 2], fd[0, 1], fd[0, 2], fd[1, 2]]) - Wref)) <= 1e-9 * np.max(np.abs(Wref))
     assert np.max(np.abs(eat[:dom.nlocal] - ea)) <= 1e-12 * np.max(np.abs(ea)) and np.all(eat[dom.nlocal:] == 0.0)
+    e2 = float(out[2 + 2 * nall])                           # the second step, list kept on the device
+    assert abs(e2 - e) <= 1e-13 * abs(e)
     ctx.close()

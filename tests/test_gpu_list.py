@@ -163,3 +163,36 @@ def test_list_and_batch_paths_interleave(ctx, oracle, tmp_path):
     E1, F1, _ = ctx.download()
     assert np.array_equal(E1, E0)
     assert abs(El - E0[1]) / len(t) * 1e3 < E_MEV_ATOM
+
+
+def test_keep_list_between_reneighbourings(ctx, oracle, tmp_path):
+    """ANN_LIST_KEEP: the list of the previous call with new positions (atoms moved by less than
+    half the skin, as between two reneighbourings) equals a full call and the oracle."""
+    structs = cases.small_binary(n_struc=1, seed=19)
+    offs, posn, types, cell = cases.batch(structs)
+    text = cases.config_potential(ctx, 2, tmp_path, precondition_batch=(offs, posn, types, cell))
+    pot = oracle.load_text(text)
+    x, t, R = structs[0]
+    skin = 1.0
+    dom = build_domain(x, t, R, ctx.rc + skin, seed=3)
+    ctx.compute_list(dom.x, dom.type, dom.numneigh, dom.neigh, precision=FP64)
+    rng = np.random.default_rng(5)
+    d = rng.normal(0.0, 1.0, (dom.nlocal, 3))
+    d *= (0.45 * skin / 2) / np.linalg.norm(d, axis=1, keepdims=True)   # < skin / 2 per atom
+    x1 = dom.x + d[dom.owner]                                         # ghosts move with their owners
+    E1, F1, W1, _ = ctx.compute_list(x1, None, None, None, precision=FP64, keep=True, inum=dom.nlocal)
+    E2, F2, W2, _ = ctx.compute_list(x1, dom.type, dom.numneigh, dom.neigh, precision=FP64)
+    assert abs(E1 - E2) <= 1e-13 * abs(E2) and _rel(F1, F2) < 1e-12 and _rel(W1, W2) < 1e-12
+    Eo, Fo, Wo = _oracle(pot, x1[:dom.nlocal], t, R)
+    assert _rel(E1, Eo) < REL and _rel(dom.fold(F1), Fo) < REL and _rel(W1, Wo) < REL
+    Em, Fm, _, _ = ctx.compute_list(x1, None, None, None, precision=MIXED, keep=True, inum=dom.nlocal)
+    assert abs(Em - Eo) / dom.nlocal * 1e3 < E_MEV_ATOM and np.max(np.abs(dom.fold(Fm) - Fo)) * 1e3 < F_MEV_A
+    with pytest.raises(AnnError, match="differ"):
+        ctx.compute_list(x1[:-1], None, None, None, precision=FP64, keep=True, inum=dom.nlocal)
+    c2 = Context()
+    try:
+        c2.load_text(text)
+        with pytest.raises(AnnError, match="staged"):
+            c2.compute_list(x1, None, None, None, precision=FP64, keep=True, inum=dom.nlocal)
+    finally:
+        c2.close()

@@ -34,3 +34,22 @@ def test_domain_rows_are_the_periodic_neighbours(oracle, case):
         F = np.zeros((dom.nall, 3))
         F[dom.nall - 1] = [1.0, 2.0, 3.0]
         assert np.array_equal(dom.fold(F)[dom.owner[-1]], [1.0, 2.0, 3.0])
+
+
+@pytest.mark.parametrize("case", ["binary", "tiny"])
+def test_fast_ghost_domain_matches(case):
+    """ann_gb300.workloads.ghost_domain (k-d tree, the bench's LAMMPS-shaped domain) gives every
+    local atom the same neighbours, by position, as the brute-force builder above."""
+    pytest.importorskip("scipy")
+    from ann_gb300 import workloads as W
+    structs = cases.small_binary(n_struc=1, seed=23) if case == "binary" else cases.tiny_cells()
+    for x, t, R in structs:
+        X, T, owner, nn, nb = W.ghost_domain(x, t, R, 6.0)
+        dom = build_domain(x, t, R, 6.0, shuffle=False)
+        assert np.array_equal(X[:len(t)], dom.x[:dom.nlocal]) and np.array_equal(T[owner], T)
+        o1 = np.concatenate([[0], np.cumsum(nn)])
+        o2 = np.concatenate([[0], np.cumsum(dom.numneigh)])
+        for i in range(len(t)):
+            a = sorted(map(tuple, np.round(X[nb[o1[i]:o1[i + 1]]], 9)))
+            b = sorted(map(tuple, np.round(dom.x[dom.neigh[o2[i]:o2[i + 1]]], 9)))
+            assert a == b, i
