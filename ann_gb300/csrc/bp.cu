@@ -222,10 +222,12 @@ static __device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
     return d;
 }
 
+// The triplet's forces in the frame of its two unit vectors: v_j = cj u_j + bj u_k and
+// v_k = ck u_k + bk u_j (u = r / |r| of the entry, gj.w = 1 / |r_ij|).
 template <typename real, int NG>
 __device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, const DampRec<real, NG>& dj,
                                               const typename V4<real>::T& gk, const DampRec<real, NG>& dk,
-                                              const real (&al)[NG][9], real (&vj)[3], real (&vk)[3]) {
+                                              const real (&al)[NG][9], real& cj, real& bj, real& ck, real& bk) {
     const real cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
     real phi = real(0), e0 = real(0), e1 = real(0);
 #pragma unroll
@@ -239,16 +241,14 @@ __device__ __forceinline__ void triplet_force(const typename V4<real>::T& gj, co
         e1 -= A * dj.D(g) * dk.Dp(g);
     }
     const real idj = gj.w, idk = gk.w;
-    const real cj = -phi * cs * idj + e0, bj = phi * idj;
-    const real ck = -phi * cs * idk + e1, bk = phi * idk;
-    vj[0] = cj * gj.x + bj * gk.x; vj[1] = cj * gj.y + bj * gk.y; vj[2] = cj * gj.z + bj * gk.z;
-    vk[0] = ck * gk.x + bk * gj.x; vk[1] = ck * gk.y + bk * gj.y; vk[2] = ck * gk.z + bk * gj.z;
+    cj = -phi * cs * idj + e0; bj = phi * idj;
+    ck = -phi * cs * idk + e1; bk = phi * idk;
 }
 
 // the same for FP32 and two damping groups, both groups at once in packed FP32 pairs (group 0 in
 // the low half): alp[p] = (al[0][p], al[1][p])
 __device__ __forceinline__ void triplet_force2(const Vec4f& gj, const DampRec<float, 2>& dj, const Vec4f& gk, const DampRec<float, 2>& dk,
-                                               const uint64_t (&alp)[9], float (&vj)[3], float (&vk)[3]) {
+                                               const uint64_t (&alp)[9], float& cj, float& bj, float& ck, float& bk) {
     const float cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
     const uint64_t c2 = pk2(cs, cs);
     uint64_t B = alp[8];
@@ -261,10 +261,8 @@ __device__ __forceinline__ void triplet_force2(const Vec4f& gj, const DampRec<fl
     const float e0 = -hsum2(mul2(mul2(A, Dpj), Dk));
     const float e1 = -hsum2(mul2(mul2(A, Dj), Dpk));
     const float idj = gj.w, idk = gk.w;
-    const float cj = -phi * cs * idj + e0, bj = phi * idj;
-    const float ck = -phi * cs * idk + e1, bk = phi * idk;
-    vj[0] = cj * gj.x + bj * gk.x; vj[1] = cj * gj.y + bj * gk.y; vj[2] = cj * gj.z + bj * gk.z;
-    vk[0] = ck * gk.x + bk * gj.x; vk[1] = ck * gk.y + bk * gj.y; vk[2] = ck * gk.z + bk * gj.z;
+    cj = -phi * cs * idj + e0; bj = phi * idj;
+    ck = -phi * cs * idk + e1; bk = phi * idk;
 }
 
 // coefficients of A_g(cos) from the block's dE/dG per slot (slot g*8 + 2q + (lambda < 0), zeta = 2^q):
@@ -295,10 +293,12 @@ __device__ __forceinline__ void angular_poly(const real* dE, const int32_t* slot
 // chunks of at most 32, and lane L owns element L of every chunk (chunk start + L). A task is
 // either the triangle of one chunk (tri: pairs a < b of [p0, p0+np)) or the rectangle of two
 // chunks P x Q (np >= nq). Partners follow a rotation (b = a + step mod n), so in every step the
-// 32 lanes touch 32 different partners and each partner is the target of exactly one lane: the
-// contribution to the lane's own element accumulates in registers, the partner's contribution is
-// routed to its owner lane with a shuffle, and each owner adds its totals to the element's
-// shared-memory accumulator once per task. No atomics; every unordered pair is evaluated once.
+// 32 lanes touch 32 different partners and each partner is the target of exactly one lane. A
+// lane keeps the forces on its own element as c u_own + s (scalar c, vector s); the partner's
+// share (ck, bk) goes to the partner's owner lane by two shuffles, and the owner adds ck to its
+// scalar and bk times the sender's unit vector (read from shared memory) to its vector. Each
+// owner adds its totals to the element's shared-memory accumulator once per task. No atomics;
+// every unordered pair is evaluated once.
 template <typename real, int NG, int PASS, bool TRI>
 __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&al)[NG][9], int lane,
                                            int p0, int np, int q0, int nq) {
@@ -309,6 +309,7 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     DampRec<real, NG> da;
     if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
     else { ga.x = ga.y = ga.z = ga.w = real(0); da.zero(); }
+    real ca = real(0), cb = real(0);                                       // along the owned unit vectors
     real sa[3] = {real(0), real(0), real(0)}, sb[3] = {real(0), real(0), real(0)};
     constexpr bool PACKED = std::is_same<real, float>::value && NG == 2;
     uint64_t alp[9];
@@ -330,20 +331,27 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
         const R4 gb = w.geo[e];
         DampRec<real, NG> db;
         db.load(w.dp + e * NDP);
-        real vj[3], vk[3];
-        if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, vj, vk);
-        else triplet_force<real, NG>(ga, da, gb, db, al, vj, vk);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            sa[c] += valid ? vj[c] : real(0);
-            const real r = __shfl_sync(0xffffffffu, valid ? vk[c] : real(0), src & 31);
-            if (TRI) sa[c] += r; else sb[c] += r;
-        }
+        const R4 gs = w.geo[p0 + (src < n ? src : 0)];     // the sending lane's own element
+        real cj, bj, ck, bk;
+        if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, cj, bj, ck, bk);
+        else triplet_force<real, NG>(ga, da, gb, db, al, cj, bj, ck, bk);
+        if (!valid) { cj = real(0); bj = real(0); ck = real(0); bk = real(0); }
+        ca += cj;
+        sa[0] += bj * gb.x; sa[1] += bj * gb.y; sa[2] += bj * gb.z;
+        const real rc = __shfl_sync(0xffffffffu, ck, src & 31);
+        const real rb = __shfl_sync(0xffffffffu, bk, src & 31);
+        if (TRI) { ca += rc; sa[0] += rb * gs.x; sa[1] += rb * gs.y; sa[2] += rb * gs.z; }
+        else { cb += rc; sb[0] += rb * gs.x; sb[1] += rb * gs.y; sb[2] += rb * gs.z; }
         part = (part + 1 == n) ? 0 : part + 1;
         src = (src == 0) ? n - 1 : src - 1;
     }
-    if (ownP) { w.ax[p0 + lane] += sa[0]; w.ay[p0 + lane] += sa[1]; w.az[p0 + lane] += sa[2]; }
-    if (ownQ) { w.ax[q0 + lane] += sb[0]; w.ay[q0 + lane] += sb[1]; w.az[q0 + lane] += sb[2]; }
+    if (ownP) {
+        w.ax[p0 + lane] += ca * ga.x + sa[0]; w.ay[p0 + lane] += ca * ga.y + sa[1]; w.az[p0 + lane] += ca * ga.z + sa[2];
+    }
+    if (ownQ) {
+        const R4 gq = w.geo[q0 + lane];
+        w.ax[q0 + lane] += cb * gq.x + sb[0]; w.ay[q0 + lane] += cb * gq.y + sb[1]; w.az[q0 + lane] += cb * gq.z + sb[2];
+    }
 }
 
 // The same chunk tasks for the symmetry functions of a fast-path block: the lane's own neighbour
