@@ -121,6 +121,23 @@ def test_generic_basis_variants(ctx, oracle, tmp_path):
     _check_mixed(ctx, offs, posn, types, cell, E, F)
 
 
+def test_step_cutoff_logcosh2_and_cos_generic(ctx, oracle):
+    """The variants the generic potential above leaves out: the STEP cutoff (cutoff.cpp:62-146),
+    the LOGCOSH2 radial form (basis_radial.cpp:263-379), and the COS cutoff on generic angular forms."""
+    text = cases.generic_potential_text()
+    text = text.replace("BasisR TANH 5.000000 SECH 3", "BasisR STEP 5.000000 LOGCOSH2 3")
+    text = text.replace("BasisR POLY3 5.000000 LOGCOSH 2", "BasisR COS 5.000000 LOGCOSH2 2")
+    text = text.replace("BasisA TANH 5.000000 GAUSS2 3", "BasisA STEP 5.000000 GAUSS2 3")
+    text = text.replace("BasisA POLY3 5.000000 STUDENT4 2", "BasisA COS 5.000000 STUDENT4 2")
+    assert text.count("LOGCOSH2") == 2 and text.count("STEP") == 2
+    ctx.load_text(text)
+    pot = oracle.load_text(text)
+    structs = cases.small_binary(n_struc=3, seed=25) + cases.tiny_cells()
+    offs, posn, types, cell = cases.batch(structs)
+    E, F, _ = _check_fp64(ctx, pot, oracle, offs, posn, types, cell)
+    _check_mixed(ctx, offs, posn, types, cell, E, F)
+
+
 def test_large_structure_reductions(ctx, oracle, tmp_path):
     """A structure of 2,600 atoms (eleven reduction chunks of at most 256 atoms) between two
     small ones: energies and virials as the oracle's, also in the mixed form."""
