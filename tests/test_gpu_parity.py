@@ -125,11 +125,10 @@ def test_step_cutoff_logcosh2_and_cos_generic(ctx, oracle):
     """The variants the generic potential above leaves out: the STEP cutoff (cutoff.cpp:62-146),
     the LOGCOSH2 radial form (basis_radial.cpp:263-379), and the COS cutoff on generic angular forms."""
     text = cases.generic_potential_text()
-    text = text.replace("BasisR TANH 5.000000 SECH 3", "BasisR STEP 5.000000 LOGCOSH2 3")
-    text = text.replace("BasisR POLY3 5.000000 LOGCOSH 2", "BasisR COS 5.000000 LOGCOSH2 2")
-    text = text.replace("BasisA TANH 5.000000 GAUSS2 3", "BasisA STEP 5.000000 GAUSS2 3")
-    text = text.replace("BasisA POLY3 5.000000 STUDENT4 2", "BasisA COS 5.000000 STUDENT4 2")
-    assert text.count("LOGCOSH2") == 2 and text.count("STEP") == 2
+    for blk in ("BasisR", "BasisA"):                   # every block of a type shares its cutoff
+        text = text.replace(f"{blk} TANH 5.000000", f"{blk} STEP 5.000000").replace(f"{blk} POLY3 5.000000", f"{blk} COS 5.000000")
+    text = text.replace("STEP 5.000000 SECH 3", "STEP 5.000000 LOGCOSH2 3").replace("COS 5.000000 LOGCOSH 2", "COS 5.000000 LOGCOSH2 2")
+    assert text.count("LOGCOSH2") == 2 and text.count("STEP") == 5 and text.count(" COS ") == 5
     ctx.load_text(text)
     pot = oracle.load_text(text)
     structs = cases.small_binary(n_struc=3, seed=25) + cases.tiny_cells()
