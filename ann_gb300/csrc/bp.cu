@@ -524,16 +524,19 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
 
         real* Gout = (PASS == PASS_SYMM) ? a.G + (size_t)i * imax : (PASS == PASS_JVP) ? a.U + (size_t)i * imax : nullptr;
 
-        // ---- 2. radial: lanes own neighbours. Symmetry functions / tangents take the block's
-        //         functions in register chunks (parameters hoisted, the radial form resolved once
-        //         per block); the force pass loops over the functions with uniform loads ----------
-        for (int J = 0; J < T; ++J) {
-            const DevRadial& R = TT.R[J];
-            if (R.n == 0) continue;
-            const int e0 = tstart[J], e1 = e0 + tcnt[J];
-            auto block = [&](auto form) {
-                constexpr int NAME = decltype(form)::value;
-                if (PASS == PASS_FORCE) {
+        // ---- 2. radial. Symmetry functions / tangents: lanes own functions. The blocks' functions
+        //         are numbered one after the other (block J's function m is slot off_J + m), lane
+        //         L takes slots L, L + 32, ... and sums its function over the block's neighbour
+        //         range in shared memory, so every slot is one lane's sequential sum (no reduction).
+        //         Force pass: lanes own neighbours and loop over the block's functions with
+        //         uniform loads ------------------------------------------------------------------
+        if (PASS == PASS_FORCE) {
+            for (int J = 0; J < T; ++J) {
+                const DevRadial& R = TT.R[J];
+                if (R.n == 0) continue;
+                const int e0 = tstart[J], e1 = e0 + tcnt[J];
+                auto block = [&](auto form) {
+                    constexpr int NAME = decltype(form)::value;
                     for (int e = e0 + lane; e < e1; e += 32) {
                         const real dd = w.d[e], f = w.fc[e], g = w.fcg[e];
                         real amp = real(0);
@@ -546,38 +549,36 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                         const R4 g4 = w.geo[e];
                         w.ax[e] += amp * g4.x; w.ay[e] += amp * g4.y; w.az[e] += amp * g4.z;
                     }
-                    return;
-                }
-                for (int m0 = 0; m0 < R.n; m0 += CHUNK) {
-                    real eta[CHUNK], rs[CHUNK], acc[CHUNK];
+                };
+                if (R.name == R_GAUSSIAN) block(std::integral_constant<int, R_GAUSSIAN>{});
+                else block(std::integral_constant<int, -1>{});
+            }
+        } else {
+            int nslot = 0;
+            for (int J = 0; J < T; ++J) nslot += TT.R[J].n;
+            for (int q = lane; q < nslot; q += 32) {
+                int J = 0, m = q, e0 = 0, ne = 0;
 #pragma unroll
-                    for (int s = 0; s < CHUNK; ++s) {
-                        const bool ok = m0 + s < R.n;
-                        eta[s] = ok ? a.prm.reta[R.pidx + m0 + s] : real(0);
-                        rs[s] = ok ? a.prm.rs[R.pidx + m0 + s] : real(0);
-                        acc[s] = real(0);
-                    }
-                    for (int e = e0 + lane; e < e1; e += 32) {
-                        const real dd = w.d[e], f = w.fc[e], g = w.fcg[e];
-                        const real tdd = (PASS == PASS_JVP) ? w.tg[e].w : real(0);
-#pragma unroll
-                        for (int s = 0; s < CHUNK; ++s) {
-                            if (m0 + s < R.n) {
-                                real val, der;
-                                radial_vd_t<NAME, real>(R.name, eta[s], rs[s], dd, f, g, val, der);
-                                acc[s] += (PASS == PASS_SYMM) ? val : der * tdd;
-                            }
-                        }
-                    }
-                    const real v = warp_slot_reduce<real, CHUNK>(acc, lane);
-                    if ((lane & 1) == 0) {
-                        const int m = m0 + ((lane >> 1) & (CHUNK - 1));
-                        if (m < R.n) Gout[R.off + m] = v;
-                    }
+                for (int t = 0; t < MAXT; ++t) {      // the lane's block, with constant indices only
+                    if (t < T && J == t && m >= TT.R[t].n) { m -= TT.R[t].n; J = t + 1; }
                 }
-            };
-            if (R.name == R_GAUSSIAN) block(std::integral_constant<int, R_GAUSSIAN>{});
-            else block(std::integral_constant<int, -1>{});
+#pragma unroll
+                for (int t = 0; t < MAXT; ++t) if (t == J) { e0 = tstart[t]; ne = tcnt[t]; }
+                const DevRadial& R = TT.R[J];
+                const real eta = a.prm.reta[R.pidx + m], rs = a.prm.rs[R.pidx + m];
+                real acc = real(0);
+                auto block = [&](auto form) {
+                    constexpr int NAME = decltype(form)::value;
+                    for (int e = e0; e < e0 + ne; ++e) {
+                        real val, der;
+                        radial_vd_t<NAME, real>(R.name, eta, rs, w.d[e], w.fc[e], w.fcg[e], val, der);
+                        acc += (PASS == PASS_SYMM) ? val : der * w.tg[e].w;
+                    }
+                };
+                if (R.name == R_GAUSSIAN) block(std::integral_constant<int, R_GAUSSIAN>{});
+                else block(std::integral_constant<int, -1>{});
+                Gout[R.off + m] = acc;
+            }
         }
         __syncwarp();
 
