@@ -370,7 +370,7 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
     const int qb = TRI ? p0 : q0;
     int part = TRI ? lane + 1 : lane;
     if (part >= n) part -= n;
-#pragma unroll 1
+#pragma unroll 2   // two independent triplets per iteration
     for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
         const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
         const int e = qb + (valid ? part : 0);
