@@ -8,6 +8,7 @@ reference raises std::invalid_argument / std::runtime_error.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 import os
 from pathlib import Path
 
@@ -67,6 +68,8 @@ _SIGS = {
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
     "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_host_alloc": (C.c_int, [_V, C.c_int64, C.POINTER(C.c_void_p)]),
+    "ann_host_free": (C.c_int, [_V, C.c_void_p]),
     "ann_compute_list": (C.c_int, [_V, C.c_int32, _I32, _I32, _I32, C.c_int32, _D, _I32, _D, _D, _D, _D, C.c_int32, C.c_int32]),
     "ann_stats_reset": (C.c_int, [_V]),
     "ann_stats_accumulate": (C.c_int, [_V]),
@@ -263,15 +266,35 @@ class Context:
         self._ck(self.lib.ann_init_network(self.h, t, seed, dist, init, sigma_b, sigma_w))
 
     # ---- compute
-    def compute(self, offs, posn, types, cell, forces=True, virial=True, precision=None):
-        """E (+F, virial) of a packed batch; returns (energy[S], forces[N,3] or None, virial[S,3,3] or None)."""
+    def pinned(self, shape, dtype=np.float64) -> np.ndarray:
+        """A numpy array in page-locked host memory (ann_host_alloc), freed with the array: inputs
+        and outputs there are copied by DMA without staging."""
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        ptr = C.c_void_p()
+        self._ck(self.lib.ann_host_alloc(self.h, nbytes, C.byref(ptr)))
+        if not ptr.value:
+            return np.zeros(shape, dt)
+        buf = (C.c_char * nbytes).from_address(ptr.value)
+        arr = np.frombuffer(buf, dtype=dt).reshape(shape)
+        weakref.finalize(buf, self.lib.ann_host_free, None, C.c_void_p(ptr.value))
+        return arr
+
+    def compute(self, offs, posn, types, cell, forces=True, virial=True, precision=None, out=None):
+        """E (+F, virial) of a packed batch; returns (energy[S], forces[N,3] or None, virial[S,3,3] or None).
+        out = (energy, forces, virial) arrays to write into (e.g. pinned ones), else new arrays."""
         prec = self.precision if precision is None else precision
         S = len(offs) - 1
         N = int(offs[-1])
         self._S, self._N = S, N
-        e = np.zeros(S)
-        f = np.zeros((N, 3)) if forces else None
-        w = np.zeros((S, 3, 3)) if virial else None
+        if out is not None:
+            e, f, w = out
+            f = f if forces else None
+            w = w if virial else None
+        else:
+            e = np.zeros(S)
+            f = np.zeros((N, 3)) if forces else None
+            w = np.zeros((S, 3, 3)) if virial else None
         self._ck(self.lib.ann_compute(self.h, S, _i64(np.ascontiguousarray(offs, np.int64)), _d(np.ascontiguousarray(posn, np.float64)),
                                       _i32(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
                                       _d(e), _d(f), _d(w), prec))

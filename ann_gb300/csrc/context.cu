@@ -1079,6 +1079,23 @@ int ann_get_input_scaling(ann_ctx* c, int32_t t, double* w, double* b, int32_t n
     return ANN_OK;
 }
 
+int ann_host_alloc(ann_ctx* c, int64_t bytes, void** ptr) {
+    if (!c || !ptr) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (bytes < 0) return fail(c, ANN_ERR_ARG, "bytes < 0");
+    *ptr = nullptr;
+    if (bytes == 0) return ANN_OK;
+    ANN_TRY(c, {
+        set_device(c);
+        ck(cudaMallocHost(ptr, (size_t)bytes), "cudaMallocHost");
+    })
+}
+int ann_host_free(ann_ctx* c, void* ptr) {   // ctx may be NULL (a buffer may outlive its context)
+    if (!ptr) return ANN_OK;
+    const cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) return fail(c, ANN_ERR_CUDA, std::string("cudaFreeHost: ") + cudaGetErrorString(e));
+    return ANN_OK;
+}
+
 // ---- inspection
 int ann_symm_width(ann_ctx* c, int32_t* w) {
     if (!c || !w) return fail(c, ANN_ERR_ARG, "NULL argument");

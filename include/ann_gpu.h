@@ -152,6 +152,13 @@ int ann_batch_download(ann_ctx* ctx, double* energy, double* forces, double* vir
 /* Same results into device pointers (double) on the context's device; synchronises.              */
 int ann_batch_results_device(ann_ctx* ctx, double* d_energy, double* d_forces, double* d_virial);
 int ann_synchronize(ann_ctx* ctx);
+/* Page-locked host memory on the context's device (cudaMallocHost): inputs built there and
+ * results read into it are copied by DMA without staging, asynchronously on the context stream.
+ * For callers that feed many batches (a data loader, an MD engine's arrays). Free with
+ * ann_host_free (ctx may be NULL there: a buffer may outlive its context); bytes = 0 returns
+ * NULL.                                                                                           */
+int ann_host_alloc(ann_ctx* ctx, int64_t bytes, void** ptr);
+int ann_host_free(ann_ctx* ctx, void* ptr);
 /* Raw CUDA stream of the context (cudaStream_t), for callers timing or ordering around it.      */
 void* ann_stream(ann_ctx* ctx);
 

@@ -229,3 +229,20 @@ def test_every_activation(ctx, oracle, neuron):
     Eo, Fo, Wo, _, _ = pot.compute(offs, posn, types, cell)
     assert _rel_err(E, Eo) < REL and _rel_err(F, Fo) < REL and _rel_err(Wv, Wo) < REL
     _check_mixed(ctx, offs, posn, types, cell, E, F)
+
+
+def test_pinned_host_buffers(ctx, tmp_path):
+    """ann_host_alloc buffers as inputs and outputs of ann_compute give the pageable-array results
+    (FP64: bit-identical; the buffers outlive nothing and are freed with their arrays)."""
+    structs = cases.small_binary(n_struc=4, seed=27)
+    offs, posn, types, cell = cases.batch(structs)
+    cases.config_potential(ctx, 2, tmp_path)
+    E0, F0, W0 = ctx.compute(offs, posn, types, cell, precision=FP64)
+    h = [ctx.pinned(offs.shape, np.int64), ctx.pinned(posn.shape), ctx.pinned(types.shape, np.int32), ctx.pinned(cell.shape)]
+    for dst, src in zip(h, (offs, posn, types, cell)):
+        dst[:] = src
+    out = (ctx.pinned(E0.shape), ctx.pinned(F0.shape), ctx.pinned(W0.shape))
+    E1, F1, W1 = ctx.compute(*h, precision=FP64, out=out)
+    assert E1 is out[0] and np.array_equal(E1, E0) and np.allclose(F1, F0, rtol=0, atol=1e-12 * np.abs(F0).max())
+    assert np.array_equal(W1, W0)
+    assert ctx.pinned((0,)).size == 0
