@@ -177,6 +177,7 @@ struct ann_ctx {
     bool profile = false;
     bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
     int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
+    int32_t* status_h = nullptr;    // page-locked copy of the status word
     cudaEvent_t ev[16] = {};
 };
 
@@ -528,6 +529,12 @@ static void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true)
     c->have_forces = forces;
 }
 
+// a page-locked copy of the device status word, for reads that ride along with result copies
+static int32_t* status_host(ann_ctx* c) {
+    if (!c->status_h) ck(cudaMallocHost(reinterpret_cast<void**>(&c->status_h), 4 * 8), "cudaMallocHost status");
+    return c->status_h;
+}
+
 // wait for the batch; on neighbour overflow grow the capacity and recompute
 static void finish_batch(ann_ctx* c) {
     for (int attempt = 0; attempt < 6; ++attempt) {
@@ -607,6 +614,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->lEs, &c->lWs, &c->st_acc, &c->st_n, &c->st_part, &c->st_pcount})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->status_h) cudaFreeHost(c->status_h);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return ANN_OK;
@@ -795,11 +803,23 @@ int ann_compute(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* p
         leave_md(c);
         upload_batch(c, nstruc, offs, posn, type, cell, false);
         run_batch(c, prec, forces != nullptr || virial != nullptr);
-        finish_batch(c);
-        if (c->S > 0) ck(cudaMemcpyAsync(energy, c->Es.p, sizeof(double) * c->S, cudaMemcpyDeviceToHost, c->stream), "D2H energy");
-        if (forces && c->N > 0) ck(cudaMemcpyAsync(forces, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream), "D2H forces");
-        if (virial && c->S > 0) ck(cudaMemcpyAsync(virial, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, cudaMemcpyDeviceToHost, c->stream), "D2H virial");
+        // the results and the status word in one round trip; a status that is not clean (list
+        // overflow, bad input) goes through finish_batch, which recovers or throws, and the
+        // results are copied again
+        auto copy_out = [&]() {
+            if (c->S > 0) ck(cudaMemcpyAsync(energy, c->Es.p, sizeof(double) * c->S, cudaMemcpyDeviceToHost, c->stream), "D2H energy");
+            if (forces && c->N > 0) ck(cudaMemcpyAsync(forces, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream), "D2H forces");
+            if (virial && c->S > 0) ck(cudaMemcpyAsync(virial, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, cudaMemcpyDeviceToHost, c->stream), "D2H virial");
+        };
+        copy_out();
+        int32_t* sh = status_host(c);
+        ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
         ck(cudaStreamSynchronize(c->stream), "synchronize");
+        if (sh[0] != 0) {
+            finish_batch(c);
+            copy_out();
+            ck(cudaStreamSynchronize(c->stream), "synchronize");
+        }
     })
 }
 
