@@ -217,20 +217,21 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
             zb[a * ld + n] = f1 * ab[a * ld + n] + f2 * zd[(size_t)l * tl + a * ld + n] * adbv;
         }
         __syncthreads();
-        // bias gradient: sum over atoms of zbar
+        // bias gradient: sum over the tile's atoms of zbar, in the pass's precision (the products
+        // are formed in it), then added to the FP64 gradient
         for (int n = threadIdx.x; n < no; n += MLP_T) {
-            double s = 0.0;
-            for (int a = 0; a < TAT; ++a) s += (double)zb[a * ld + n];
-            atomicAdd(&A.grad[pbase + bias_at[l] + n], s);
+            real s = real(0);
+            for (int a = 0; a < TAT; ++a) s += zb[a * ld + n];
+            atomicAdd(&A.grad[pbase + bias_at[l] + n], (double)s);
         }
         // weight gradient: sum_a zbar[a][n] a_{l}[a][m] + zdbar[a][n] ad_{l}[a][m], column-major
         const real* xin = act + (size_t)l * tl;
         const real* xind = actd + (size_t)l * tl;
         for (int idx = threadIdx.x; idx < no * ni; idx += MLP_T) {
             const int n = idx % no, m = idx / no;
-            double s = 0.0;
-            for (int a = 0; a < TAT; ++a) s += (double)zb[a * ld + n] * (double)xin[a * ld + m] + (double)zdb[a * ld + n] * (double)xind[a * ld + m];
-            atomicAdd(&A.grad[pbase + wt_at[l] + m * no + n], s);
+            real s = real(0);
+            for (int a = 0; a < TAT; ++a) s += zb[a * ld + n] * xin[a * ld + m] + zdb[a * ld + n] * xind[a * ld + m];
+            atomicAdd(&A.grad[pbase + wt_at[l] + m * no + n], (double)s);
         }
         __syncthreads();
         if (l > 0) {
