@@ -61,6 +61,63 @@ __device__ __forceinline__ void layer_bwd(const real* __restrict__ WTl, int no, 
     }
 }
 
+// Register-tiled forms of the training pass, which carries a value and a tangent through every
+// layer: each thread computes RT consecutive outputs of one atom for both, so one weight load
+// feeds 2 FMAs and one activation load feeds RT of them.
+constexpr int RT = 4;
+// z[a][n] = b[n] + sum_m W[n][m] x[a][m] and zd[a][n] = sum_m W[n][m] xd[a][m]
+template <typename real, int TAn>
+__device__ __forceinline__ void layer_fwd2(const real* __restrict__ Wl, const real* __restrict__ bl, int no, int ni,
+                                           const real* x, const real* xd, real* z, real* zd, int ld) {
+    const int ng = (no + RT - 1) / RT;
+    for (int idx = threadIdx.x; idx < TAn * ng; idx += MLP_T) {
+        const int a = idx % TAn, n0 = (idx / TAn) * RT;
+        const real* xr = x + a * ld;
+        const real* xdr = xd + a * ld;
+        real s[RT], sd[RT];
+#pragma unroll
+        for (int k = 0; k < RT; ++k) { s[k] = (n0 + k < no) ? bl[n0 + k] : real(0); sd[k] = real(0); }
+        const real* w0 = Wl + (size_t)n0 * ni;
+        for (int m = 0; m < ni; ++m) {
+            const real xv = xr[m], xdv = xdr[m];
+#pragma unroll
+            for (int k = 0; k < RT; ++k) {
+                const real w = (n0 + k < no) ? w0[(size_t)k * ni + m] : real(0);
+                s[k] += w * xv; sd[k] += w * xdv;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < RT; ++k)
+            if (n0 + k < no) { z[a * ld + n0 + k] = s[k]; zd[a * ld + n0 + k] = sd[k]; }
+    }
+}
+// y[a][m] = sum_n WT[m][n] x[a][n] and yd[a][m] = sum_n WT[m][n] xd[a][n]   (WT = W^T, rows of length no)
+template <typename real, int TAn>
+__device__ __forceinline__ void layer_bwd2(const real* __restrict__ WTl, int no, int ni, const real* x, const real* xd, real* y,
+                                           real* yd, int ld) {
+    const int mg = (ni + RT - 1) / RT;
+    for (int idx = threadIdx.x; idx < TAn * mg; idx += MLP_T) {
+        const int a = idx % TAn, m0 = (idx / TAn) * RT;
+        const real* xr = x + a * ld;
+        const real* xdr = xd + a * ld;
+        real s[RT], sd[RT];
+#pragma unroll
+        for (int k = 0; k < RT; ++k) { s[k] = real(0); sd[k] = real(0); }
+        const real* w0 = WTl + (size_t)m0 * no;
+        for (int n = 0; n < no; ++n) {
+            const real xv = xr[n], xdv = xdr[n];
+#pragma unroll
+            for (int k = 0; k < RT; ++k) {
+                const real w = (m0 + k < ni) ? w0[(size_t)k * no + n] : real(0);
+                s[k] += w * xv; sd[k] += w * xdv;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < RT; ++k)
+            if (m0 + k < ni) { y[a * ld + m0 + k] = s[k]; yd[a * ld + m0 + k] = sd[k]; }
+    }
+}
+
 // ---------------------------------------------------------------- forward + dE/dG
 template <typename real>
 __global__ void __launch_bounds__(MLP_T) k_mlp_fb(const __grid_constant__ DevPot pot, const MlpArgs<real> A, int ld) {
@@ -176,8 +233,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
         real* xind = actd + (size_t)l * tl;
         real* xo = act + (size_t)(l + 1) * tl;
         real* xod = actd + (size_t)(l + 1) * tl;
-        layer_fwd<real, TAT>(A.prm.w + net.woff[l], A.prm.b + net.boff[l], no, ni, xin, xo, ld);
-        layer_fwd<real, TAT>(A.prm.w + net.woff[l], nullptr, no, ni, xind, xod, ld);
+        layer_fwd2<real, TAT>(A.prm.w + net.woff[l], A.prm.b + net.boff[l], no, ni, xin, xind, xo, xod, ld);
         __syncthreads();
         const int actn = (l == L - 1) ? (int)N_LINEAR : net.neuron;
         for (int idx = threadIdx.x; idx < TAT * no; idx += MLP_T) {
@@ -224,19 +280,37 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
             for (int a = 0; a < TAT; ++a) s += zb[a * ld + n];
             atomicAdd(&A.grad[pbase + bias_at[l] + n], (double)s);
         }
-        // weight gradient: sum_a zbar[a][n] a_{l}[a][m] + zdbar[a][n] ad_{l}[a][m], column-major
+        // weight gradient: sum_a zbar[a][n] a_{l}[a][m] + zdbar[a][n] ad_{l}[a][m], column-major;
+        // each thread a block of RT outputs n x 2 inputs m (every shared value used 2 or RT times)
         const real* xin = act + (size_t)l * tl;
         const real* xind = actd + (size_t)l * tl;
-        for (int idx = threadIdx.x; idx < no * ni; idx += MLP_T) {
-            const int n = idx % no, m = idx / no;
-            real s = real(0);
-            for (int a = 0; a < TAT; ++a) s += zb[a * ld + n] * xin[a * ld + m] + zdb[a * ld + n] * xind[a * ld + m];
-            atomicAdd(&A.grad[pbase + wt_at[l] + m * no + n], (double)s);
+        const int ngw = (no + RT - 1) / RT, mgw = (ni + 1) / 2;
+        for (int idx = threadIdx.x; idx < ngw * mgw; idx += MLP_T) {
+            const int n0 = (idx % ngw) * RT, m0 = (idx / ngw) * 2;
+            real s[RT][2];
+#pragma unroll
+            for (int k = 0; k < RT; ++k) { s[k][0] = real(0); s[k][1] = real(0); }
+            for (int a = 0; a < TAT; ++a) {
+                const real x0 = xin[a * ld + m0], xd0 = xind[a * ld + m0];
+                const real x1 = (m0 + 1 < ni) ? xin[a * ld + m0 + 1] : real(0), xd1 = (m0 + 1 < ni) ? xind[a * ld + m0 + 1] : real(0);
+#pragma unroll
+                for (int k = 0; k < RT; ++k) {
+                    const int n = min(n0 + k, no - 1);
+                    const real zv = zb[a * ld + n], zdv = zdb[a * ld + n];
+                    s[k][0] += zv * x0 + zdv * xd0;
+                    s[k][1] += zv * x1 + zdv * xd1;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < RT; ++k) {
+                if (n0 + k >= no) continue;
+                atomicAdd(&A.grad[pbase + wt_at[l] + m0 * no + n0 + k], (double)s[k][0]);
+                if (m0 + 1 < ni) atomicAdd(&A.grad[pbase + wt_at[l] + (m0 + 1) * no + n0 + k], (double)s[k][1]);
+            }
         }
         __syncthreads();
         if (l > 0) {
-            layer_bwd<real, TAT>(A.prm.wt + net.woff[l], no, ni, zb, ab, ld);
-            layer_bwd<real, TAT>(A.prm.wt + net.woff[l], no, ni, zdb, adb, ld);
+            layer_bwd2<real, TAT>(A.prm.wt + net.woff[l], no, ni, zb, zdb, ab, adb, ld);
             __syncthreads();
         }
     }
