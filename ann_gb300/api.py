@@ -445,9 +445,11 @@ class Context:
                                             _d(np.ascontiguousarray(f_ref, np.float64)), w_energy, w_force, prec, _d(loss)))
         return loss
 
-    def train_backward(self, scale=1.0) -> np.ndarray:
-        g = np.zeros(self.nparams)
-        self._ck(self.lib.ann_train_backward(self.h, scale, _d(g), len(g)))
+    def train_backward(self, scale=1.0, download=True):
+        """dL/dp (times scale) as an array; download=False leaves the gradient on the device only
+        (for adam_step) and returns None."""
+        g = np.zeros(self.nparams) if download else None
+        self._ck(self.lib.ann_train_backward(self.h, scale, _d(g), self.nparams))
         return g
 
     def adam_init(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-16):

@@ -1220,25 +1220,36 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
         set_device(c);
         leave_md(c);
         upload_batch(c, nstruc, offs, posn, type, cell, false);
-        run_batch(c, prec, true);
-        finish_batch(c);
         const size_t N = std::max(c->N, 1), S = std::max(c->S, 1), rb = (prec == ANN_FP64) ? 8 : 4;
         c->Eref.ensure(8 * S); c->Fref.ensure(8 * 3 * N); c->loss3.ensure(8 * 4); c->ce.ensure(8 * N);
         c->lam.ensure(rb * 3 * N); c->U.ensure(rb * N * std::max(c->pot.max_input(), 1));
         if (c->S > 0) ck(cudaMemcpyAsync(c->Eref.p, Eref, 8 * (size_t)c->S, cudaMemcpyHostToDevice, c->stream), "H2D Eref");
         if (c->N > 0) ck(cudaMemcpyAsync(c->Fref.p, Fref, 8 * 3 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D Fref");
-        ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
-        launch_train_loss(c->S, c->N, c->off_d, c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
-                          c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->loss3.as<double>(), c->ce.as<double>(), c->lam.p,
-                          prec == ANN_FP64, c->stream);
-        ck(cudaGetLastError(), "loss kernel");
-        ck(cudaMemcpyAsync(loss3, c->loss3.p, 8 * 3, cudaMemcpyDeviceToHost, c->stream), "D2H loss");
+        run_batch(c, prec, true);
+        // the loss right behind the E+F sequence, read back with the status word in one round trip;
+        // a status that is not clean goes through finish_batch (recover or throw) and the loss again
+        auto loss = [&]() {
+            ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
+            launch_train_loss(c->S, c->N, c->off_d, c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
+                              c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->loss3.as<double>(), c->ce.as<double>(), c->lam.p,
+                              prec == ANN_FP64, c->stream);
+            ck(cudaGetLastError(), "loss kernel");
+            ck(cudaMemcpyAsync(loss3, c->loss3.p, 8 * 3, cudaMemcpyDeviceToHost, c->stream), "D2H loss");
+        };
+        loss();
+        int32_t* sh = status_host(c);
+        ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
         ck(cudaStreamSynchronize(c->stream), "synchronize");
+        if (sh[0] != 0) {
+            finish_batch(c);
+            loss();
+            ck(cudaStreamSynchronize(c->stream), "synchronize");
+        }
         c->have_train = true; c->train_prec = prec; c->train_wE = wE; c->train_wF = wF;
     })
 }
 int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
-    if (!c || !grad) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
     ANN_TRY(c, {
         set_device(c);
         if (!c->have_train || !c->have_results) throw ann_error(ANN_ERR_STATE, "ann_train_backward needs a preceding ann_train_forward");
@@ -1259,12 +1270,12 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
         };
         if (c->train_prec == ANN_FP64) go(double()); else go(float());
         ck(cudaGetLastError(), "backward kernels");
-        ck(cudaMemcpyAsync(grad, c->grad.p, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "D2H grad");
+        if (grad) ck(cudaMemcpyAsync(grad, c->grad.p, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "D2H grad");
+        int32_t* sh = status_host(c);
+        ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
         ck(cudaStreamSynchronize(c->stream), "synchronize");
-        int32_t st[8];
-        ck(cudaMemcpy(st, c->status.p, sizeof(st), cudaMemcpyDeviceToHost), "D2H status");
-        if (st[0] != 0) throw ann_error(ANN_ERR_CUDA, "device status " + std::to_string(st[0]) + " in backward pass");
-        for (int64_t k = 0; k < n; ++k) grad[k] *= scale;
+        if (sh[0] != 0) throw ann_error(ANN_ERR_CUDA, "device status " + std::to_string(sh[0]) + " in backward pass");
+        if (grad) for (int64_t k = 0; k < n; ++k) grad[k] *= scale;
         c->have_grad = true;
     })
 }

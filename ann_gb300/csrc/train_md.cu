@@ -19,20 +19,31 @@ template <typename real>
 __global__ void k_train_loss(int nstruc, int natoms, const int32_t* off, const int32_t* sid, const double* Es, const double* Fout,
                              const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* ce, real* lam) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= natoms) return;
-    const int s = sid[a];
-    const double ns = (double)(off[s + 1] - off[s]);
-    const double dU = (Es[s] - Eref[s]) / ns;
-    ce[a] = wE / nstruc * dU / ns;
-    if (a == off[s]) atomicAdd(&loss3[1], 0.5 * dU * dU * wE / nstruc);
-    const double sc = wF / (3.0 * natoms);
-    double l2 = 0.0;
-    for (int c = 0; c < 3; ++c) {
-        const double df = Fout[3 * (size_t)a + c] - Fref[3 * (size_t)a + c];
-        l2 += df * df;
-        lam[3 * (size_t)a + c] = (real)(sc * df);
+    double le = 0.0, lf = 0.0;   // this atom's share of the two loss terms
+    if (a < natoms) {
+        const int s = sid[a];
+        const double ns = (double)(off[s + 1] - off[s]);
+        const double dU = (Es[s] - Eref[s]) / ns;
+        ce[a] = wE / nstruc * dU / ns;
+        if (a == off[s]) le = 0.5 * dU * dU * wE / nstruc;
+        const double sc = wF / (3.0 * natoms);
+        double l2 = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            const double df = Fout[3 * (size_t)a + c] - Fref[3 * (size_t)a + c];
+            l2 += df * df;
+            lam[3 * (size_t)a + c] = (real)(sc * df);
+        }
+        lf = 0.5 * l2 * sc;
     }
-    atomicAdd(&loss3[2], 0.5 * l2 * sc);
+    // one atomic per warp and term (the loss words are shared by the whole batch)
+    for (int o = 16; o > 0; o >>= 1) {
+        le += __shfl_xor_sync(0xffffffffu, le, o);
+        lf += __shfl_xor_sync(0xffffffffu, lf, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (le != 0.0) atomicAdd(&loss3[1], le);
+        atomicAdd(&loss3[2], lf);
+    }
 }
 __global__ void k_train_loss_final(double* loss3) { loss3[0] = loss3[1] + loss3[2]; }
 

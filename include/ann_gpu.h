@@ -194,7 +194,8 @@ int ann_train_forward(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets,
                       const int32_t* type, const double* cell, const double* energy_ref,
                       const double* forces_ref, double w_energy, double w_force, int32_t precision,
                       double* loss3);
-/* dL/dp (reference packing, types in NNP order) scaled by dl_scale. Requires ann_train_forward.  */
+/* dL/dp (reference packing, types in NNP order) scaled by dl_scale. Requires ann_train_forward.
+ * grad may be NULL: the gradient then stays on the device only, for ann_adam_step.               */
 int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t nparams);
 /* Adam optimiser on the device (NN::ADAM::step, opt/algo.cpp:272-296): ann_adam_init sets the
  * step size (gamma), beta1, beta2, eps and zeroes the moments; each ann_adam_step applies one

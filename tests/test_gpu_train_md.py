@@ -155,6 +155,14 @@ def test_adam_steps_on_device(ctx, tmp_path):
         p = p - lr / (1 - b1 ** t) * m / (np.sqrt(v / (1 - b2 ** t)) + eps)
     pd = ctx.get_params()
     assert np.allclose(pd, p, rtol=1e-12, atol=1e-15)
+    # the same three steps with the gradient left on the device (train_backward without download)
+    ctx.load_text(text)
+    ctx.adam_init(lr, b1, b2, eps)
+    for t in range(1, 4):
+        ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+        assert ctx.train_backward(download=False) is None
+        ctx.adam_step()
+    assert np.allclose(ctx.get_params(), pd, rtol=1e-12, atol=1e-15)   # gradient sums are atomic: last bits vary
     other = Context()
     try:
         other.load_text(text)
