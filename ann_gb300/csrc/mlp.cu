@@ -20,6 +20,7 @@ namespace ann {
 constexpr int TA = 32;        // atoms per block (energy/force network pass)
 constexpr int TAT = 16;       // atoms per block (training pass, more state per atom)
 constexpr int MLP_T = 128;    // threads per block
+constexpr int MLP_TT = 256;   // threads per block of the training pass (two blocks per SM fit its shared memory)
 
 // map block -> (type, first atom in the type list); returns false if the block is spare
 template <int TAn>
@@ -70,7 +71,7 @@ template <typename real, int TAn>
 __device__ __forceinline__ void layer_fwd2(const real* __restrict__ Wl, const real* __restrict__ bl, int no, int ni,
                                            const real* x, const real* xd, real* z, real* zd, int ld) {
     const int ng = (no + RT - 1) / RT;
-    for (int idx = threadIdx.x; idx < TAn * ng; idx += MLP_T) {
+    for (int idx = threadIdx.x; idx < TAn * ng; idx += blockDim.x) {
         const int a = idx % TAn, n0 = (idx / TAn) * RT;
         const real* xr = x + a * ld;
         const real* xdr = xd + a * ld;
@@ -96,7 +97,7 @@ template <typename real, int TAn>
 __device__ __forceinline__ void layer_bwd2(const real* __restrict__ WTl, int no, int ni, const real* x, const real* xd, real* y,
                                            real* yd, int ld) {
     const int mg = (ni + RT - 1) / RT;
-    for (int idx = threadIdx.x; idx < TAn * mg; idx += MLP_T) {
+    for (int idx = threadIdx.x; idx < TAn * mg; idx += blockDim.x) {
         const int a = idx % TAn, m0 = (idx / TAn) * RT;
         const real* xr = x + a * ld;
         const real* xdr = xd + a * ld;
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_fb(const __grid_constant__ DevPot
 
 // ---------------------------------------------------------------- training: d/dp [ce E + ct dE/dG . u]
 template <typename real>
-__global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ DevPot pot, const MlpArgs<real> A, int ld) {
+__global__ void __launch_bounds__(MLP_TT) k_mlp_train(const __grid_constant__ DevPot pot, const MlpArgs<real> A, int ld) {
     extern __shared__ __align__(16) unsigned char msm[];
     int type, a0, na;
     if (!tile_of_block<TAT>(A.ntypes, A.tstart, type, a0, na)) return;
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
     const int nin = net.nin;
     const real* inpw = A.prm.inpw + net.inoff;
     const real* inpb = A.prm.inpb + net.inoff;
-    for (int idx = threadIdx.x; idx < TAT * nin; idx += MLP_T) {
+    for (int idx = threadIdx.x; idx < TAT * nin; idx += blockDim.x) {
         const int a = idx / nin, m = idx % nin;
         const int at = atoms[a];
         act[a * ld + m] = (at >= 0) ? inpw[m] * (A.G[(size_t)at * A.imax + m] + inpb[m]) : real(0);
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
         layer_fwd2<real, TAT>(A.prm.w + net.woff[l], A.prm.b + net.boff[l], no, ni, xin, xind, xo, xod, ld);
         __syncthreads();
         const int actn = (l == L - 1) ? (int)N_LINEAR : net.neuron;
-        for (int idx = threadIdx.x; idx < TAT * no; idx += MLP_T) {
+        for (int idx = threadIdx.x; idx < TAT * no; idx += blockDim.x) {
             const int a = idx % TAT, n = idx / TAT;
             real av, f1, f2;
             act_fd<real>(actn, c, xo[a * ld + n], av, f1, f2);
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
         __syncthreads();
     }
     // seeds at the output: abar_L = ce*outw, adbar_L = ct*outw
-    for (int a = threadIdx.x; a < TAT; a += MLP_T) {
+    for (int a = threadIdx.x; a < TAT; a += blockDim.x) {
         ab[a * ld] = (real)(ce[a] * net.outw);
         adb[a * ld] = (atoms[a] >= 0) ? (real)(A.ct * net.outw) : real(0);
     }
@@ -265,7 +266,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
     }
     for (int l = L - 1; l >= 0; --l) {
         const int no = net.nodes[l], ni = (l == 0) ? nin : net.nodes[l - 1];
-        for (int idx = threadIdx.x; idx < TAT * no; idx += MLP_T) {
+        for (int idx = threadIdx.x; idx < TAT * no; idx += blockDim.x) {
             const int a = idx % TAT, n = idx / TAT;
             const real f1 = d1[(size_t)l * tl + a * ld + n], f2 = d2[(size_t)l * tl + a * ld + n];
             const real adbv = adb[a * ld + n];
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
         __syncthreads();
         // bias gradient: sum over the tile's atoms of zbar, in the pass's precision (the products
         // are formed in it), then added to the FP64 gradient
-        for (int n = threadIdx.x; n < no; n += MLP_T) {
+        for (int n = threadIdx.x; n < no; n += blockDim.x) {
             real s = real(0);
             for (int a = 0; a < TAT; ++a) s += zb[a * ld + n];
             atomicAdd(&A.grad[pbase + bias_at[l] + n], (double)s);
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(MLP_T) k_mlp_train(const __grid_constant__ Dev
         const real* xin = act + (size_t)l * tl;
         const real* xind = actd + (size_t)l * tl;
         const int ngw = (no + RT - 1) / RT, mgw = (ni + 1) / 2;
-        for (int idx = threadIdx.x; idx < ngw * mgw; idx += MLP_T) {
+        for (int idx = threadIdx.x; idx < ngw * mgw; idx += blockDim.x) {
             const int n0 = (idx % ngw) * RT, m0 = (idx / ngw) * 2;
             real s[RT][2];
 #pragma unroll
@@ -342,7 +343,7 @@ void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream
     const int L = mlp_maxL(pot);
     const size_t smem = (size_t)(2 * (L + 1) + 3 * L + 4) * TAT * ld * sizeof(real);
     const int grid = (a.natoms + TAT - 1) / TAT + a.ntypes;
-    ++::ann::g_launch_counter, k_mlp_train<real><<<grid, MLP_T, smem, st>>>(pot, a, ld);
+    ++::ann::g_launch_counter, k_mlp_train<real><<<grid, MLP_TT, smem, st>>>(pot, a, ld);
 }
 void configure_mlp(int maxsmem) {
     set_max_dynamic_smem(k_mlp_fb<float>, maxsmem);
