@@ -274,9 +274,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nstruc", type=int, default=256)
     ap.add_argument("--no-extras", action="store_true", help="skip the training and MD legs")
+    ap.add_argument("--only", choices=["training", "md", "lammps"],
+                    help="run one secondary leg alone with --steps / --warmup and print its JSON (for profiling)")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     W_ = max(args.warmup, 3)
+    if args.only:
+        leg = {"training": training_leg, "md": md_leg, "lammps": lammps_leg}[args.only]
+        print(json.dumps({args.only: leg(local if world > 1 else 0, steps=args.steps, warmup=args.warmup)}))
+        return
 
     from ann_gb300 import workloads as WL
     from ann_gb300.api import pack_batch
