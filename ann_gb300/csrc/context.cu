@@ -111,6 +111,8 @@ struct GraphKey {
 struct ann_ctx {
     ann_options opt;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;                 // fork / join branch of the E+F sequence
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
     bool have_pot = false;
     Potential pot;
@@ -447,13 +449,26 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     cudaStream_t st = c->stream;
     const bool fp64 = std::is_same<real, double>::value;
     const DevPot& pot = c->plan.pot;
+    // the per-type atom lists depend on the types only: outside the phase-timed and debug modes
+    // they run on a side stream that forks here and joins before the networks (a parallel branch
+    // of the captured graph, beside the neighbour search and the symmetry functions)
+    const bool side = !c->profile && !c->debug;
+    auto type_lists = [&](cudaStream_t s) {
+        launch_type_lists(c->N, c->pot.ntypes(), c->type.as<int32_t>(), c->tcount.as<int32_t>(), c->tstart.as<int32_t>(),
+                          c->tlist.as<int32_t>(), c->status.as<int32_t>(), s);
+    };
+    if (side) {
+        ck(cudaEventRecord(c->ev_fork, st), "event record");
+        ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "stream wait");
+        type_lists(c->side);
+        ck(cudaEventRecord(c->ev_join, c->side), "event record");
+    }
     mark(c, 0);
     if (build_list) launch_neighbors(nbr_args(c, c->pot.rc + (c->md_ready ? c->md_skin : 0.0)), fp64, st);
     else launch_refresh_geometry(nbr_args(c, c->pot.rc + c->md_skin), fp64, st);
     check_phase(c, "neighbour list");
     mark(c, 1);
-    launch_type_lists(c->N, c->pot.ntypes(), c->type.as<int32_t>(), c->tcount.as<int32_t>(), c->tstart.as<int32_t>(), c->tlist.as<int32_t>(),
-                      c->status.as<int32_t>(), st);
+    if (!side) type_lists(st);
     check_phase(c, "type lists");
     mark(c, 2);
     BpArgs<real> b = bp_args<real>(c);
@@ -461,6 +476,7 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     launch_symm<real>(pot, b, st);
     check_phase(c, "symmetry functions");
     mark(c, 3);
+    if (side) ck(cudaStreamWaitEvent(st, c->ev_join, 0), "stream wait");
     enqueue_networks<real>(c, c->N, c->G, c->dEdG, c->Eatom, c->tstart, c->tlist, b.prm);
     check_phase(c, "networks");
     mark(c, 4);
@@ -582,6 +598,9 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         if (c->opt.device < 0 || c->opt.device >= n) throw ann_error(ANN_ERR_CUDA, "CUDA device " + std::to_string(c->opt.device) + " not available");
         set_device(c);
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream create");
+        ck(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream create");
+        ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event create");
+        ck(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event create");
         configure_kernels();
         cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->opt.device);
         cudaDeviceGetAttribute(&c->tc.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->opt.device);
@@ -590,6 +609,10 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         c->debug = dbg && dbg[0] == '1';
         if (c->debug) c->opt.use_graphs = 0;
     } catch (ann_error& e) {
+        if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->side) cudaStreamDestroy(c->side);
+        if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+        if (c->ev_join) cudaEventDestroy(c->ev_join);
         delete c;
         return fail(nullptr, e.code, e.what());
     }
@@ -616,6 +639,9 @@ int ann_destroy(ann_ctx* c) {
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     if (c->status_h) cudaFreeHost(c->status_h);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     delete c;
     return ANN_OK;
 }
