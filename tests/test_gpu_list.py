@@ -196,3 +196,29 @@ def test_keep_list_between_reneighbourings(ctx, oracle, tmp_path):
             c2.compute_list(x1, None, None, None, precision=FP64, keep=True, inum=dom.nlocal)
     finally:
         c2.close()
+
+
+def test_large_domain_matches_periodic_batch(gpu_lib, tmp_path):
+    """A 16,384-atom FCC box as an MD engine's domain (k-d tree ghosts, full list with a 2 A skin,
+    as the LAMMPS-shaped bench leg builds it): the list call gives the periodic box's energy and,
+    after folding the ghost forces, its forces, in FP64 and in mixed precision."""
+    pytest.importorskip("scipy")
+    c = Context()
+    try:
+        cases.W.make_potential(c, 5)
+        x, R = cases.W.fcc(16, 16, 16, 5.26)
+        rng = np.random.default_rng(12)
+        x = x + rng.normal(0.0, 0.05, x.shape)
+        t = np.zeros(len(x), np.int32)
+        X, T, owner, nn, nb = cases.W.ghost_domain(x, t, R, c.rc + 2.0)
+        offs, posn, types, cell = cases.batch([(X[:len(t)], t, R)])
+        for prec, tol_e, tol_f in ((FP64, 1e-11, 1e-9), (MIXED, 1e-6, 2e-3)):
+            E0, F0, W0 = c.compute(offs, posn, types, cell, precision=prec)
+            E, F, Wv, _ = c.compute_list(X, T, nn, nb, precision=prec)
+            Ff = np.zeros((len(t), 3))
+            np.add.at(Ff, owner, F)
+            assert abs(E - E0[0]) <= tol_e * abs(E0[0]), (prec, E, E0[0])
+            assert np.max(np.abs(Ff - F0)) <= tol_f * max(np.max(np.abs(F0)), 1.0), prec
+            assert np.max(np.abs(Wv - W0[0])) <= tol_f * np.max(np.abs(W0[0])), prec
+    finally:
+        c.close()
