@@ -71,16 +71,22 @@ __global__ void __launch_bounds__(SETUP_T) k_struc_setup(NbrArgs a) {
         a.geo[s] = g;
         local += g.nb[0] * g.nb[1] * g.nb[2];
     }
-    part[threadIdx.x] = local;
+    // exclusive prefix of the SETUP_T partials: inclusive scan inside each warp, then over the
+    // warp totals
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) { const int32_t v = __shfl_up_sync(0xffffffffu, incl, o); if (lane >= o) incl += v; }
+    if (lane == 31) part[wid] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {  // serial prefix over the SETUP_T partials
+    if (threadIdx.x == 0) {
         int32_t run = 0;
-        for (int t = 0; t < (int)blockDim.x; ++t) { const int32_t v = part[t]; part[t] = run; run += v; }
+        for (int w = 0; w < SETUP_T / 32; ++w) { const int32_t v = part[w]; part[w] = run; run += v; }
         *a.nbins_total = run;
         if (run > a.nbins_cap) atomicOr(a.status, (int)ST_NBR_OVERFLOW);
     }
     __syncthreads();
-    int32_t run = part[threadIdx.x];
+    int32_t run = part[wid] + incl - local;
     for (int s = lo; s < hi; ++s) { a.geo[s].bin0 = run; run += a.geo[s].nb[0] * a.geo[s].nb[1] * a.geo[s].nb[2]; }
 }
 
