@@ -68,6 +68,7 @@ _SIGS = {
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
     "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_train_set_loss": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_double]),
     "ann_host_alloc": (C.c_int, [_V, C.c_int64, C.POINTER(C.c_void_p)]),
     "ann_host_free": (C.c_int, [_V, C.c_void_p]),
     "ann_compute_list": (C.c_int, [_V, C.c_int32, _I32, _I32, _I32, C.c_int32, _D, _I32, _D, _D, _D, _D, C.c_int32, C.c_int32]),
@@ -444,6 +445,15 @@ class Context:
                                             _d(np.ascontiguousarray(cell, np.float64)), _d(np.ascontiguousarray(e_ref, np.float64)),
                                             _d(np.ascontiguousarray(f_ref, np.float64)), w_energy, w_force, prec, _d(loss)))
         return loss
+
+    LOSS = {"MSE": 1, "MAE": 2, "HUBER": 3, "ASINH": 4}
+    NORM = {"IDENTITY": 0, "LINEAR": 1, "SQRT": 2, "CBRT": 3, "LOG": 4}
+
+    def train_set_loss(self, loss="MSE", norm="LINEAR", delta=1.0):
+        """Energy term of the training loss (the reference trainer's LOSS / NORM / DELTA)."""
+        lo = self.LOSS[loss] if isinstance(loss, str) else int(loss)
+        no = self.NORM[norm] if isinstance(norm, str) else int(norm)
+        self._ck(self.lib.ann_train_set_loss(self.h, lo, no, float(delta)))
 
     def train_backward(self, scale=1.0, download=True):
         """dL/dp (times scale) as an array; download=False leaves the gradient on the device only

@@ -28,8 +28,8 @@
 namespace ann {
 // training loss / adjoint seeds (train.cu)
 void launch_train_loss(int nstruc, int natoms, const int32_t* off, const int32_t* sid, const double* Es, const double* Fout,
-                       const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* ce, void* lam,
-                       bool fp64, cudaStream_t st);
+                       const double* Eref, const double* Fref, double wE, double wF, int lossf, int norm, double delta, double* loss3,
+                       double* ce, void* lam, bool fp64, cudaStream_t st);
 void launch_md_kick_drift(int natoms, double* pos, double* vel, const void* F, bool fp64, const double* minv, const int32_t* type,
                           double dt, const double* R, const double* Ri, double* disp_ref, int32_t* maxdisp_flag, double half_skin2,
                           int stage, cudaStream_t st);
@@ -141,6 +141,8 @@ struct ann_ctx {
     bool have_train = false;
     int train_prec = 0;
     double train_wE = 0, train_wF = 0;
+    int train_loss = ANN_LOSS_MSE, train_norm = ANN_NORM_LINEAR;   // energy term (ann_train_set_loss)
+    double train_delta = 1.0;
     // MD
     bool md_ready = false;
     int md_prec = 0;

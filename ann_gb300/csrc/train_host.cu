@@ -145,8 +145,8 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
         auto loss = [&]() {
             ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
             launch_train_loss(c->S, c->N, c->off_d, c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
-                              c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->loss3.as<double>(), c->ce.as<double>(), c->lam.p,
-                              prec == ANN_FP64, c->stream);
+                              c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->train_loss, c->train_norm, c->train_delta,
+                              c->loss3.as<double>(), c->ce.as<double>(), c->lam.p, prec == ANN_FP64, c->stream);
             ck(cudaGetLastError(), "loss kernel");
             ck(cudaMemcpyAsync(loss3, c->loss3.p, 8 * 3, cudaMemcpyDeviceToHost, c->stream), "D2H loss");
         };
@@ -161,6 +161,14 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
         }
         c->have_train = true; c->train_prec = prec; c->train_wE = wE; c->train_wF = wF;
     })
+}
+int ann_train_set_loss(ann_ctx* c, int32_t loss, int32_t norm, double delta) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (loss < ANN_LOSS_MSE || loss > ANN_LOSS_ASINH) return fail(c, ANN_ERR_ARG, "Invalid loss function.");
+    if (norm < ANN_NORM_IDENTITY || norm > ANN_NORM_LOG) return fail(c, ANN_ERR_ARG, "Invalid normalization method.");
+    if (!(std::isfinite(delta) && delta > 0.0)) return fail(c, ANN_ERR_ARG, "delta must be finite and > 0");
+    c->train_loss = loss; c->train_norm = norm; c->train_delta = delta;
+    return ANN_OK;
 }
 int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");

@@ -1,10 +1,10 @@
 // Training-loss seeds (K6 entry) and the velocity-Verlet integrator (K7).
 //
-// Loss (nnptefr2.cpp:1321-1374 energy term with MSE / LINEAR normalisation averaged over the batch
-// as nnptefr2.cpp:984-995; force term as intended by nnptef.cpp:1715-1825):
-//   L = wE/S sum_s 1/2 ((E_s-Eref_s)/N_s)^2 + wF/(3N) sum_a 1/2 |F_a-Fref_a|^2
-// Seeds for the adjoint pass: ce_i = dL/dE_s(i) = wE/S (E_s-Eref_s)/N_s^2 for every atom i of s,
-// lam_a = dL/dF_a = wF/(3N) (F_a - Fref_a).
+// Loss (nnptefr2.cpp:1321-1374 energy term, any of its losses and normalisations, averaged over
+// the batch as nnptefr2.cpp:984-995; force term as intended by nnptef.cpp:1715-1825):
+//   L = wE/S sum_s loss(dU_s) + wF/(3N) sum_a 1/2 |F_a-Fref_a|^2,  dU_s = (E_s-Eref_s) normt(N_s)
+// (MSE / LINEAR: loss = 1/2 dU^2, normt = 1/N). Seeds for the adjoint pass: ce_i = dL/dE_s(i) =
+// wE/S d loss/dE_s for every atom i of s, lam_a = dL/dF_a = wF/(3N) (F_a - Fref_a).
 //
 // MD: Verlet::compute (src/torch/integrator.cpp:177-200) in metal units (x A, v A/fs, dt fs,
 // m Da, F eV/A; a = F/(m mvv_to_e), mvv_to_e = 103.642696526805, src/chem/units.cpp:151).
@@ -15,17 +15,44 @@
 
 namespace ann {
 
+// energy term of one structure (nnptefr2.cpp:1339-1368, normalisation 606-612): the loss and
+// gfac = d loss / dE for loss 1 MSE, 2 MAE, 3 HUBER, 4 ASINH and norm 0 IDENTITY, 1 LINEAR, 2 SQRT,
+// 3 CBRT, 4 LOG
+__device__ __forceinline__ void energy_loss(int lossf, int norm, double delta, double dE, double ns, double& L, double& gfac) {
+    double normt = 1.0;
+    switch (norm) {
+        case 1: normt = 1.0 / ns; break;
+        case 2: normt = 1.0 / sqrt(ns); break;
+        case 3: normt = 1.0 / cbrt(ns); break;
+        case 4: normt = 1.0 / (log(ns) + 1.0); break;
+        default: break;
+    }
+    const double dU = dE * normt, deltai = 1.0 / delta;
+    gfac = normt;
+    switch (lossf) {
+        case 2: L = fabs(dU); gfac *= (double)((dU > 0) - (dU < 0)); break;
+        case 3: { const double arg = dU * deltai, sq = sqrt(1.0 + arg * arg); L = delta * delta * (sq - 1.0); gfac *= dU / sq; } break;
+        case 4: {
+            const double arg = dU * deltai, sq = sqrt(1.0 + arg * arg), lg = log(arg + sq);
+            L = delta * delta * (1.0 - sq + arg * lg); gfac *= lg * delta;
+        } break;
+        default: L = 0.5 * dU * dU; gfac *= dU; break;
+    }
+}
+
 template <typename real>
 __global__ void k_train_loss(int nstruc, int natoms, const int32_t* off, const int32_t* sid, const double* Es, const double* Fout,
-                             const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* ce, real* lam) {
+                             const double* Eref, const double* Fref, double wE, double wF, int lossf, int norm, double delta,
+                             double* loss3, double* ce, real* lam) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     double le = 0.0, lf = 0.0;   // this atom's share of the two loss terms
     if (a < natoms) {
         const int s = sid[a];
         const double ns = (double)(off[s + 1] - off[s]);
-        const double dU = (Es[s] - Eref[s]) / ns;
-        ce[a] = wE / nstruc * dU / ns;
-        if (a == off[s]) le = 0.5 * dU * dU * wE / nstruc;
+        double Ls, gfac;
+        energy_loss(lossf, norm, delta, Es[s] - Eref[s], ns, Ls, gfac);
+        ce[a] = wE / nstruc * gfac;
+        if (a == off[s]) le = wE / nstruc * Ls;
         const double sc = wF / (3.0 * natoms);
         double l2 = 0.0;
         for (int c = 0; c < 3; ++c) {
@@ -48,12 +75,16 @@ __global__ void k_train_loss(int nstruc, int natoms, const int32_t* off, const i
 __global__ void k_train_loss_final(double* loss3) { loss3[0] = loss3[1] + loss3[2]; }
 
 void launch_train_loss(int nstruc, int natoms, const int32_t* off, const int32_t* sid, const double* Es, const double* Fout,
-                       const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* ce, void* lam,
-                       bool fp64, cudaStream_t st) {
+                       const double* Eref, const double* Fref, double wE, double wF, int lossf, int norm, double delta, double* loss3,
+                       double* ce, void* lam, bool fp64, cudaStream_t st) {
     if (natoms > 0) {
         const int g = (natoms + 255) / 256;
-        if (fp64) ++::ann::g_launch_counter, k_train_loss<double><<<g, 256, 0, st>>>(nstruc, natoms, off, sid, Es, Fout, Eref, Fref, wE, wF, loss3, ce, (double*)lam);
-        else ++::ann::g_launch_counter, k_train_loss<float><<<g, 256, 0, st>>>(nstruc, natoms, off, sid, Es, Fout, Eref, Fref, wE, wF, loss3, ce, (float*)lam);
+        if (fp64)
+            ++::ann::g_launch_counter, k_train_loss<double><<<g, 256, 0, st>>>(nstruc, natoms, off, sid, Es, Fout, Eref, Fref, wE, wF, lossf,
+                                                                               norm, delta, loss3, ce, (double*)lam);
+        else
+            ++::ann::g_launch_counter, k_train_loss<float><<<g, 256, 0, st>>>(nstruc, natoms, off, sid, Es, Fout, Eref, Fref, wE, wF, lossf,
+                                                                              norm, delta, loss3, ce, (float*)lam);
     }
     ++::ann::g_launch_counter, k_train_loss_final<<<1, 1, 0, st>>>(loss3);
 }

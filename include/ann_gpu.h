@@ -186,7 +186,7 @@ int ann_get_neighbors(ann_ctx* ctx, int32_t* i_out, int32_t* j_out, int32_t* img
                       double* r_out /* 3 per, FP64 pipelines only else NULL */, int64_t cap);
 
 /* ---- training: forward/backward pair (the contract of a torch.autograd.Function) ------------ */
-/* L = wE/S sum_s 1/2 ((E_s-Eref_s)/N_s)^2 + wF/(3N) sum_a 1/2 |F_a-Fref_a|^2
+/* L = wE/S sum_s 1/2 ((E_s-Eref_s)/N_s)^2 + wF/(3N) sum_a 1/2 |F_a-Fref_a|^2 (energy term: see ann_train_set_loss)
  * (energy term = NNPTEFR::error_cost_o1 MSE/LINEAR, nnptefr2.cpp:1321-1374 + 984-995;
  *  force term = the intent of NNPTE::error, nnptef.cpp:1715-1825, with all neighbour terms).
  * loss3 = {L, L_E, L_F}. Saves the state the backward pass needs on the device.                 */
@@ -194,6 +194,16 @@ int ann_train_forward(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets,
                       const int32_t* type, const double* cell, const double* energy_ref,
                       const double* forces_ref, double w_energy, double w_force, int32_t precision,
                       double* loss3);
+/* The energy term's loss and normalisation for later ann_train_forward calls (NNPTEFR,
+ * nnptefr2.cpp:1339-1368, normalisation 606-612). For structure s with dU = (E_s - Eref_s) normt(N_s):
+ * MSE 1/2 dU^2, MAE |dU|, HUBER delta^2 (sqrt(1 + (dU/delta)^2) - 1), ASINH delta^2 (1 - sqrt(1 + a^2)
+ * + a asinh(a)) with a = dU/delta; normt = 1, 1/N, 1/sqrt(N), 1/cbrt(N), 1/(ln N + 1). The
+ * energy term of L is wE/S sum_s loss_s. The default is MSE with LINEAR. The force term stays the
+ * mean squared error. Enum values are those of opt::Loss (opt/loss.hpp:18-24) and Norm
+ * (nnptefr2.hpp:119-126).                                                                         */
+enum ann_loss { ANN_LOSS_MSE = 1, ANN_LOSS_MAE = 2, ANN_LOSS_HUBER = 3, ANN_LOSS_ASINH = 4 };
+enum ann_norm { ANN_NORM_IDENTITY = 0, ANN_NORM_LINEAR = 1, ANN_NORM_SQRT = 2, ANN_NORM_CBRT = 3, ANN_NORM_LOG = 4 };
+int ann_train_set_loss(ann_ctx* ctx, int32_t loss, int32_t norm, double delta);
 /* dL/dp (reference packing, types in NNP order) scaled by dl_scale. Requires ann_train_forward.
  * grad may be NULL: the gradient then stays on the device only, for ann_adam_step.               */
 int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t nparams);

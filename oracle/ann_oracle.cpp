@@ -1096,8 +1096,40 @@ int orc_compute(void* pp, int nstruc, const long long* off, const double* x, con
 // Force term (nnptef.cpp:1715-1825 intent, all neighbour terms included):
 //   L_F = wF/(3 Ntot) * sum_a 1/2 |F_a - Fref_a|^2
 // loss3 = {L, L_E, L_F}; grad += dL/dp.
-int orc_train(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
-              const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* grad) {
+// Energy term of one structure (nnptefr2.cpp:1339-1368) with its normalisation normt
+// (nnptefr2.cpp:606-612): loss 1 MSE, 2 MAE, 3 HUBER, 4 ASINH (opt/loss.hpp:18-24; HUBER and ASINH with
+// the scale delta, used as 1/delta and delta^2 as nnptefr2.cpp:188-189); norm 0 IDENTITY, 1 LINEAR,
+// 2 SQRT, 3 CBRT, 4 LOG (nnptefr2.hpp:119-126). L = the structure's loss, gfac = dL/dE.
+static void energy_loss(int loss, int norm, double delta, double dE, double nAtoms, double& L, double& gfac) {
+    double normt;
+    switch (norm) {
+        case 0: normt = 1.0; break;
+        case 1: normt = 1.0 / nAtoms; break;
+        case 2: normt = 1.0 / std::sqrt(nAtoms); break;
+        case 3: normt = 1.0 / std::cbrt(nAtoms); break;
+        case 4: normt = 1.0 / (std::log(nAtoms) + 1.0); break;
+        default: throw std::invalid_argument("Invalid normalization method.");
+    }
+    const double dU = dE * normt, deltai = 1.0 / delta, delta2 = delta * delta;
+    gfac = normt;
+    switch (loss) {
+        case 1: L = 0.5 * dU * dU; gfac *= dU; break;
+        case 2: L = std::fabs(dU); gfac *= (double)((dU > 0) - (dU < 0)); break;
+        case 3: {
+            const double arg = dU * deltai, sq = std::sqrt(1.0 + arg * arg);
+            L = delta2 * (sq - 1.0); gfac *= dU / sq;
+        } break;
+        case 4: {
+            const double arg = dU * deltai, sq = std::sqrt(1.0 + arg * arg), lg = std::log(arg + sq);
+            L = delta2 * (1.0 - sq + arg * lg); gfac *= lg * delta;
+        } break;
+        default: throw std::invalid_argument("Invalid loss function.");
+    }
+}
+
+int orc_train_ex(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
+                 const double* Eref, const double* Fref, double wE, double wF, int loss, int norm, double delta, double* loss3,
+                 double* grad) {
     try {
         NNP& p = *(NNP*)pp;
         const int P = p.nparams();
@@ -1113,9 +1145,10 @@ int orc_train(void* pp, int nstruc, const long long* off, const double* x, const
             compute_symm(p, s);
             std::vector<double> F(3 * (size_t)s.N);
             const double E = compute_force(p, s, F.data(), nullptr, 1);
-            const double dU = (E - Eref[si]) / s.N;
-            LE += 0.5 * dU * dU;
-            const double ce = wE / nstruc * dU / s.N;
+            double Ls, gfac;
+            energy_loss(loss, norm, delta, E - Eref[si], (double)s.N, Ls, gfac);
+            LE += Ls;
+            const double ce = wE / nstruc * gfac;
             std::vector<double> lam(3 * (size_t)s.N);
             for (int a = 0; a < 3 * s.N; ++a) {
                 const double df = F[a] - Fref[3 * off[si] + a];
@@ -1137,11 +1170,17 @@ int orc_train(void* pp, int nstruc, const long long* off, const double* x, const
     } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
 
-// NNPTEFR::error_cost_o1 restated literally (energy only, MSE, LINEAR norm, nnptefr2.cpp:1321-1374),
+int orc_train(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
+              const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* grad) {
+    return orc_train_ex(pp, nstruc, off, x, type, cell, Eref, Fref, wE, wF, 1, 1, 1.0, loss3, grad);
+}
+
+// NNPTEFR::error_cost_o1 restated literally (energy only, nnptefr2.cpp:1321-1374; MSE, LINEAR norm
+// unless given),
 // followed by the batch average of nnptefr2.cpp:984-995. Eref excludes vacuum energies, as the
 // structure energies the trainer compares against (the network outputs only are summed, 1337).
-int orc_error_cost_o1(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
-                      const double* Eref, double* loss, double* grad) {
+int orc_error_cost_o1_ex(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
+                         const double* Eref, int lossf, int norm, double delta, double* loss, double* grad) {
     try {
         NNP& p = *(NNP*)pp;
         const int P = p.nparams();
@@ -1161,17 +1200,19 @@ int orc_error_cost_o1(void* pp, int nstruc, const long long* off, const double* 
                 pe += p.h[t].nn.forward(s.symm[i].data());
                 p.h[t].nn.cost_grad(1.0, gs.data() + poff[t]);
             }
-            const double normt = 1.0 / s.N;
-            const double dE = pe - Eref[si];
-            const double dU = dE * normt;
-            err += 0.5 * dU * dU;
-            const double gfac = normt * dU;
+            double Ls, gfac;
+            energy_loss(lossf, norm, delta, pe - Eref[si], (double)s.N, Ls, gfac);
+            err += Ls;
             for (int k = 0; k < P; ++k) g[k] += gs[k] * gfac;
         }
         *loss = err / nstruc;
         for (int k = 0; k < P; ++k) grad[k] = g[k] / nstruc;
         return 0;
     } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+int orc_error_cost_o1(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
+                      const double* Eref, double* loss, double* grad) {
+    return orc_error_cost_o1_ex(pp, nstruc, off, x, type, cell, Eref, 1, 1, 1.0, loss, grad);
 }
 
 // u = J lam for a batch (tangent of the symmetry functions), rows padded to imax

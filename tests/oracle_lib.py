@@ -69,6 +69,8 @@ class Oracle:
         L.orc_compute.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int]
         L.orc_train.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_double, C.c_double, _D, _D]
         L.orc_error_cost_o1.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, _D]
+        L.orc_error_cost_o1_ex.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, C.c_int, C.c_int, C.c_double, _D, _D]
+        L.orc_train_ex.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_double, C.c_double, C.c_int, C.c_int, C.c_double, _D, _D]
         L.orc_symm_jvp.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_int]
         L.orc_lj.restype = C.c_double
         L.orc_lj.argtypes = [C.c_int, _D, _D, C.c_double, C.c_double, C.c_double, _D]
@@ -201,24 +203,29 @@ class Potential:
             raise RuntimeError(self.o.err())
         return E, F, W, G, D
 
-    def train(self, offs, posn, types, cell, e_ref, f_ref, wE=1.0, wF=0.1):
+    def train(self, offs, posn, types, cell, e_ref, f_ref, wE=1.0, wF=0.1, loss=1, norm=1, delta=1.0):
+        """Loss (L, L_E, L_F) and dL/dp; loss 1 MSE, 2 MAE, 3 HUBER, 4 ASINH; norm 0 IDENTITY,
+        1 LINEAR, 2 SQRT, 3 CBRT, 4 LOG (the energy term)."""
         offs = np.ascontiguousarray(offs, np.int64)
-        loss = np.zeros(3)
+        lossv = np.zeros(3)
         g = np.zeros(self.nparams)
-        rc = self.L.orc_train(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
-                              _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
-                              _d(np.ascontiguousarray(e_ref, np.float64)), _d(np.ascontiguousarray(f_ref, np.float64)), wE, wF, _d(loss), _d(g))
+        rc = self.L.orc_train_ex(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
+                                 _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
+                                 _d(np.ascontiguousarray(e_ref, np.float64)), _d(np.ascontiguousarray(f_ref, np.float64)), wE, wF,
+                                 loss, norm, delta, _d(lossv), _d(g))
+        loss = lossv
         if rc != 0:
             raise RuntimeError(self.o.err())
         return loss, g
 
-    def error_cost_o1(self, offs, posn, types, cell, e_ref):
+    def error_cost_o1(self, offs, posn, types, cell, e_ref, loss=1, norm=1, delta=1.0):
         offs = np.ascontiguousarray(offs, np.int64)
-        loss = np.zeros(1)
+        lossv = np.zeros(1)
         g = np.zeros(self.nparams)
-        rc = self.L.orc_error_cost_o1(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
-                                      _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
-                                      _d(np.ascontiguousarray(e_ref, np.float64)), _d(loss), _d(g))
+        rc = self.L.orc_error_cost_o1_ex(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
+                                         _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
+                                         _d(np.ascontiguousarray(e_ref, np.float64)), loss, norm, delta, _d(lossv), _d(g))
+        loss = lossv
         if rc != 0:
             raise RuntimeError(self.o.err())
         return loss[0], g

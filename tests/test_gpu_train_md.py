@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import cases
-from ann_gb300 import FP64, MIXED, Context
+from ann_gb300 import FP64, MIXED, AnnError, Context
 from ann_gb300 import workloads as W
 from ann_gb300.api import pack_batch
 
@@ -59,6 +59,36 @@ def test_gradient_matches_oracle(ctx, oracle, tmp_path, wE, wF):
     ctx.train_forward(offs, posn, types, cell, Eref, Fref, wE, wF, precision=MIXED)
     gm = ctx.train_backward()
     assert np.abs(gm - g).max() <= 1e-3 * scale
+
+
+@pytest.mark.parametrize("loss", ["MSE", "MAE", "HUBER", "ASINH"])
+def test_loss_variants_match_oracle(ctx, oracle, tmp_path, loss):
+    """The trainer's energy losses (MSE, MAE, HUBER, ASINH) under every normalisation (IDENTITY,
+    LINEAR, SQRT, CBRT, LOG) with the force term on: loss and gradient vs the oracle in FP64, the
+    mixed gradient near FP64, and the setting left as found for the other tests."""
+    text = cases.config_potential(ctx, 3, tmp_path)
+    pot = oracle.load_text(text)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    try:
+        for norm in range(5):
+            ctx.train_set_loss(loss, norm, delta=0.5)
+            lo, go = pot.train(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, loss=ctx.LOSS[loss], norm=norm, delta=0.5)
+            l3 = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+            g = ctx.train_backward()
+            assert np.allclose(l3, lo, rtol=1e-10, atol=1e-14), (loss, norm)
+            assert np.abs(g - go).max() <= 1e-9 * np.abs(go).max(), (loss, norm)
+            if norm == 1:
+                ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=MIXED)
+                gm = ctx.train_backward()
+                assert np.abs(gm - go).max() <= 2e-3 * np.abs(go).max(), loss
+        with pytest.raises(AnnError, match="loss"):
+            ctx.train_set_loss(5, 1)
+        with pytest.raises(AnnError, match="normalization"):
+            ctx.train_set_loss(loss, 5)
+        with pytest.raises(AnnError, match="delta"):
+            ctx.train_set_loss(loss, 1, delta=0.0)
+    finally:
+        ctx.train_set_loss("MSE", "LINEAR", 1.0)
 
 
 def test_gradient_finite_differences_on_gpu(ctx, tmp_path):

@@ -182,6 +182,38 @@ def test_energy_gradient_matches_error_cost_o1(oracle):
     assert np.allclose(g, g2, rtol=1e-10, atol=1e-14)
 
 
+@pytest.mark.parametrize("loss", [1, 2, 3, 4])
+def test_energy_loss_variants_fd(oracle, loss):
+    """Every loss (MSE, MAE, HUBER, ASINH; nnptefr2.cpp:1339-1368) under every normalisation
+    (IDENTITY, LINEAR, SQRT, CBRT, LOG; 606-612): the gradient of the energy term against central
+    differences, and the same numbers from the error_cost_o1 restatement."""
+    pot = oracle.load_text(W.config_potential_text(3))
+    structs = cases.small_binary(n_struc=2, seed=14)
+    offs, posn, types, cell = pack_batch(structs)
+    Eref = np.array([-0.05 * len(t) for _, t, _ in structs])
+    Fref = np.zeros_like(posn)
+    p0 = pot.get_params()
+    rng = np.random.default_rng(loss)
+    for norm in range(5):
+        (L, LE, _), g = pot.train(offs, posn, types, cell, Eref, Fref, 1.0, 0.0, loss=loss, norm=norm, delta=0.5)
+        l2, g2 = pot.error_cost_o1(offs, posn, types, cell, Eref, loss=loss, norm=norm, delta=0.5)
+        assert abs(LE - l2) <= 1e-12 * max(1.0, abs(l2)) and np.allclose(g, g2, rtol=1e-10, atol=1e-14), (loss, norm)
+        gscale = np.abs(g).max()
+        for k in rng.choice(len(p0), 4, replace=False):
+            h = 1e-5 * max(1.0, abs(p0[k]))
+            pp = p0.copy(); pp[k] += h
+            pot.set_params(pp)
+            lp = pot.error_cost_o1(offs, posn, types, cell, Eref, loss=loss, norm=norm, delta=0.5)[0]
+            pp[k] -= 2 * h
+            pot.set_params(pp)
+            lm = pot.error_cost_o1(offs, posn, types, cell, Eref, loss=loss, norm=norm, delta=0.5)[0]
+            pot.set_params(p0)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - g[k]) <= 1e-6 * max(abs(fd), abs(g[k])) + 1e-7 * gscale, (loss, norm, k, fd, g[k])
+    with pytest.raises(RuntimeError):
+        pot.error_cost_o1(offs, posn, types, cell, Eref, loss=loss, norm=5)
+
+
 @pytest.mark.parametrize("neuron", range(1, 20))
 def test_activation_derivatives_fd(oracle, neuron):
     """d = da/dz and d2 = dd/dz for every activation of nn.cpp:149-810, away from the kinks at 0"""
