@@ -68,6 +68,7 @@ _SIGS = {
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
     "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_adam_set_schedule": (C.c_int, [_V, C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_double]),
     "ann_train_set_loss": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_double]),
     "ann_host_alloc": (C.c_int, [_V, C.c_int64, C.POINTER(C.c_void_p)]),
     "ann_host_free": (C.c_int, [_V, C.c_void_p]),
@@ -465,6 +466,15 @@ class Context:
     def adam_init(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-16):
         """Adam on the device (NN::ADAM; eps defaults to the reference's 1e-16)."""
         self._ck(self.lib.ann_adam_init(self.h, lr, beta1, beta2, eps))
+
+    DECAY = {"CONST": 1, "EXP": 2, "GAUSS": 3, "SQRT": 4, "INV": 5, "STEP": 6}
+    REG = {"LASSO": 0, "RIDGE": 1, "HUBER": 2, "ASINH": 3, "NONE": 4}
+
+    def adam_schedule(self, decay="CONST", alpha=0.0, period=1, reg="NONE", eta=0.0):
+        """The trainer's step-size schedule (DECAY / ALPHA / PERIOD) and weight decay (REG / ETA)."""
+        de = self.DECAY[decay] if isinstance(decay, str) else int(decay)
+        rg = self.REG[reg] if isinstance(reg, str) else int(reg)
+        self._ck(self.lib.ann_adam_set_schedule(self.h, de, float(alpha), int(period), rg, float(eta)))
 
     def adam_step(self, scale=1.0):
         """One Adam step with the gradient of the last train_backward (times scale)."""

@@ -36,7 +36,7 @@ void launch_md_kick_drift(int natoms, double* pos, double* vel, const void* F, b
 void launch_md_ke(int natoms, const double* vel, const double* mass, const int32_t* type, double* ke, cudaStream_t st);
 // optimiser and parameter refresh (optim.cu)
 void launch_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2, double b1ii,
-                 double b2ii, double eps, cudaStream_t st);
+                 double b2ii, double eps, int reg, double eta, const int32_t* map, cudaStream_t st);
 void launch_param_refresh(int64_t n, const double* p, const int32_t* map, double* w64, double* wt64, double* b64, float* w32, float* wt32,
                           float* b32, uint8_t* img, cudaStream_t st);
 void configure_kernels();
@@ -114,6 +114,10 @@ struct ann_ctx {
     bool adam_ready = false, have_grad = false;
     int64_t adam_t = 0;
     double adam_lr = 0, adam_b1 = 0, adam_b2 = 0, adam_eps = 0;
+    double adam_b1i = 0, adam_b2i = 0;        // beta^t, kept as running products (opt/algo.cpp:275-295)
+    double adam_gamma = 0;                    // the step size after the decay schedule
+    int adam_decay = 1, adam_period = 1, adam_reg = 4;   // Decay CONST, Regularization NONE
+    double adam_alpha = 0, adam_eta = 0;
     ParamSet<float> pf;
     ParamSet<double> pd;
     DevBuf poff;

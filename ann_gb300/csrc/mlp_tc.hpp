@@ -59,6 +59,8 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
 // nn.cpp:846-859): 8 ints per parameter, -1 where a destination does not apply.
 enum ParamSlot { PM_KIND = 0, PM_I64, PM_IT, PM_F32, PM_FH, PM_FL, PM_BH, PM_BL, PM_N };
 enum ParamKind { PK_BIAS = 0, PK_WEIGHT = 1 };
+// weight decay of the optimiser step (Regularization, nnptefr2.hpp:173-181)
+enum RegKind { REG_LASSO = 0, REG_RIDGE = 1, REG_HUBER = 2, REG_ASINH = 3, REG_NONE = 4 };
 // PM_I64: index into the FP64/FP32 bias or row-major weight arrays; PM_IT: index into the
 // transposed weights; PM_F32: byte offset of an FP32 copy in the tensor-core images (hidden bias,
 // last-layer weight or bias); PM_FH/FL, PM_BH/BL: byte offsets of the BF16 hi/lo entries of the

@@ -12,8 +12,11 @@
 
 namespace ann {
 
+// one Adam step, then the trainer's weight decay on weights (not biases; nnptefr2.cpp:909-921,
+// 1028-1049): p -= gamma eta f(p_old), f = sgn (LASSO), x (RIDGE), x / sqrt(1 + x^2) (HUBER),
+// asinh (ASINH); reg = REG_NONE skips it
 __global__ void k_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2,
-                       double b1ii, double b2ii, double eps) {
+                       double b1ii, double b2ii, double eps, int reg, double eta, const int32_t* map) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double gi = g[i] * scale;
@@ -21,7 +24,19 @@ __global__ void k_adam(int64_t n, const double* g, double scale, double* m, doub
     const double vi = v[i] * b2 + (1.0 - b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
-    p[i] -= lr * b1ii * mi / (sqrt(b2ii * vi) + eps);
+    const double p0 = p[i];
+    double pn = p0 - lr * b1ii * mi / (sqrt(b2ii * vi) + eps);
+    if (reg != REG_NONE && map[PM_N * i + PM_KIND] != PK_BIAS) {
+        double f = 0.0;
+        switch (reg) {
+            case REG_LASSO: f = (double)((p0 > 0) - (p0 < 0)); break;
+            case REG_RIDGE: f = p0; break;
+            case REG_HUBER: f = p0 / sqrt(1.0 + p0 * p0); break;
+            default: f = asinh(p0); break;
+        }
+        pn -= lr * eta * f;
+    }
+    p[i] = pn;
 }
 
 // one thread per parameter: FP64 and FP32 copies (row-major and transposed weights, biases) and,
@@ -54,9 +69,9 @@ __global__ void k_param_refresh(int64_t n, const double* p, const int32_t* map, 
 }
 
 void launch_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2, double b1ii,
-                 double b2ii, double eps, cudaStream_t st) {
+                 double b2ii, double eps, int reg, double eta, const int32_t* map, cudaStream_t st) {
     if (n <= 0) return;
-    ++::ann::g_launch_counter, k_adam<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, g, scale, m, v, p, lr, b1, b2, b1ii, b2ii, eps);
+    ++::ann::g_launch_counter, k_adam<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, g, scale, m, v, p, lr, b1, b2, b1ii, b2ii, eps, reg, eta, map);
 }
 void launch_param_refresh(int64_t n, const double* p, const int32_t* map, double* w64, double* wt64, double* b64, float* w32, float* wt32,
                           float* b32, uint8_t* img, cudaStream_t st) {

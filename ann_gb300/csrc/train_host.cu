@@ -215,8 +215,18 @@ int ann_adam_init(ann_ctx* c, double lr, double beta1, double beta2, double eps)
         ck(cudaMemsetAsync(c->adam_v.p, 0, 8 * n, c->stream), "memset");
         ck(cudaStreamSynchronize(c->stream), "synchronize");
         c->adam_lr = lr; c->adam_b1 = beta1; c->adam_b2 = beta2; c->adam_eps = eps; c->adam_t = 0;
+        c->adam_b1i = beta1; c->adam_b2i = beta2; c->adam_gamma = lr;
         c->adam_ready = true;
     })
+}
+int ann_adam_set_schedule(ann_ctx* c, int32_t decay, double alpha, int32_t period, int32_t reg, double eta) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (decay < ANN_DECAY_CONST || decay > ANN_DECAY_STEP) return fail(c, ANN_ERR_ARG, "Invalid decay schedule.");
+    if (reg < ANN_REG_LASSO || reg > ANN_REG_NONE) return fail(c, ANN_ERR_ARG, "Invalid regularization.");
+    if (!std::isfinite(alpha) || !std::isfinite(eta)) return fail(c, ANN_ERR_ARG, "alpha and eta must be finite");
+    if (decay == ANN_DECAY_STEP && period < 1) return fail(c, ANN_ERR_ARG, "the STEP schedule needs period >= 1");
+    c->adam_decay = decay; c->adam_alpha = alpha; c->adam_period = std::max(period, 1); c->adam_reg = reg; c->adam_eta = eta;
+    return ANN_OK;
 }
 int ann_adam_step(ann_ctx* c, double scale) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
@@ -225,12 +235,26 @@ int ann_adam_step(ann_ctx* c, double scale) {
         if (!c->have_grad) throw ann_error(ANN_ERR_STATE, "ann_adam_step needs the gradient of a preceding ann_train_backward");
         set_device(c);
         const int64_t n = c->pot.nparams();
-        ++c->adam_t;
-        const double b1ii = 1.0 / (1.0 - std::pow(c->adam_b1, (double)c->adam_t));
-        const double b2ii = 1.0 / (1.0 - std::pow(c->adam_b2, (double)c->adam_t));
+        // the step size of this iteration (Decay::step, opt/decay.cpp:42-62, applied before the
+        // optimiser step as nnptefr2.cpp:1025 with the iteration index counted from 0)
+        const double t = (double)c->adam_t, al = c->adam_alpha;
+        double& gamma = c->adam_gamma;
+        switch (c->adam_decay) {
+            case ANN_DECAY_EXP: gamma = gamma * (1.0 - al); break;
+            case ANN_DECAY_GAUSS: gamma = gamma * (1.0 - 2.0 * al * t); break;
+            case ANN_DECAY_SQRT: gamma = gamma * (1.0 - 0.5 * al / (1.0 + al * t)); break;
+            case ANN_DECAY_INV: gamma = gamma * (1.0 - al / (1.0 + al * t)); break;
+            case ANN_DECAY_STEP: if (c->adam_t > 0 && c->adam_t % c->adam_period == 0) gamma = gamma * al; break;
+            default: break;
+        }
+        const double b1ii = 1.0 / (1.0 - c->adam_b1i);
+        const double b2ii = 1.0 / (1.0 - c->adam_b2i);
         const int64_t before = g_launch_counter;
-        launch_adam(n, c->grad.as<double>(), scale, c->adam_m.as<double>(), c->adam_v.as<double>(), c->p64.as<double>(), c->adam_lr, c->adam_b1,
-                    c->adam_b2, b1ii, b2ii, c->adam_eps, c->stream);
+        launch_adam(n, c->grad.as<double>(), scale, c->adam_m.as<double>(), c->adam_v.as<double>(), c->p64.as<double>(), gamma, c->adam_b1,
+                    c->adam_b2, b1ii, b2ii, c->adam_eps, c->adam_reg, c->adam_eta, c->pmap.as<int32_t>(), c->stream);
+        c->adam_b1i *= c->adam_b1;
+        c->adam_b2i *= c->adam_b2;
+        ++c->adam_t;
         launch_param_refresh(n, c->p64.as<double>(), c->pmap.as<int32_t>(), c->pd.w.as<double>(), c->pd.wt.as<double>(), c->pd.b.as<double>(),
                              c->pf.w.as<float>(), c->pf.wt.as<float>(), c->pf.b.as<float>(), c->tc.ok ? c->tcimg.as<uint8_t>() : nullptr,
                              c->stream);

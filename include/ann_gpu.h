@@ -214,6 +214,17 @@ int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t npar
  * parameter transfer. ann_get_params / ann_write_potential read the updated parameters.       */
 int ann_adam_init(ann_ctx* ctx, double lr, double beta1, double beta2, double eps);
 int ann_adam_step(ann_ctx* ctx, double scale);
+/* The trainer's step-size schedule and weight decay around the Adam step (nnptefr2.cpp:1025-1049):
+ * before step t (counted from 0 since ann_adam_init), gamma <- decay(gamma, t) with DECAY / ALPHA /
+ * PERIOD as opt::Decay (opt/decay.cpp:42-62): CONST gamma, EXP gamma (1 - alpha), GAUSS
+ * gamma (1 - 2 alpha t), SQRT gamma (1 - alpha / (2 (1 + alpha t))), INV gamma (1 - alpha /
+ * (1 + alpha t)), STEP gamma alpha every PERIOD steps. After the step, the weights (not the biases)
+ * get p -= gamma eta f(p_old), with f = sgn (LASSO), x (RIDGE), x / sqrt(1 + x^2) (HUBER), or asinh
+ * (ASINH); REG_NONE skips this. The default is CONST and NONE. Enum values are those of opt::Decay
+ * (opt/decay.hpp:28-36) and Regularization (nnptefr2.hpp:173-181).                               */
+enum ann_decay { ANN_DECAY_CONST = 1, ANN_DECAY_EXP = 2, ANN_DECAY_GAUSS = 3, ANN_DECAY_SQRT = 4, ANN_DECAY_INV = 5, ANN_DECAY_STEP = 6 };
+enum ann_reg { ANN_REG_LASSO = 0, ANN_REG_RIDGE = 1, ANN_REG_HUBER = 2, ANN_REG_ASINH = 3, ANN_REG_NONE = 4 };
+int ann_adam_set_schedule(ann_ctx* ctx, int32_t decay, double alpha, int32_t period, int32_t reg, double eta);
 
 /* ---- input statistics and pre-conditioning of a training set (nnptefr2.cpp:686-858) ----------
  * The trainer's set-up: statistics of every input over all atoms of each type in the training

@@ -207,6 +207,53 @@ def test_adam_steps_on_device(ctx, tmp_path):
         other.close()
 
 
+def _decay(name, gamma, t, alpha, period):
+    """opt::Decay::step (opt/decay.cpp:42-62)."""
+    return {"CONST": gamma, "EXP": gamma * (1.0 - alpha), "GAUSS": gamma * (1.0 - 2.0 * alpha * t),
+            "SQRT": gamma * (1.0 - 0.5 * alpha / (1.0 + alpha * t)), "INV": gamma * (1.0 - alpha / (1.0 + alpha * t)),
+            "STEP": gamma * alpha if (t > 0 and t % period == 0) else gamma}[name]
+
+
+@pytest.mark.parametrize("decay", ["CONST", "EXP", "GAUSS", "SQRT", "INV", "STEP"])
+def test_adam_schedule_and_weight_decay(ctx, tmp_path, decay):
+    """The trainer's order (nnptefr2.cpp:1025-1049): gamma from the decay schedule, the Adam step,
+    then weight decay of the weights (not the biases) from the pre-step values, for every
+    regularisation; four steps against a numpy replay of the same gradients."""
+    text = cases.config_potential(ctx, 3, tmp_path)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    wm = np.tile(np.r_[np.zeros(64 + 64 + 1), np.ones(72 * 64 + 64 * 64 + 64)], 2)   # biases, then weights, per type
+    f = {"LASSO": np.sign, "RIDGE": lambda x: x, "HUBER": lambda x: x / np.sqrt(1.0 + x * x), "ASINH": np.arcsinh}
+    lr, b1, b2, eps, alpha, period, eta = 1e-3, 0.9, 0.999, 1e-16, 0.05, 2, 0.01
+    try:
+        for reg in ("NONE", "LASSO", "RIDGE", "HUBER", "ASINH"):
+            ctx.load_text(text)
+            p = ctx.get_params()
+            assert len(p) == len(wm)
+            ctx.adam_init(lr, b1, b2, eps)
+            ctx.adam_schedule(decay, alpha=alpha, period=period, reg=reg, eta=eta)
+            m = np.zeros_like(p); v = np.zeros_like(p)
+            gamma, b1i, b2i = lr, b1, b2
+            for t in range(4):
+                ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+                g = ctx.train_backward()
+                ctx.adam_step()
+                gamma = _decay(decay, gamma, t, alpha, period)
+                m = b1 * m + (1 - b1) * g
+                v = b2 * v + (1 - b2) * g * g
+                pn = p - gamma * (1.0 / (1.0 - b1i)) * m / (np.sqrt((1.0 / (1.0 - b2i)) * v) + eps)
+                if reg != "NONE":
+                    pn = pn - gamma * eta * wm * f[reg](p)
+                p = pn
+                b1i *= b1; b2i *= b2
+            assert np.allclose(ctx.get_params(), p, rtol=1e-10, atol=1e-13), (decay, reg)
+        with pytest.raises(AnnError, match="decay"):
+            ctx.adam_schedule(7)
+        with pytest.raises(AnnError, match="regularization"):
+            ctx.adam_schedule("CONST", reg=5)
+    finally:
+        ctx.adam_schedule()
+
+
 def test_compute_after_md_leaves_md(ctx, tmp_path):
     """A batch computed after an MD run replaces the MD system: same results as a fresh context."""
     text = cases.config_potential(ctx, 5, tmp_path)
