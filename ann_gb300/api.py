@@ -68,7 +68,9 @@ _SIGS = {
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
     "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
-    "ann_adam_set_schedule": (C.c_int, [_V, C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_double]),
+    "ann_opt_set_schedule": (C.c_int, [_V, C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_double]),
+    "ann_opt_init": (C.c_int, [_V, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "ann_opt_step": (C.c_int, [_V, C.c_double]),
     "ann_train_set_loss": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_double]),
     "ann_host_alloc": (C.c_int, [_V, C.c_int64, C.POINTER(C.c_void_p)]),
     "ann_host_free": (C.c_int, [_V, C.c_void_p]),
@@ -470,11 +472,26 @@ class Context:
     DECAY = {"CONST": 1, "EXP": 2, "GAUSS": 3, "SQRT": 4, "INV": 5, "STEP": 6}
     REG = {"LASSO": 0, "RIDGE": 1, "HUBER": 2, "ASINH": 3, "NONE": 4}
 
-    def adam_schedule(self, decay="CONST", alpha=0.0, period=1, reg="NONE", eta=0.0):
+    OPT = {"SGD": 1, "SDM": 2, "NAG": 3, "ADAGRAD": 4, "ADADELTA": 5, "RMSPROP": 6, "ADAM": 7, "ADAMW": 8, "ADAB": 9, "YOGI": 10,
+           "NOGI": 11, "NADAM": 12, "AMSGRAD": 13, "BFGS": 14, "RPROP": 15, "CG": 16}
+
+    def opt_schedule(self, decay="CONST", alpha=0.0, period=1, reg="NONE", eta=0.0):
         """The trainer's step-size schedule (DECAY / ALPHA / PERIOD) and weight decay (REG / ETA)."""
         de = self.DECAY[decay] if isinstance(decay, str) else int(decay)
         rg = self.REG[reg] if isinstance(reg, str) else int(reg)
-        self._ck(self.lib.ann_adam_set_schedule(self.h, de, float(alpha), int(period), rg, float(eta)))
+        self._ck(self.lib.ann_opt_set_schedule(self.h, de, float(alpha), int(period), rg, float(eta)))
+
+    adam_schedule = opt_schedule
+
+    def opt_init(self, algo="ADAM", gamma=1e-3, eta=0.9, eps=1e-8, w=0.0):
+        """The trainer's ALGO on the device (opt::algo): step size gamma, momentum / decay eta,
+        guard eps, ADAMW weight decay w."""
+        a = self.OPT[algo] if isinstance(algo, str) else int(algo)
+        self._ck(self.lib.ann_opt_init(self.h, a, float(gamma), float(eta), float(eps), float(w)))
+
+    def opt_step(self, scale=1.0):
+        """One optimiser step with the gradient of the last train_backward (times scale)."""
+        self._ck(self.lib.ann_opt_step(self.h, scale))
 
     def adam_step(self, scale=1.0):
         """One Adam step with the gradient of the last train_backward (times scale)."""

@@ -427,7 +427,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
-                      &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->adam_m, &c->adam_v,
+                      &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->opt_s0, &c->opt_s1, &c->opt_s2, &c->opt_gold, &c->opt_part,
                       &c->lx, &c->ltype, &c->lilist, &c->lnoff, &c->lneigh, &c->lrtype, &c->lnn, &c->lntc, &c->lnj, &c->lnr, &c->lG,
                       &c->ldEdG, &c->lEatom, &c->lF, &c->lW, &c->lFout, &c->ltcount, &c->ltstart, &c->ltlist, &c->ltables, &c->lpartial,
                       &c->lEs, &c->lWs, &c->st_acc, &c->st_n, &c->st_part, &c->st_pcount})
@@ -456,7 +456,7 @@ int ann_load_potential_text(ann_ctx* c, const char* text) {
         p.read_text(text);
         p.validate();
         c->pot = p;
-        c->adam_ready = false;
+        c->opt_ready = false;
         c->st_ready = false;   // statistics belong to the previous potential's inputs
         rebuild_plan(c);
     })

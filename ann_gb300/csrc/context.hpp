@@ -35,8 +35,6 @@ void launch_md_kick_drift(int natoms, double* pos, double* vel, const void* F, b
                           int stage, cudaStream_t st);
 void launch_md_ke(int natoms, const double* vel, const double* mass, const int32_t* type, double* ke, cudaStream_t st);
 // optimiser and parameter refresh (optim.cu)
-void launch_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2, double b1ii,
-                 double b2ii, double eps, int reg, double eta, const int32_t* map, cudaStream_t st);
 void launch_param_refresh(int64_t n, const double* p, const int32_t* map, double* w64, double* wt64, double* b64, float* w32, float* wt32,
                           float* b32, uint8_t* img, cudaStream_t st);
 void configure_kernels();
@@ -109,15 +107,18 @@ struct ann_ctx {
     // packed FP64 parameters on the device and where each one is copied to
     DevBuf p64, pmap;
     bool params_dev_newer = false;  // an optimiser step changed p64 after the host copy
-    // Adam state (NN::ADAM, opt/algo.cpp:272-296)
-    DevBuf adam_m, adam_v;
-    bool adam_ready = false, have_grad = false;
-    int64_t adam_t = 0;
-    double adam_lr = 0, adam_b1 = 0, adam_b2 = 0, adam_eps = 0;
-    double adam_b1i = 0, adam_b2i = 0;        // beta^t, kept as running products (opt/algo.cpp:275-295)
-    double adam_gamma = 0;                    // the step size after the decay schedule
-    int adam_decay = 1, adam_period = 1, adam_reg = 4;   // Decay CONST, Regularization NONE
-    double adam_alpha = 0, adam_eta = 0;
+    // optimiser state (opt::algo, src/opt/algo.cpp): s0 / s1 / s2 per parameter, the previous
+    // gradient, and the CG reduction
+    DevBuf opt_s0, opt_s1, opt_s2, opt_gold, opt_part;
+    bool opt_ready = false, have_grad = false;
+    int opt_algo = 7;                         // ADAM
+    int64_t opt_t = 0;
+    double opt_lr = 0, opt_b1 = 0.9, opt_b2 = 0.999, opt_eps = 0, opt_eta = 0, opt_w = 0;
+    double opt_b1i = 0, opt_b2i = 0;          // beta^t, kept as running products (opt/algo.cpp:275-295)
+    double opt_gamma = 0;                     // the step size after the decay schedule
+    int opt_decay = 1, opt_period = 1, opt_reg = 4;      // Decay CONST, Regularization NONE
+    double opt_alpha = 0, opt_reg_eta = 0;
+    double last_loss = 0, prev_loss = 0;      // training loss of the last forward pass / of the previous step (RPROP)
     ParamSet<float> pf;
     ParamSet<double> pd;
     DevBuf poff;

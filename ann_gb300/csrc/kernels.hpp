@@ -100,6 +100,25 @@ struct ListArgs {
 void launch_list_rows(const ListArgs& a, bool fp64, cudaStream_t st);
 template <typename real> void launch_to_double(size_t n, const real* in, double* out, cudaStream_t st);
 
+// ---- optimiser steps (optim.cu) ---------------------------------------------------------------
+// algorithms with the values of opt::algo::Name (src/opt/algo.hpp:31-49)
+enum OptAlgo { OPT_SGD = 1, OPT_SDM = 2, OPT_NAG = 3, OPT_ADAGRAD = 4, OPT_ADADELTA = 5, OPT_RMSPROP = 6, OPT_ADAM = 7, OPT_ADAMW = 8,
+               OPT_ADAB = 9, OPT_YOGI = 10, OPT_NOGI = 11, OPT_NADAM = 12, OPT_AMSGRAD = 13, OPT_BFGS = 14, OPT_RPROP = 15, OPT_CG = 16 };
+struct OptArgs {
+    int64_t n;
+    int algo, reg, inc;              // inc (RPROP): the loss rose since the previous step
+    const double* g;                 // gradient, times scale
+    double scale;
+    double* p;                       // FP64 parameters
+    double* s0; double* s1; double* s2;   // per-parameter state (s1 / s2 NULL where unused)
+    double* gold;                    // previous gradient (RPROP, CG; else NULL)
+    double* beta;                    // CG: device scalar from the reduction
+    double gamma, eta, eps, w, b1, b2, b1ii, b2ii;
+    double reg_eta;                  // weight-decay strength
+    const int32_t* map;              // parameter map (bias / weight kind)
+};
+void launch_opt(const OptArgs& o, double* part, cudaStream_t st);
+
 // ---- input statistics of a training set (stats.cu) -------------------------------------------
 int stats_chunks_per_type(int natoms);
 template <typename real>

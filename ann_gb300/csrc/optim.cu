@@ -1,5 +1,6 @@
-// Optimiser step on the device and the refresh of every device copy of the network parameters
-// from the packed FP64 vector, so that a training loop keeps its parameters resident.
+// Optimiser steps on the device (every elementwise algorithm of opt::algo, and CG) and the refresh
+// of every device copy of the network parameters from the packed FP64 vector, so that a training
+// loop keeps its parameters resident.
 //
 // Reference: NN::ADAM::step (src/opt/algo.cpp:280-296): m = b1 m + (1-b1) g, v = b2 v + (1-b2) g^2,
 // p -= gamma / (1 - b1^t) m / (sqrt(v / (1 - b2^t)) + eps); the packing order of the parameters is
@@ -12,31 +13,91 @@
 
 namespace ann {
 
-// one Adam step, then the trainer's weight decay on weights (not biases; nnptefr2.cpp:909-921,
-// 1028-1049): p -= gamma eta f(p_old), f = sgn (LASSO), x (RIDGE), x / sqrt(1 + x^2) (HUBER),
-// asinh (ASINH); reg = REG_NONE skips it
-__global__ void k_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2,
-                       double b1ii, double b2ii, double eps, int reg, double eta, const int32_t* map) {
+// One optimiser step of opt::algo (src/opt/algo.cpp:97-660), then the trainer's weight decay on
+// weights (not biases; nnptefr2.cpp:909-921, 1028-1049): p -= gamma eta f(p_old) with f = sgn
+// (LASSO), x (RIDGE), x / sqrt(1 + x^2) (HUBER), asinh (ASINH). State per parameter: s0, s1, s2 (the
+// algorithm's running vectors) and gold (the previous gradient, for RPROP and CG). The Adam family
+// uses beta1 = b1, beta2 = b2 and the bias corrections b1ii = 1/(1 - b1^t), b2ii = 1/(1 - b2^t).
+__global__ void k_opt(OptArgs o) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double gi = g[i] * scale;
-    const double mi = m[i] * b1 + (1.0 - b1) * gi;
-    const double vi = v[i] * b2 + (1.0 - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    const double p0 = p[i];
-    double pn = p0 - lr * b1ii * mi / (sqrt(b2ii * vi) + eps);
-    if (reg != REG_NONE && map[PM_N * i + PM_KIND] != PK_BIAS) {
+    if (i >= o.n) return;
+    double g = o.g[i] * o.scale;
+    const double p0 = o.p[i], gm = o.gamma, b1 = o.b1, b2 = o.b2, eps = o.eps, eta = o.eta;
+    double p = p0;
+    double s0 = o.s0[i], s1 = o.s1 ? o.s1[i] : 0.0, s2 = o.s2 ? o.s2[i] : 0.0;
+    auto sgn = [](double x) { return (double)((x > 0) - (x < 0)); };
+    switch (o.algo) {
+        case OPT_SGD: p -= gm * g; break;
+        case OPT_SDM: s0 = eta * s0 + gm * g; p -= s0; break;
+        case OPT_NAG: s0 = eta * s0 + gm * (eta + 1.0) * g; p -= s0; break;
+        case OPT_ADAGRAD: s0 += g * g; p -= gm * g / (sqrt(s0) + eps); break;
+        case OPT_ADADELTA: {
+            s0 = eta * s0 + (1.0 - eta) * g * g;
+            const double dx = g * sqrt(s1) / (sqrt(s0) + eps);
+            p -= dx;
+            s1 = eta * s1 + (1.0 - eta) * dx * dx;
+        } break;
+        case OPT_RMSPROP: s0 = 0.9 * s0 + 0.1 * g * g; p -= gm * g / (sqrt(s0) + eps); break;
+        case OPT_ADAM: case OPT_ADAMW: case OPT_ADAB: case OPT_YOGI: case OPT_NOGI: case OPT_NADAM: case OPT_AMSGRAD: {
+            s0 = s0 * b1 + (1.0 - b1) * g;
+            if (o.algo == OPT_ADAB) s1 = s1 * b2 + (1.0 - b2) * (g - s0) * (g - s0) + eps;
+            else if (o.algo == OPT_YOGI || o.algo == OPT_NOGI) s1 -= (1.0 - b2) * sgn(s1 - g * g) * (g * g);
+            else s1 = s1 * b2 + (1.0 - b2) * g * g;
+            double vv = s1;
+            if (o.algo == OPT_AMSGRAD) { if (s1 > s2) s2 = s1; vv = s2; }
+            const double mm = (o.algo == OPT_NOGI || o.algo == OPT_NADAM) ? b1 * s0 + (1.0 - b1) * g : s0;
+            if (o.algo == OPT_ADAMW) p -= gm * (o.b1ii * mm / (sqrt(o.b2ii * vv) + eps) + o.w * p0);
+            else p -= gm * o.b1ii * mm / (sqrt(o.b2ii * vv) + eps);
+        } break;
+        case OPT_RPROP: {   // s0 = delta, s1 = dx; the gradient kept for the next step is zeroed on a sign change
+            const double sg = g * o.gold[i];
+            if (sg > 0) { s0 = fmin(s0 * 1.2, 50.0); s1 = -1.0 * sgn(g) * s0; p += s1; }
+            else if (sg < 0) { s0 = fmax(s0 * 0.5, 1e-14); if (o.inc) p -= s1; g = 0.0; }
+            else { s1 = -1.0 * sgn(g) * s0; p += s1; }
+        } break;
+        case OPT_CG: s0 = (*o.beta) * s0 - g; p += gm * s0; break;
+        default: break;
+    }
+    if (o.reg != REG_NONE && o.map[PM_N * i + PM_KIND] != PK_BIAS) {
         double f = 0.0;
-        switch (reg) {
-            case REG_LASSO: f = (double)((p0 > 0) - (p0 < 0)); break;
+        switch (o.reg) {
+            case REG_LASSO: f = sgn(p0); break;
             case REG_RIDGE: f = p0; break;
             case REG_HUBER: f = p0 / sqrt(1.0 + p0 * p0); break;
             default: f = asinh(p0); break;
         }
-        pn -= lr * eta * f;
+        p -= gm * o.reg_eta * f;
     }
-    p[i] = pn;
+    o.p[i] = p;
+    o.s0[i] = s0;
+    if (o.s1) o.s1[i] = s1;
+    if (o.s2) o.s2[i] = s2;
+    if (o.gold) o.gold[i] = g;
+}
+
+// CG: beta = g . (g - g_old) / (|g_old|^2 + eps) in a fixed order (block partials, then one block)
+constexpr int CG_T = 256;
+__global__ void k_cg_partial(int64_t n, const double* g, double scale, const double* gold, double* part) {
+    __shared__ double a[CG_T], b[CG_T];
+    double sa = 0.0, sb = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)CG_T + threadIdx.x; i < n; i += (int64_t)gridDim.x * CG_T) {
+        const double gi = g[i] * scale;
+        sa += gi * (gi - gold[i]);
+        sb += gold[i] * gold[i];
+    }
+    a[threadIdx.x] = sa; b[threadIdx.x] = sb;
+    __syncthreads();
+    for (int w = CG_T / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) { a[threadIdx.x] += a[threadIdx.x + w]; b[threadIdx.x] += b[threadIdx.x + w]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { part[2 * blockIdx.x] = a[0]; part[2 * blockIdx.x + 1] = b[0]; }
+}
+__global__ void k_cg_beta(int nb, const double* part, double eps, double* beta) {
+    if (threadIdx.x != 0) return;
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nb; ++k) { a += part[2 * k]; b += part[2 * k + 1]; }
+    *beta = a / (b + eps);
 }
 
 // one thread per parameter: FP64 and FP32 copies (row-major and transposed weights, biases) and,
@@ -68,10 +129,14 @@ __global__ void k_param_refresh(int64_t n, const double* p, const int32_t* map, 
     }
 }
 
-void launch_adam(int64_t n, const double* g, double scale, double* m, double* v, double* p, double lr, double b1, double b2, double b1ii,
-                 double b2ii, double eps, int reg, double eta, const int32_t* map, cudaStream_t st) {
-    if (n <= 0) return;
-    ++::ann::g_launch_counter, k_adam<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, g, scale, m, v, p, lr, b1, b2, b1ii, b2ii, eps, reg, eta, map);
+void launch_opt(const OptArgs& o, double* part, cudaStream_t st) {
+    if (o.n <= 0) return;
+    if (o.algo == OPT_CG) {
+        const int nb = (int)std::min<int64_t>((o.n + CG_T - 1) / CG_T, 64);
+        ++::ann::g_launch_counter, k_cg_partial<<<nb, CG_T, 0, st>>>(o.n, o.g, o.scale, o.gold, part);
+        ++::ann::g_launch_counter, k_cg_beta<<<1, 32, 0, st>>>(nb, part, o.eps, o.beta);
+    }
+    ++::ann::g_launch_counter, k_opt<<<(unsigned)((o.n + 255) / 256), 256, 0, st>>>(o);
 }
 void launch_param_refresh(int64_t n, const double* p, const int32_t* map, double* w64, double* wt64, double* b64, float* w32, float* wt32,
                           float* b32, uint8_t* img, cudaStream_t st) {

@@ -159,6 +159,7 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
             loss();
             ck(cudaStreamSynchronize(c->stream), "synchronize");
         }
+        c->last_loss = loss3[0];
         c->have_train = true; c->train_prec = prec; c->train_wE = wE; c->train_wF = wF;
     })
 }
@@ -202,68 +203,97 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
     })
 }
 
+}  // extern "C"
+
+// the optimiser of the trainer (opt::algo): state zeroed (RPROP: step sizes 0.1), step counter and
+// the running beta powers reset
+static void opt_reset(ann_ctx* c, int algo, double lr, double b1, double b2, double eps, double eta, double w) {
+    if (!c->have_pot) throw ann_error(ANN_ERR_STATE, "no potential loaded");
+    if (algo == OPT_BFGS) throw ann_error(ANN_ERR_UNSUPPORTED, "BFGS keeps a dense P x P matrix; not provided on the device");
+    if (algo < OPT_SGD || algo > OPT_CG) throw ann_error(ANN_ERR_ARG, "Invalid optimization algorithm.");
+    if (!(lr >= 0) || !(b1 >= 0 && b1 < 1) || !(b2 >= 0 && b2 < 1) || !(eps >= 0) || !(eta >= 0 && eta <= 1) || !(w >= 0 && w <= 1))
+        throw ann_error(ANN_ERR_ARG, "invalid optimiser settings (gamma >= 0, 0 <= beta < 1, eps >= 0, 0 <= eta, w <= 1)");
+    set_device(c);
+    const size_t n = (size_t)std::max<int64_t>(c->pot.nparams(), 1);
+    for (DevBuf* b : {&c->opt_s0, &c->opt_s1, &c->opt_s2, &c->opt_gold}) {
+        b->ensure(8 * n);
+        ck(cudaMemsetAsync(b->p, 0, 8 * n, c->stream), "memset");
+    }
+    c->opt_part.ensure(8 * 2 * 64 + 8);
+    if (algo == OPT_RPROP) {   // RPROP::resize: delta = 0.1 (src/opt/algo.cpp:604-608)
+        const std::vector<double> d(n, 0.1);
+        ck(cudaMemcpyAsync(c->opt_s0.p, d.data(), 8 * n, cudaMemcpyHostToDevice, c->stream), "H2D");
+    }
+    ck(cudaStreamSynchronize(c->stream), "synchronize");
+    c->opt_algo = algo; c->opt_lr = lr; c->opt_b1 = b1; c->opt_b2 = b2; c->opt_eps = eps; c->opt_eta = eta; c->opt_w = w;
+    c->opt_t = 0; c->opt_b1i = b1; c->opt_b2i = b2; c->opt_gamma = lr; c->prev_loss = 0.0;
+    c->opt_ready = true;
+}
+
+extern "C" {
+int ann_opt_init(ann_ctx* c, int32_t algo, double gamma, double eta, double eps, double w) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    ANN_TRY(c, { opt_reset(c, algo, gamma, 0.9, 0.999, eps, eta, w); })
+}
 int ann_adam_init(ann_ctx* c, double lr, double beta1, double beta2, double eps) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
     ANN_TRY(c, {
-        if (!c->have_pot) throw ann_error(ANN_ERR_STATE, "no potential loaded");
-        if (!(lr > 0) || !(beta1 >= 0 && beta1 < 1) || !(beta2 >= 0 && beta2 < 1) || !(eps >= 0))
-            throw ann_error(ANN_ERR_ARG, "invalid Adam settings (lr > 0, 0 <= beta < 1, eps >= 0)");
-        set_device(c);
-        const size_t n = (size_t)std::max<int64_t>(c->pot.nparams(), 1);
-        c->adam_m.ensure(8 * n); c->adam_v.ensure(8 * n);
-        ck(cudaMemsetAsync(c->adam_m.p, 0, 8 * n, c->stream), "memset");
-        ck(cudaMemsetAsync(c->adam_v.p, 0, 8 * n, c->stream), "memset");
-        ck(cudaStreamSynchronize(c->stream), "synchronize");
-        c->adam_lr = lr; c->adam_b1 = beta1; c->adam_b2 = beta2; c->adam_eps = eps; c->adam_t = 0;
-        c->adam_b1i = beta1; c->adam_b2i = beta2; c->adam_gamma = lr;
-        c->adam_ready = true;
+        if (!(lr > 0)) throw ann_error(ANN_ERR_ARG, "invalid Adam settings (lr > 0, 0 <= beta < 1, eps >= 0)");
+        opt_reset(c, OPT_ADAM, lr, beta1, beta2, eps, 0.0, 0.0);
     })
 }
-int ann_adam_set_schedule(ann_ctx* c, int32_t decay, double alpha, int32_t period, int32_t reg, double eta) {
+int ann_opt_set_schedule(ann_ctx* c, int32_t decay, double alpha, int32_t period, int32_t reg, double eta) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
     if (decay < ANN_DECAY_CONST || decay > ANN_DECAY_STEP) return fail(c, ANN_ERR_ARG, "Invalid decay schedule.");
     if (reg < ANN_REG_LASSO || reg > ANN_REG_NONE) return fail(c, ANN_ERR_ARG, "Invalid regularization.");
     if (!std::isfinite(alpha) || !std::isfinite(eta)) return fail(c, ANN_ERR_ARG, "alpha and eta must be finite");
     if (decay == ANN_DECAY_STEP && period < 1) return fail(c, ANN_ERR_ARG, "the STEP schedule needs period >= 1");
-    c->adam_decay = decay; c->adam_alpha = alpha; c->adam_period = std::max(period, 1); c->adam_reg = reg; c->adam_eta = eta;
+    c->opt_decay = decay; c->opt_alpha = alpha; c->opt_period = std::max(period, 1); c->opt_reg = reg; c->opt_reg_eta = eta;
     return ANN_OK;
 }
-int ann_adam_step(ann_ctx* c, double scale) {
+int ann_opt_step(ann_ctx* c, double scale) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
     ANN_TRY(c, {
-        if (!c->adam_ready) throw ann_error(ANN_ERR_STATE, "ann_adam_init first");
-        if (!c->have_grad) throw ann_error(ANN_ERR_STATE, "ann_adam_step needs the gradient of a preceding ann_train_backward");
+        if (!c->opt_ready) throw ann_error(ANN_ERR_STATE, "initialise the optimiser first (ann_opt_init / ann_adam_init)");
+        if (!c->have_grad) throw ann_error(ANN_ERR_STATE, "an optimiser step needs the gradient of a preceding ann_train_backward");
         set_device(c);
         const int64_t n = c->pot.nparams();
         // the step size of this iteration (Decay::step, opt/decay.cpp:42-62, applied before the
         // optimiser step as nnptefr2.cpp:1025 with the iteration index counted from 0)
-        const double t = (double)c->adam_t, al = c->adam_alpha;
-        double& gamma = c->adam_gamma;
-        switch (c->adam_decay) {
+        const double t = (double)c->opt_t, al = c->opt_alpha;
+        double& gamma = c->opt_gamma;
+        switch (c->opt_decay) {
             case ANN_DECAY_EXP: gamma = gamma * (1.0 - al); break;
             case ANN_DECAY_GAUSS: gamma = gamma * (1.0 - 2.0 * al * t); break;
             case ANN_DECAY_SQRT: gamma = gamma * (1.0 - 0.5 * al / (1.0 + al * t)); break;
             case ANN_DECAY_INV: gamma = gamma * (1.0 - al / (1.0 + al * t)); break;
-            case ANN_DECAY_STEP: if (c->adam_t > 0 && c->adam_t % c->adam_period == 0) gamma = gamma * al; break;
+            case ANN_DECAY_STEP: if (c->opt_t > 0 && c->opt_t % c->opt_period == 0) gamma = gamma * al; break;
             default: break;
         }
-        const double b1ii = 1.0 / (1.0 - c->adam_b1i);
-        const double b2ii = 1.0 / (1.0 - c->adam_b2i);
+        OptArgs o{};
+        o.n = n; o.algo = c->opt_algo; o.reg = c->opt_reg; o.inc = c->last_loss > c->prev_loss ? 1 : 0;
+        o.g = c->grad.as<double>(); o.scale = scale; o.p = c->p64.as<double>();
+        o.s0 = c->opt_s0.as<double>(); o.s1 = c->opt_s1.as<double>(); o.s2 = c->opt_s2.as<double>(); o.gold = c->opt_gold.as<double>();
+        o.beta = c->opt_part.as<double>() + 2 * 64;
+        o.gamma = gamma; o.eta = c->opt_eta; o.eps = c->opt_eps; o.w = c->opt_w; o.b1 = c->opt_b1; o.b2 = c->opt_b2;
+        o.b1ii = 1.0 / (1.0 - c->opt_b1i); o.b2ii = 1.0 / (1.0 - c->opt_b2i);
+        o.reg_eta = c->opt_reg_eta; o.map = c->pmap.as<int32_t>();
         const int64_t before = g_launch_counter;
-        launch_adam(n, c->grad.as<double>(), scale, c->adam_m.as<double>(), c->adam_v.as<double>(), c->p64.as<double>(), gamma, c->adam_b1,
-                    c->adam_b2, b1ii, b2ii, c->adam_eps, c->adam_reg, c->adam_eta, c->pmap.as<int32_t>(), c->stream);
-        c->adam_b1i *= c->adam_b1;
-        c->adam_b2i *= c->adam_b2;
-        ++c->adam_t;
+        launch_opt(o, c->opt_part.as<double>(), c->stream);
         launch_param_refresh(n, c->p64.as<double>(), c->pmap.as<int32_t>(), c->pd.w.as<double>(), c->pd.wt.as<double>(), c->pd.b.as<double>(),
                              c->pf.w.as<float>(), c->pf.wt.as<float>(), c->pf.b.as<float>(), c->tc.ok ? c->tcimg.as<uint8_t>() : nullptr,
                              c->stream);
         c->kernels += g_launch_counter - before;
-        ck(cudaGetLastError(), "Adam step");
+        ck(cudaGetLastError(), "optimiser step");
+        c->opt_b1i *= c->opt_b1;
+        c->opt_b2i *= c->opt_b2;
+        ++c->opt_t;
+        c->prev_loss = c->last_loss;
         c->params_dev_newer = true;
         c->have_results = false;
         c->have_grad = false;
     })
 }
+int ann_adam_step(ann_ctx* c, double scale) { return ann_opt_step(c, scale); }
 
 }  // extern "C"

@@ -214,8 +214,8 @@ int ann_train_backward(ann_ctx* ctx, double dl_scale, double* grad, int64_t npar
  * parameter transfer. ann_get_params / ann_write_potential read the updated parameters.       */
 int ann_adam_init(ann_ctx* ctx, double lr, double beta1, double beta2, double eps);
 int ann_adam_step(ann_ctx* ctx, double scale);
-/* The trainer's step-size schedule and weight decay around the Adam step (nnptefr2.cpp:1025-1049):
- * before step t (counted from 0 since ann_adam_init), gamma <- decay(gamma, t) with DECAY / ALPHA /
+/* The trainer's step-size schedule and weight decay around every optimiser step (nnptefr2.cpp:1025-1049):
+ * before step t (counted from 0 since the optimiser's init), gamma <- decay(gamma, t) with DECAY / ALPHA /
  * PERIOD as opt::Decay (opt/decay.cpp:42-62): CONST gamma, EXP gamma (1 - alpha), GAUSS
  * gamma (1 - 2 alpha t), SQRT gamma (1 - alpha / (2 (1 + alpha t))), INV gamma (1 - alpha /
  * (1 + alpha t)), STEP gamma alpha every PERIOD steps. After the step, the weights (not the biases)
@@ -224,7 +224,21 @@ int ann_adam_step(ann_ctx* ctx, double scale);
  * (opt/decay.hpp:28-36) and Regularization (nnptefr2.hpp:173-181).                               */
 enum ann_decay { ANN_DECAY_CONST = 1, ANN_DECAY_EXP = 2, ANN_DECAY_GAUSS = 3, ANN_DECAY_SQRT = 4, ANN_DECAY_INV = 5, ANN_DECAY_STEP = 6 };
 enum ann_reg { ANN_REG_LASSO = 0, ANN_REG_RIDGE = 1, ANN_REG_HUBER = 2, ANN_REG_ASINH = 3, ANN_REG_NONE = 4 };
-int ann_adam_set_schedule(ann_ctx* ctx, int32_t decay, double alpha, int32_t period, int32_t reg, double eta);
+int ann_opt_set_schedule(ann_ctx* ctx, int32_t decay, double alpha, int32_t period, int32_t reg, double eta);
+/* Any optimiser of the reference trainer (opt::algo, src/opt/algo.cpp:97-660) on the device, with
+ * the values of opt::algo::Name (src/opt/algo.hpp:31-49). gamma is the step size, eta the momentum
+ * / decay of SDM, NAG and ADADELTA, eps the denominator's guard, and w ADAMW's weight decay. The
+ * Adam family uses beta1 = 0.9, beta2 = 0.999 as the reference; ann_adam_init takes other betas.
+ * RPROP compares the loss of the last ann_train_forward with the loss at the previous step. BFGS
+ * keeps a dense P x P matrix and returns ANN_ERR_UNSUPPORTED. ann_opt_step applies one step with
+ * the gradient of the preceding ann_train_backward (times scale), like ann_adam_step.            */
+enum ann_opt {
+    ANN_OPT_SGD = 1, ANN_OPT_SDM = 2, ANN_OPT_NAG = 3, ANN_OPT_ADAGRAD = 4, ANN_OPT_ADADELTA = 5, ANN_OPT_RMSPROP = 6,
+    ANN_OPT_ADAM = 7, ANN_OPT_ADAMW = 8, ANN_OPT_ADAB = 9, ANN_OPT_YOGI = 10, ANN_OPT_NOGI = 11, ANN_OPT_NADAM = 12,
+    ANN_OPT_AMSGRAD = 13, ANN_OPT_BFGS = 14, ANN_OPT_RPROP = 15, ANN_OPT_CG = 16
+};
+int ann_opt_init(ann_ctx* ctx, int32_t algo, double gamma, double eta, double eps, double w);
+int ann_opt_step(ann_ctx* ctx, double scale);
 
 /* ---- input statistics and pre-conditioning of a training set (nnptefr2.cpp:686-858) ----------
  * The trainer's set-up: statistics of every input over all atoms of each type in the training

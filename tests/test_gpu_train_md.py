@@ -230,7 +230,7 @@ def test_adam_schedule_and_weight_decay(ctx, tmp_path, decay):
             p = ctx.get_params()
             assert len(p) == len(wm)
             ctx.adam_init(lr, b1, b2, eps)
-            ctx.adam_schedule(decay, alpha=alpha, period=period, reg=reg, eta=eta)
+            ctx.opt_schedule(decay, alpha=alpha, period=period, reg=reg, eta=eta)
             m = np.zeros_like(p); v = np.zeros_like(p)
             gamma, b1i, b2i = lr, b1, b2
             for t in range(4):
@@ -247,11 +247,108 @@ def test_adam_schedule_and_weight_decay(ctx, tmp_path, decay):
                 b1i *= b1; b2i *= b2
             assert np.allclose(ctx.get_params(), p, rtol=1e-10, atol=1e-13), (decay, reg)
         with pytest.raises(AnnError, match="decay"):
-            ctx.adam_schedule(7)
+            ctx.opt_schedule(7)
         with pytest.raises(AnnError, match="regularization"):
-            ctx.adam_schedule("CONST", reg=5)
+            ctx.opt_schedule("CONST", reg=5)
     finally:
-        ctx.adam_schedule()
+        ctx.opt_schedule()
+
+
+class _RefOpt:
+    """The reference's optimiser steps (src/opt/algo.cpp:97-660) in numpy, for the replay."""
+
+    def __init__(self, algo, n, gamma, eta, eps, w):
+        self.a, self.gamma, self.eta, self.eps, self.w = algo, gamma, eta, eps, w
+        self.s0 = np.full(n, 0.1) if algo == "RPROP" else np.zeros(n)
+        self.s1, self.s2, self.gold, self.cg = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n)
+        self.b1i, self.b2i, self.b1, self.b2 = 0.9, 0.999, 0.9, 0.999
+        self.val_old = 0.0
+
+    def step(self, p, g, val):
+        a, gm, eta, eps = self.a, self.gamma, self.eta, self.eps
+        b1, b2 = self.b1, self.b2
+        b1ii, b2ii = 1.0 / (1.0 - self.b1i), 1.0 / (1.0 - self.b2i)
+        p = p.copy(); g = g.copy()
+        if a == "SGD":
+            p -= gm * g
+        elif a in ("SDM", "NAG"):
+            self.s0 = eta * self.s0 + gm * ((eta + 1.0) if a == "NAG" else 1.0) * g
+            p -= self.s0
+        elif a == "ADAGRAD":
+            self.s0 += g * g; p -= gm * g / (np.sqrt(self.s0) + eps)
+        elif a == "ADADELTA":
+            self.s0 = eta * self.s0 + (1 - eta) * g * g
+            dx = g * np.sqrt(self.s1) / (np.sqrt(self.s0) + eps)
+            p -= dx
+            self.s1 = eta * self.s1 + (1 - eta) * dx * dx
+        elif a == "RMSPROP":
+            self.s0 = 0.9 * self.s0 + 0.1 * g * g; p -= gm * g / (np.sqrt(self.s0) + eps)
+        elif a in ("ADAM", "ADAMW", "ADAB", "YOGI", "NOGI", "NADAM", "AMSGRAD"):
+            self.s0 = self.s0 * b1 + (1 - b1) * g
+            if a == "ADAB":
+                self.s1 = self.s1 * b2 + (1 - b2) * (g - self.s0) * (g - self.s0) + eps
+            elif a in ("YOGI", "NOGI"):
+                self.s1 = self.s1 - (1 - b2) * np.sign(self.s1 - g * g) * (g * g)
+            else:
+                self.s1 = self.s1 * b2 + (1 - b2) * g * g
+            vv = self.s1
+            if a == "AMSGRAD":
+                self.s2 = np.maximum(self.s2, self.s1); vv = self.s2
+            mm = b1 * self.s0 + (1 - b1) * g if a in ("NOGI", "NADAM") else self.s0
+            if a == "ADAMW":
+                p -= gm * (b1ii * mm / (np.sqrt(b2ii * vv) + eps) + self.w * p)
+            else:
+                p -= gm * b1ii * mm / (np.sqrt(b2ii * vv) + eps)
+        elif a == "RPROP":
+            inc = val > self.val_old
+            sg = g * self.gold
+            up, dn, ze = sg > 0, sg < 0, sg == 0
+            self.s0[up] = np.minimum(self.s0[up] * 1.2, 50.0)
+            self.s1[up] = -1.0 * np.sign(g[up]) * self.s0[up]
+            p[up] += self.s1[up]
+            self.s0[dn] = np.maximum(self.s0[dn] * 0.5, 1e-14)
+            if inc:
+                p[dn] -= self.s1[dn]
+            g[dn] = 0.0
+            self.s1[ze] = -1.0 * np.sign(g[ze]) * self.s0[ze]
+            p[ze] += self.s1[ze]
+        elif a == "CG":
+            beta = np.dot(g, g - self.gold) / (np.dot(self.gold, self.gold) + eps)
+            self.cg = beta * self.cg - g
+            p += gm * self.cg
+        self.gold = g
+        self.val_old = val
+        self.b1i *= b1; self.b2i *= b2
+        return p
+
+
+@pytest.mark.parametrize("algo", ["SGD", "SDM", "NAG", "ADAGRAD", "ADADELTA", "RMSPROP", "ADAM", "ADAMW", "ADAB", "YOGI", "NOGI",
+                                  "NADAM", "AMSGRAD", "RPROP", "CG"])
+def test_every_optimiser_matches_reference_steps(ctx, tmp_path, algo):
+    """Every optimiser of the reference trainer on the device: three steps with the gradients and
+    losses of the same batch against a numpy replay of opt::algo's step (CG's dot products on the
+    device in a fixed order: 1e-9)."""
+    text = cases.config_potential(ctx, 3, tmp_path)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    ctx.load_text(text)
+    p = ctx.get_params()
+    gamma, eta, eps, w = 1e-3, 0.5, 1e-8, 0.01
+    ctx.opt_init(algo, gamma=gamma, eta=eta, eps=eps, w=w)
+    ref = _RefOpt(algo, len(p), gamma, eta, eps, w)
+    for _ in range(3):
+        loss = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+        g = ctx.train_backward()
+        ctx.opt_step()
+        p = ref.step(p, g, loss[0])
+    assert np.allclose(ctx.get_params(), p, rtol=1e-9, atol=1e-12), algo
+
+
+def test_optimiser_errors(ctx, tmp_path):
+    cases.config_potential(ctx, 3, tmp_path)
+    with pytest.raises(AnnError, match="BFGS"):
+        ctx.opt_init("BFGS")
+    with pytest.raises(AnnError, match="algorithm"):
+        ctx.opt_init(17)
 
 
 def test_compute_after_md_leaves_md(ctx, tmp_path):
