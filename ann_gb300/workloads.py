@@ -216,6 +216,88 @@ def precondition(ctx, offs, posn, types, cell, symm=None):
         ctx.set_input_scaling(t, w, -mu)
 
 
+# ------------------------------------------------------------ a pair potential held by a network
+def radial_eta(n_radial: int) -> np.ndarray:
+    """The radial widths potential_text writes (eta = sqrt(eta_B), eta_B log-spaced 0.01..1 A^-2),
+    rounded as they are printed, so that host-side sums match the loaded potential."""
+    return np.array([float(f"{np.sqrt(e):f}") for e in np.logspace(np.log10(0.01), np.log10(1.0), n_radial)])
+
+
+def _radial_g(r, rc, eta):
+    """GAUSSIAN radial functions with rs = 0 and the COS cutoff, g_i(r) = exp(-(eta_i r)^2) fc(r),
+    and their r-derivatives (basis_radial.cpp:268-272, cutoff.hpp COS)."""
+    r = np.asarray(r, float)[:, None]
+    inside = r < rc
+    fc = np.where(inside, 0.5 * (np.cos(np.pi * r / rc) + 1.0), 0.0)
+    dfc = np.where(inside, -0.5 * np.pi / rc * np.sin(np.pi * r / rc), 0.0)
+    e = np.exp(-(eta[None, :] * r) ** 2)
+    return e * fc, e * (-2.0 * eta[None, :] ** 2 * r * fc + dfc)
+
+
+def lj_pair_coefficients(rc, eta, eps=0.0104, sig=3.405, r0=3.0, lam=1e-8):
+    """c such that phi(r) = 2 c.g(r) follows the Lennard-Jones pair energy shifted to zero at rc
+    (argon: eps 10.4 meV, sigma 3.405 A) on [r0, rc]: ridge-regularised least squares on values and
+    derivatives, weighted towards the first-neighbour shell. A network whose atomic energy is c.G
+    then carries phi as its pair potential, since sum_atoms c.G_atom = sum_pairs 2 c.g(r)."""
+    r = np.linspace(r0, rc, 400)
+    g, dg = _radial_g(r, rc, eta)
+    u = (sig / r) ** 6
+    phi = 4.0 * eps * u * (u - 1.0) - 4.0 * eps * ((sig / rc) ** 6) * ((sig / rc) ** 6 - 1.0)
+    dphi = -24.0 * eps * u * (2.0 * u - 1.0) / r
+    w = np.tile(np.exp(-0.5 * (r - 3.8) ** 2) + 0.05, 2)
+    A = np.vstack([g, 0.3 * dg]) * w[:, None]
+    b = np.concatenate([phi, 0.3 * dphi]) / 2.0 * w
+    return np.linalg.solve(A.T @ A + lam * np.eye(len(eta)), A.T @ b)
+
+
+def fcc_radial_sums(a, rc, eta) -> np.ndarray:
+    """Per-atom radial symmetry functions G_i = sum_j g_i(r_j) of a perfect FCC crystal."""
+    n = int(np.ceil(rc / a)) + 1
+    basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(*[np.arange(-n, n + 1)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    d = np.linalg.norm(((g[:, None, :] + basis[None]).reshape(-1, 3)) * a, axis=1)
+    d = d[(d > 1e-9) & (d < rc)]
+    return _radial_g(d, rc, eta)[0].sum(axis=0)
+
+
+def linear_network(coef, nin: int, nodes, seed: int, scale: float = 0.003, out_bias: float = 0.0):
+    """Packed parameters (reference packing, nn.cpp:846-859) of a tanh network whose output is
+    coef.z + out_bias to a relative 1e-5 over |coef.z| <= 1: the first layer writes scale*u_k*(coef.z)
+    into every unit (u ~ N(0,1)), the second mixes them with N(0,1/32) weights, and the output
+    weights are rescaled so the small-signal gain is one. Every unit is active, so the network
+    costs what a trained one does."""
+    rng = np.random.default_rng(seed)
+    coef = np.asarray(coef, float)
+    h1, h2 = nodes[0], nodes[1]
+    u = rng.normal(0.0, 1.0, h1)
+    W1 = scale * np.outer(np.pad(coef, (0, nin - len(coef))), u)           # [in, out]
+    W2 = rng.normal(0.0, 1.0 / np.sqrt(h1), (h1, h2))
+    w3 = rng.normal(0.0, 1.0 / np.sqrt(h2), h2)
+    w3 /= scale * float(u @ W2 @ w3)
+    biases = np.concatenate([np.zeros(h1), np.zeros(h2), [out_bias]])
+    return np.concatenate([biases, W1.reshape(-1), W2.reshape(-1), w3])
+
+
+def lj_argon_text(cfg: int = 5, a: float = 5.26, seed: int | None = None) -> str:
+    """The configuration's potential (one type, tanh networks) with weights that make it the
+    Lennard-Jones argon pair potential of lj_pair_coefficients: radial inputs shifted by their FCC
+    values at lattice constant a (inpb = -G(a), so c.z stays small and free of cancellation), the
+    angular inputs weighted zero, and c.G(a) as the output bias. Unlike randomly initialised
+    weights, which attract atoms without bound, this keeps an FCC crystal stable under MD."""
+    spec = CONFIG_POT[cfg]
+    assert len(spec["names"]) == 1 and spec["neuron"] == "TANH" and len(spec["nodes"]) == 3
+    rc, nr = spec["rc"], spec["n_radial"]
+    eta = radial_eta(nr)
+    c = lj_pair_coefficients(rc, eta)
+    G0 = fcc_radial_sums(a, rc, eta)
+    nin = nr + len(spec["ang_eta_b"]) * 8
+    p = linear_network(c, nin, spec["nodes"], SEED0 + cfg if seed is None else seed, out_bias=float(c @ G0))
+    text = set_network_text(potential_text(**spec), [p], nin, spec["nodes"])
+    inpb = np.concatenate([-G0, np.zeros(nin - nr)])
+    return "\n".join(("inpb " + " ".join(f"{v:.15f}" for v in inpb) + " ") if ln.startswith("inpb ") else ln
+                     for ln in text.splitlines()) + "\n"
+
+
 # ---------------------------------------------------------------------------------- structures
 def fcc(nx, ny, nz, a):
     basis = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])

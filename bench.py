@@ -203,14 +203,17 @@ def training_leg(dev, steps=10, warmup=3):
 
 
 def md_leg(dev, steps=1000, warmup=20):
-    """Velocity-Verlet MD of the 262,144-atom FCC argon box (16-32-32-1 tanh networks, dt = 2 fs,
-    list cutoff rc + 0.5 A, rebuild at 0.25 A displacement), mixed precision: atom-steps/s and
-    the total-energy drift."""
+    """Velocity-Verlet MD of the 262,144-atom FCC argon box (16-32-32-1 tanh networks whose weights
+    hold a Lennard-Jones argon pair potential, workloads.lj_argon_text; dt = 2 fs, list cutoff
+    rc + 0.5 A, rebuild at 0.25 A displacement), mixed precision: atom-steps/s, the total-energy
+    drift and the final temperature. The crystal stays a crystal, so the per-step cost is that of
+    a fixed neighbour count (randomly initialised weights attract atoms without bound: the box
+    collapses, heats to thousands of kelvin and the triplet count triples within 2 ps)."""
     from ann_gb300 import MIXED, Context
     from ann_gb300 import workloads as WL
     x, v, t, R = WL.config5()
     ctx = Context(device=dev)
-    WL.make_potential(ctx, 5)
+    ctx.load_text(WL.lj_argon_text(5))
     ctx.md_init(x, v, t, R, np.array([WL.MASS["Ar"]]), dt_fs=2.0, skin=0.5, precision=MIXED)
     ctx.md_run(warmup)
     pe0, ke0, _ = ctx.md_run(1)
@@ -222,20 +225,22 @@ def md_leg(dev, steps=1000, warmup=20):
     ctx.close()
     return {"workload": f"FCC Ar {n} atoms, 80 K, dt 2 fs, {steps} steps", "atom_steps_per_s": n * steps / dt,
             "ms_per_step": dt / steps * 1e3, "rebuilds": int(rebuilds),
-            "drift_mev_atom_ps": float((pe + ke - pe0 - ke0) / n * 1e3 / ps), "precision": "mixed"}
+            "drift_mev_atom_ps": float((pe + ke - pe0 - ke0) / n * 1e3 / ps),
+            "T_end_K": float(2.0 * ke / (3.0 * n * 8.617333262e-5)), "precision": "mixed"}
 
 
 def lammps_leg(dev, steps=20, warmup=3, skin=2.0):
     """The LAMMPS pair-style path (ann_compute_list) on the 262,144-atom FCC argon box (16-32-32-1
-    tanh networks, mixed precision) as one MD domain: local atoms plus ghosts within rc + skin
-    (LAMMPS's default metal-units skin, 2 A), a full list of the same radius. Times, end to end
-    from host arrays to host forces of all local and ghost atoms: a reneighbouring step (list, types
-    and positions sent) and a step between reneighbourings (ANN_LIST_KEEP: positions only)."""
+    tanh networks holding the Lennard-Jones argon potential, mixed precision) as one MD domain:
+    local atoms plus ghosts within rc + skin (LAMMPS's default metal-units skin, 2 A), a full list
+    of the same radius. Times, end to end from host arrays to host forces of all local and ghost
+    atoms: a reneighbouring step (list, types and positions sent) and a step between
+    reneighbourings (ANN_LIST_KEEP: positions only)."""
     from ann_gb300 import MIXED, Context
     from ann_gb300 import workloads as WL
     x, _, t, R = WL.config5()
     ctx = Context(device=dev)
-    WL.make_potential(ctx, 5)
+    ctx.load_text(WL.lj_argon_text(5))
     X, T, owner, nn, nb = WL.ghost_domain(x, t, R, ctx.rc + skin)
     n, nall = len(t), len(X)
 

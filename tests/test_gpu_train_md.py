@@ -151,6 +151,29 @@ def test_md_energy_conservation(ctx, tmp_path, prec):
     assert rebuilds >= 0
 
 
+def test_md_lj_argon_crystal_mixed(ctx):
+    """mixed-precision MD of an FCC argon box (256 atoms) under the networks that hold a
+    Lennard-Jones pair potential: over 2 ps the crystal holds (minimum distance > 3 A, temperature
+    near equipartition of the 80 K start) and the total energy drifts < 0.05 meV/atom"""
+    ctx.load_text(W.lj_argon_text(5))
+    x, v, t, R = W.config5(cells=(4, 4, 4))
+    ctx.md_init(x, v, t, R, np.array([W.MASS["Ar"]]), dt_fs=2.0, skin=0.5, precision=MIXED)
+    pe0, ke0, _ = ctx.md_run(1)
+    pe, ke, rebuilds = ctx.md_run(1000)
+    n = len(t)
+    T = 2 * ke / (3 * n * 8.617333262e-5)
+    assert 15.0 < T < 70.0, T
+    assert abs(pe + ke - pe0 - ke0) / n < 5e-5, (pe + ke - pe0 - ke0) / n
+    xs = ctx.md_state()[0]
+    d = xs[:, None] - xs[None]
+    Ls = np.diag(R)
+    d -= Ls * np.round(d / Ls)
+    dd = np.linalg.norm(d, axis=2)
+    np.fill_diagonal(dd, np.inf)
+    assert dd.min() > 3.0
+    assert rebuilds < 1000
+
+
 @pytest.mark.parametrize("neuron", ["GELU", "MISH", "SERF", "ARCTAN", "TEST"])
 def test_gradient_other_activations(ctx, oracle, neuron):
     """the force-term adjoint through f'' of the other activations, FP64 vs the oracle"""
