@@ -31,7 +31,7 @@ class AnnError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("newton", C.c_int32), ("max_neighbors", C.c_int32),
-                ("use_graphs", C.c_int32), ("mlp_backend", C.c_int32)]
+                ("use_graphs", C.c_int32), ("mlp_backend", C.c_int32), ("tc_groups", C.c_int32)]
 
 
 def library_path() -> Path:
@@ -173,12 +173,12 @@ class Context:
     """One device context: a loaded potential plus device buffers (one per host thread)."""
 
     def __init__(self, device: int = 0, precision: int = MIXED, newton: int = NEWTON_ALL_IMAGES, max_neighbors: int = 0,
-                 use_graphs: bool = True, mlp_backend: int = 0):
+                 use_graphs: bool = True, mlp_backend: int = 0, tc_groups: int = 0):
         self.lib = load_library()
         o = Options()
         self.lib.ann_default_options(C.byref(o))
         o.device, o.precision, o.newton, o.max_neighbors = device, precision, newton, max_neighbors
-        o.use_graphs, o.mlp_backend = int(use_graphs), mlp_backend
+        o.use_graphs, o.mlp_backend, o.tc_groups = int(use_graphs), mlp_backend, tc_groups
         h = _V()
         rc = self.lib.ann_create(C.byref(h), C.byref(o))
         if rc != 0:

@@ -42,7 +42,7 @@ static void upload_params(ann_ctx* c, ParamSet<real>& P) {
 static void reset_graph(ann_ctx* c) {
     for (int k = 0; k < 2; ++k) {
         if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
-        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, 0};
+        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, -1, 0};
     }
 }
 void rebuild_plan(ann_ctx* c) {
@@ -260,6 +260,9 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
         ck(cudaEventRecord(c->ev_join, c->side), "event record");
     }
     mark(c, 0);
+    // MD: the list holds rc + skin and is rebuilt only when an atom moved skin/2; between
+    // rebuilds its pair vectors are recomputed from the current positions
+    if (!build_list && !c->md_ready) throw ann_error(ANN_ERR_STATE, "a list refresh outside MD");
     if (build_list) launch_neighbors(nbr_args(c, c->pot.rc + (c->md_ready ? c->md_skin : 0.0)), fp64, st);
     else launch_refresh_geometry(nbr_args(c, c->pot.rc + c->md_skin), fp64, st);
     check_phase(c, "neighbour list");
@@ -300,7 +303,7 @@ void run_batch(ann_ctx* c, int prec, bool forces, bool build_list) {
                                               " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
     if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
-    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), g_alloc_gen.load()};
+    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), c->md_ready ? 1 : 0, g_alloc_gen.load()};
     const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
     const int gs = build_list ? 0 : 1;
     if (graphs) {
@@ -379,6 +382,7 @@ extern "C" {
 void ann_default_options(ann_options* o) {
     if (!o) return;
     o->device = 0; o->precision = ANN_MIXED; o->newton = ANN_NEWTON_ALL_IMAGES; o->max_neighbors = 0; o->use_graphs = 1; o->mlp_backend = 0;
+    o->tc_groups = 0;
 }
 int ann_abi_version(void) { return ANN_GPU_ABI_VERSION; }
 
@@ -401,6 +405,8 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->opt.device);
         cudaDeviceGetAttribute(&c->tc.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->opt.device);
         if (c->opt.mlp_backend < 0 || c->opt.mlp_backend > 2) throw ann_error(ANN_ERR_ARG, "mlp_backend must be 0, 1 or 2");
+        if (c->opt.tc_groups != 0 && c->opt.tc_groups != 1 && c->opt.tc_groups != 2 && c->opt.tc_groups != 4)
+            throw ann_error(ANN_ERR_ARG, "tc_groups must be 0, 1, 2 or 4");
         const char* dbg = std::getenv("ANN_DEBUG");
         c->debug = dbg && dbg[0] == '1';
         if (c->debug) c->opt.use_graphs = 0;

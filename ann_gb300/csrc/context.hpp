@@ -86,10 +86,11 @@ inline void ck(cudaError_t e, const char* what) {
 
 struct GraphKey {
     int S, N, cap, prec, forces, nbins, nchunks;
+    int md;         // MD mode: list cutoff rc + skin, refreshed between rebuilds
     uint64_t gen;   // g_alloc_gen at capture
     bool operator==(const GraphKey& o) const {
         return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins && nchunks == o.nchunks &&
-               gen == o.gen;
+               md == o.md && gen == o.gen;
     }
 };
 
@@ -223,7 +224,7 @@ inline void enqueue_networks(ann_ctx* c, int natoms, DevBuf& G, DevBuf& dEdG, De
             ta.tstart = tstart.as<int32_t>(); ta.tlist = tlist.as<int32_t>();
             ta.G = G.as<float>(); ta.dEdG = dEdG.as<float>(); ta.Eatom = Eatom.as<double>();
             ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>();
-            launch_mlp_tc(c->tc.t[ty], ta, c->tc.smem_bytes(ty), c->stream);
+            launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->opt.tc_groups, c->tc.smem_bytes(ty), c->stream);
         }
     } else {
         MlpArgs<real> m{};

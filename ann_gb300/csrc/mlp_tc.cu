@@ -4,8 +4,9 @@
 // Reference: NN::ANN::fpbp (src/ml/nn.cpp:1343-1409), NN::DODZ::grad (nn.cpp:1801-1824) and
 // NNH::energy (src/nnp/nnh.cpp:118-121), the same computation as the SIMT kernel in mlp.cu.
 //
-// Per CTA (512 threads: 4 warps per TMEM lane quadrant; tile row r <-> TMEM lane r), persistent
-// over the type's tiles:
+// Per CTA (128 x G threads: G warps per TMEM lane quadrant, G = 1, 2 or 4 so that 4 / G CTAs share
+// an SM when tensor memory allows and the type has tiles enough; tile row r <-> TMEM lane r),
+// persistent over the type's tiles:
 //   weights   : one bulk asynchronous copy (cp.async.bulk + mbarrier) of the type's image
 //               (B operands W_l and W_l^T in the canonical K-major no-swizzle layout, BF16 hi/lo).
 //   per tile  : A0 = inpw*(G+inpb) split into BF16 hi+lo rows, then for every hidden layer
@@ -138,11 +139,10 @@ static __device__ __forceinline__ void tc_st16(uint32_t taddr, const float (&v)[
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-// TC_GROUPS warps share each TMEM lane quadrant (warp w: rows 32*(w%4).., column chunks c with
-// c % TC_GROUPS == w / 4), so an epilogue runs on TC_GROUPS * 4 warps
-constexpr int TC_THREADS = TC_M * TC_GROUPS;
-
-__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant__ TcType tt, const TcArgs a) {
+// G warps share each TMEM lane quadrant (warp w: rows 32*(w%4).., column chunks c with
+// c % G == w / 4), so an epilogue runs on G * 4 warps; 4 / G CTAs share an SM (tc_groups)
+template <int G>
+__global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constant__ TcType tt, const TcArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int quad = warp & 3, grp = warp >> 2;
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
     uint8_t* Alo = (tt.split >= 2) ? Ahi + abytes : nullptr;
     uint64_t* bar = reinterpret_cast<uint64_t*>(Ahi + abytes * (tt.split >= 2 ? 2 : 1));
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
-    float* ered = reinterpret_cast<float*>(bar + 4);      // [TC_GROUPS][TC_M] energy partial sums
+    float* ered = reinterpret_cast<float*>(bar + 4);      // [G][TC_M] energy partial sums
     const uint32_t asbo = (uint32_t)tt.wmax * 16u;   // (wmax / 8) * 128
 
     if (t == 0) { tc_mbar_init(&bar[0]); tc_mbar_init(&bar[1]); }
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
         // ---- A0 = inpw * (G + inpb), 8-column chunks shared out over the groups
         // rows 16-byte aligned (row length and base pointers): vector loads / stores of full chunks
         const bool vec = (a.imax & 3) == 0 && ((reinterpret_cast<uintptr_t>(a.G) | reinterpret_cast<uintptr_t>(a.dEdG)) & 15) == 0;
-        for (int c0 = grp * 8; c0 < tt.K0; c0 += 8 * TC_GROUPS) {
+        for (int c0 = grp * 8; c0 < tt.K0; c0 += 8 * G) {
             float v[8];
             if (vec && at >= 0 && c0 + 8 <= tt.nin) {
                 const float4 g0 = *reinterpret_cast<const float4*>(Grow + c0), g1 = *reinterpret_cast<const float4*>(Grow + c0 + 4);
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
             if (!good) break;
             const float* bias = reinterpret_cast<const float*>(img + tt.bias[l]);
             const bool last = (l == tt.nhidden - 1);
-            for (int c0 = grp * 16; c0 < N; c0 += 16 * TC_GROUPS) {
+            for (int c0 = grp * 16; c0 < N; c0 += 16 * G) {
                 float v[16], o[16];
                 const uint32_t ta = tmem + lane_off + (uint32_t)(tt.fwd_col[l] + c0);
                 tc_ld16(ta, v);
@@ -274,11 +274,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
             if (l == tt.nhidden - 1 && grp == 0 && at >= 0) {   // ered is complete after the GEMM's barrier
                 float e = 0.0f;
 #pragma unroll
-                for (int g = 0; g < TC_GROUPS; ++g) e += ered[g * TC_M + r];
+                for (int g = 0; g < G; ++g) e += ered[g * TC_M + r];
                 const float blast = *reinterpret_cast<const float*>(img + tt.blast);
                 a.Eatom[at] = (double)(tt.outb + tt.outw * (e + blast)) + tt.evac;
             }
-            for (int c0 = grp * 16; c0 < Nout; c0 += 16 * TC_GROUPS) {
+            for (int c0 = grp * 16; c0 < Nout; c0 += 16 * G) {
                 float gv[16];
                 tc_ld16(tmem + lane_off + (uint32_t)(tt.bwd_col + c0), gv);
                 if (l > 0) {
@@ -321,12 +321,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant_
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)tt.tmem_cols) : "memory");
 }
 
-void launch_mlp_tc(const TcType& tt, const TcArgs& a, size_t smem, cudaStream_t st) {
+void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, cudaStream_t st) {
     if (a.natoms <= 0) return;
+    // a forced split cannot oversubscribe tensor memory: smem_bytes admits at most 512 / tmem_cols
+    // CTAs per SM whatever their width
+    const int g = groups ? groups : tc_groups(tt, est_atoms, 152);
     int grid = (a.natoms + TC_M - 1) / TC_M;
-    grid = std::min(grid, 152);
-    ++::ann::g_launch_counter, k_mlp_tc<<<grid, TC_THREADS, smem, st>>>(tt, a);
+    grid = std::min(grid, 152 * (4 / g));
+    ++::ann::g_launch_counter;
+    if (g == 1) k_mlp_tc<1><<<grid, TC_M, smem, st>>>(tt, a);
+    else if (g == 2) k_mlp_tc<2><<<grid, TC_M * 2, smem, st>>>(tt, a);
+    else k_mlp_tc<4><<<grid, TC_M * 4, smem, st>>>(tt, a);
 }
-void configure_mlp_tc(int maxsmem) { set_max_dynamic_smem(k_mlp_tc, maxsmem); }
+void configure_mlp_tc(int maxsmem) {
+    set_max_dynamic_smem(k_mlp_tc<1>, maxsmem);
+    set_max_dynamic_smem(k_mlp_tc<2>, maxsmem);
+    set_max_dynamic_smem(k_mlp_tc<4>, maxsmem);
+}
 
 }  // namespace ann

@@ -10,7 +10,7 @@ namespace ann {
 
 constexpr int TC_M = 128;          // atoms per tile (one TMEM lane each)
 constexpr int TC_MAXH = 5;         // hidden layers
-constexpr int TC_GROUPS = 4;       // warps per TMEM lane quadrant (the epilogue's column split)
+constexpr int TC_GROUPS = 4;       // most warps per TMEM lane quadrant (the epilogue's column split)
 // shared memory after the A tiles: 2 mbarriers, the TMEM address, per-group energy partials
 constexpr int TC_TAIL_BYTES = 32 + 4 * TC_GROUPS * TC_M;
 
@@ -41,6 +41,19 @@ struct TcType {
     int32_t tmem_cols;               // allocated TMEM columns (power of two, <= 512)
     int32_t split;                   // 1: A and B single BF16; 2: A split hi+lo; 3: A and B split
 };
+
+// Warps per lane quadrant for a type's launch. A CTA is latency-bound on its chain of small GEMMs
+// and epilogues; with 128 x G threads of up to 128 registers, 4 / G CTAs share an SM (as far as
+// tensor memory allows, 512 / tmem_cols). More, narrower CTAs pay off only when each still gets
+// a few tiles to amortise its prologue (weight image copy, TMEM allocation): the finest split
+// whose CTAs get at least two tiles of est_atoms atoms, else G = 4 (one CTA per SM).
+inline int tc_groups(const TcType& tt, long long est_atoms, int nsm) {
+    const int allowed = 512 / (tt.tmem_cols > 32 ? tt.tmem_cols : 32);
+    const long long tiles = (est_atoms + TC_M - 1) / TC_M;
+    for (int per_sm = 4; per_sm >= 2; per_sm /= 2)
+        if (per_sm <= allowed && tiles >= 2LL * nsm * per_sm) return 4 / per_sm;
+    return 4;
+}
 
 struct TcPlan {
     bool ok = false;                 // every type fits the tensor-core kernel
@@ -77,7 +90,9 @@ struct TcArgs {
     const uint8_t* image;            // device copy of TcPlan::image
     int32_t* status;
 };
-void launch_mlp_tc(const TcType& tt, const TcArgs& a, size_t smem, cudaStream_t st);
+// est_atoms: the expected atoms of the type (its count is known on the device only); groups:
+// 1, 2 or 4 to force the split, 0 to choose it (tc_groups)
+void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, cudaStream_t st);
 void configure_mlp_tc(int maxsmem);
 
 }  // namespace ann

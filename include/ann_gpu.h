@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define ANN_GPU_ABI_VERSION 1
+#define ANN_GPU_ABI_VERSION 2
 
 enum ann_status {
     ANN_OK = 0,
@@ -69,6 +69,8 @@ typedef struct ann_options {
     int32_t max_neighbors;       /* initial neighbour capacity per atom (0 = estimate from density)   */
     int32_t use_graphs;          /* capture the per-batch kernel sequence in a CUDA graph (1 = yes)   */
     int32_t mlp_backend;         /* 0 = auto, 1 = SIMT kernels, 2 = tcgen05 tensor-core kernels (MIXED) */
+    int32_t tc_groups;           /* tensor-core network kernel: warps per TMEM lane quadrant, 1, 2 or 4 */
+                                 /* (4 / tc_groups CTAs per SM); 0 = chosen per launch                 */
 } ann_options;
 
 typedef struct ann_ctx ann_ctx;

@@ -108,3 +108,26 @@ def test_too_wide_for_tensor_core_is_reported(contexts, tmp_path):
         _mixed_bars(E, F, E64, F64, offs)
     finally:
         auto.close()
+
+
+@pytest.mark.parametrize("groups", [1, 2, 4])
+def test_forced_warp_split(contexts, tmp_path, groups):
+    """Each width of the kernel (1, 2 or 4 warps per TMEM lane quadrant, 4, 2 or 1 CTAs per SM)
+    against FP64: a batch with many tiles per CTA, a ragged one-type batch and odd layer widths."""
+    _, simt = contexts
+    tc = Context(mlp_backend=2, tc_groups=groups)
+    try:
+        structs = cases.W.config2(nstruc=160)
+        offs, posn, types, cell = cases.batch(structs)
+        text = cases.config_potential(tc, 2, tmp_path, precondition_batch=(offs, posn, types, cell))
+        _compare(tc, simt, text, structs)
+        one_type = [(x, np.zeros_like(t), R) for (x, t, R) in cases.small_binary(n_struc=2, seed=3)]
+        _compare(tc, simt, text, one_type)
+        _compare(tc, simt, cases.generic_potential_text(), cases.small_binary(n_struc=3, seed=21) + cases.tiny_cells())
+    finally:
+        tc.close()
+
+
+def test_tc_groups_validated(gpu_lib):
+    with pytest.raises(AnnError):
+        Context(tc_groups=3)

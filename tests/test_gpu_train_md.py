@@ -138,6 +138,34 @@ def test_md_steps_match_oracle(ctx, oracle, tmp_path):
         assert abs(pe - peo) < 1e-9 * max(1.0, abs(peo)) and abs(ke - keo) < 1e-9 * max(1.0, keo)
 
 
+def test_md_multitype_steps_match_oracle(ctx, oracle, tmp_path):
+    """three species, so every MD step compacts type-sorted list rows segment by segment: FP64
+    steps against the oracle, and the MIXED forces of the first step within 10 meV/A"""
+    text = cases.config_potential(ctx, 4, tmp_path)
+    pot = oracle.load_text(text)
+    [(x, t, R)] = cases.ternary_box(dims=(8, 8, 6))
+    masses = np.array([39.948, 20.180, 83.798])
+    v = np.random.default_rng(4).normal(0.0, 0.002, x.shape)
+    offs, _, _, cell = pack_batch([(x, t, R)])
+    ctx.md_init(x, v, t, R, masses, dt_fs=1.0, skin=0.5, precision=MIXED)
+    Fm = ctx.md_state()[2]
+    ctx.md_init(x, v, t, R, masses, dt_fs=1.0, skin=0.5, precision=FP64)
+    xo, vo = x.copy(), v.copy()
+    Fo = pot.compute(offs, xo, t, cell)[1]
+    assert np.abs(Fm - Fo).max() < 10e-3
+    Ri = np.linalg.inv(R)
+    for step in range(5):
+        pe, ke, _ = ctx.md_run(1)
+        peo, keo = pot.md_step(xo, vo, t, R, masses, 1.0, Fo)
+        xg, vg, fg = ctx.md_state()
+        d = xg - xo
+        d -= (np.round(d @ Ri.T)) @ R.T
+        assert np.abs(d).max() < 1e-9
+        assert np.abs(vg - vo).max() < 1e-10
+        assert np.abs(fg - Fo).max() < 1e-8 * max(1.0, np.abs(Fo).max())
+        assert abs(pe - peo) < 1e-9 * max(1.0, abs(peo)) and abs(ke - keo) < 1e-9 * max(1.0, keo)
+
+
 @pytest.mark.parametrize("prec", [FP64, MIXED])
 def test_md_energy_conservation(ctx, tmp_path, prec):
     cases.config_potential(ctx, 5, tmp_path)
