@@ -370,6 +370,39 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
     const int qb = TRI ? p0 : q0;
     int part = TRI ? lane + 1 : lane;
     if (part >= n) part -= n;
+    if constexpr (std::is_same<real, float>::value && NG <= 2) {
+        // FP32: the slot pair (lambda = +1, lambda = -1) of each zeta in one packed register,
+        // (|1/2 + cos/2|^zeta, |1/2 - cos/2|^zeta) by packed squaring, accumulated by packed FMA
+        uint64_t acc2[S / 2];
+#pragma unroll
+        for (int k = 0; k < S / 2; ++k) acc2[k] = pk2(acc[2 * k], acc[2 * k + 1]);
+#pragma unroll 2   // two independent triplets per iteration
+        for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
+            const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
+            const int e = qb + (valid ? part : 0);
+            const R4 gb = w.geo[e];
+            DampRec<real, NG> db;
+            db.load(w.dp + e * NDP);
+            const float cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
+            uint64_t pw[4];
+            pw[0] = pk2(fabsf(0.5f + 0.5f * cs), fabsf(0.5f - 0.5f * cs));
+            pw[1] = mul2(pw[0], pw[0]); pw[2] = mul2(pw[1], pw[1]); pw[3] = mul2(pw[2], pw[2]);
+#pragma unroll
+            for (int g = 0; g < NG; ++g) {
+                const float DD = valid ? da.D(g) * db.D(g) : 0.0f;
+                const uint64_t D2 = pk2(DD, DD);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc2[g * 4 + q] = fma2(pw[q], D2, acc2[g * 4 + q]);
+            }
+            part = (part + 1 == n) ? 0 : part + 1;
+        }
+#pragma unroll
+        for (int k = 0; k < S / 2; ++k) {
+            float lo, hi;
+            asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc2[k]));
+            acc[2 * k] = lo; acc[2 * k + 1] = hi;
+        }
+    } else {
 #pragma unroll 2   // two independent triplets per iteration
     for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
         const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
@@ -389,6 +422,7 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
             for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
         }
         part = (part + 1 == n) ? 0 : part + 1;
+    }
     }
 }
 
