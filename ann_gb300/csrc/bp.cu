@@ -666,6 +666,47 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                     }
                     TriIter<ROWS> ti; RectIter<ROWS> ri;
                     if (PASS == PASS_JVP) { if (J == K) ti.init(nJ, lane); else ri.init(max(nJ, 1), max(nK, 1), lane); }
+                    if constexpr (PASS == PASS_JVP && std::is_same<real, float>::value && NG <= 2) {
+                        // FP32: the (lambda = +1, lambda = -1) pair of each zeta in one packed
+                        // register; d|1/2 +- cos/2|^zeta = +-(zeta/2) |.|^(zeta-1) dcos
+                        uint64_t acc2[S / 2];
+#pragma unroll
+                        for (int k2 = 0; k2 < S / 2; ++k2) acc2[k2] = pk2(acc[2 * k2], acc[2 * k2 + 1]);
+                        for (int t = lane; t < total; t += 32) {
+                            int j, k;
+                            if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
+                            else { j = aJ + ri.q; k = aK + ri.c; ri.adv(); }
+                            const R4 gj = w.geo[j], gk = w.geo[k];
+                            DampRec<real, NG> dj, dk;
+                            dj.load(w.dp + j * NDP); dk.load(w.dp + k * NDP);
+                            const float cs = gj.x * gk.x + gj.y * gk.y + gj.z * gk.z;
+                            uint64_t pw[4], kq[4];
+                            pw[0] = pk2(fabsf(0.5f + 0.5f * cs), fabsf(0.5f - 0.5f * cs));
+                            pw[1] = mul2(pw[0], pw[0]); pw[2] = mul2(pw[1], pw[1]); pw[3] = mul2(pw[2], pw[2]);
+                            kq[0] = pk2(0.5f, -0.5f);                                  // (zeta/2) cw^(zeta-1), zeta = 1
+                            kq[1] = mul2(pw[0], pk2(1.0f, -1.0f));                     // zeta = 2
+                            kq[2] = mul2(mul2(pw[0], pw[1]), pk2(2.0f, -2.0f));        // zeta = 4
+                            kq[3] = mul2(mul2(mul2(pw[0], pw[1]), pw[2]), pk2(4.0f, -4.0f));   // zeta = 8
+                            const R4 tj = w.tg[j], tk = w.tg[k];
+                            const float idj = gj.w, idk = gk.w;
+                            const float dcos = (tj.x * gk.x + tj.y * gk.y + tj.z * gk.z) * idj +
+                                               (tk.x * gj.x + tk.y * gj.y + tk.z * gj.z) * idk - cs * (tj.w * idj + tk.w * idk);
+#pragma unroll
+                            for (int g = 0; g < NG; ++g) {
+                                const float DD = dj.D(g) * dk.D(g);
+                                const float dDD = dj.Dp(g) * dk.D(g) * tj.w + dj.D(g) * dk.Dp(g) * tk.w;
+                                const uint64_t a2 = pk2(DD * dcos, DD * dcos), b2 = pk2(dDD, dDD);
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) acc2[g * 4 + q] = fma2(kq[q], a2, fma2(pw[q], b2, acc2[g * 4 + q]));
+                            }
+                        }
+#pragma unroll
+                        for (int k2 = 0; k2 < S / 2; ++k2) {
+                            float lo, hi;
+                            asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc2[k2]));
+                            acc[2 * k2] = lo; acc[2 * k2 + 1] = hi;
+                        }
+                    } else {
                     for (int t = lane; PASS == PASS_JVP && t < total; t += 32) {
                         int j, k;
                         if (J == K) { j = aJ + ti.j(); k = aJ + ti.k(); ti.adv(); }
@@ -697,6 +738,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                                 acc[g * 8 + 2 * q + 1] += -z * real(0.5) * qm[q] * DD * dcos + pm[q] * dDD;
                             }
                         }
+                    }
                     }
                     if (PASS != PASS_FORCE) {
                         const real v = warp_slot_reduce<real, S>(acc, lane);
