@@ -104,6 +104,8 @@ _SIGS = {
     "ann_md_run": (C.c_int, [_V, C.c_int32, _D, _D, _I32]),
     "ann_md_get_state": (C.c_int, [_V, _D, _D, _D]),
     "ann_network_noalloc": (C.c_int, [_V, C.c_int32, _V, _V, _V, _V, C.c_int32]),
+    "ann_autotune": (C.c_int, [_V, C.c_int32, C.c_int32, _V]),
+    "ann_set_tuning": (C.c_int, [_V, _V]),
 }
 
 ABI_SYMBOLS = tuple(_SIGS)
@@ -167,6 +169,16 @@ def pack_batch(structures):
     cell = np.ascontiguousarray(np.stack([np.asarray(R, dtype=np.float64).T.reshape(9) for _, _, R in structures])
                                 if structures else np.zeros((0, 9)), dtype=np.float64)
     return offs, posn, types, cell
+
+
+class Tuning(C.Structure):
+    """ann_tuning: launch shapes of the E+F sequence (0 = the built-in rule)."""
+    _fields_ = [("tc_groups", C.c_int32 * 4), ("bp_blocks_per_sm", C.c_int32), ("nbr_blocks_per_sm", C.c_int32),
+                ("ms", C.c_double), ("ms_default", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {"tc_groups": list(self.tc_groups), "bp_blocks_per_sm": self.bp_blocks_per_sm,
+                "nbr_blocks_per_sm": self.nbr_blocks_per_sm, "ms": self.ms, "ms_default": self.ms_default}
 
 
 class Context:
@@ -402,6 +414,23 @@ class Context:
         ms = np.zeros(6)
         self._ck(self.lib.ann_phase_times(self.h, _d(ms), 6))
         return ms
+
+    # ---- launch shapes
+    def autotune(self, precision=None, reps: int = 5) -> dict:
+        """Time the run-time launch shapes on the staged batch (the last compute call's structures)
+        and keep the fastest for later calls (ann_autotune); returns the choice and its time."""
+        prec = self.precision if precision is None else precision
+        t = Tuning()
+        self._ck(self.lib.ann_autotune(self.h, prec, reps, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, tc_groups=(0, 0, 0, 0), bp_blocks_per_sm: int = 0, nbr_blocks_per_sm: int = 0):
+        """Apply stored launch shapes (ann_set_tuning); zeros restore the built-in rules."""
+        t = Tuning()
+        for k, g in enumerate(list(tc_groups)[:4]):
+            t.tc_groups[k] = int(g)
+        t.bp_blocks_per_sm, t.nbr_blocks_per_sm = int(bp_blocks_per_sm), int(nbr_blocks_per_sm)
+        self._ck(self.lib.ann_set_tuning(self.h, C.byref(t)))
 
     # ---- inspection
     def symm_width(self) -> int:

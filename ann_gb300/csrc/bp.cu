@@ -895,6 +895,7 @@ static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t s
         const size_t smem = wb * BP_WARPS;
         int per_sm = (int)std::max<size_t>(1, (size_t)(227 * 1024) / std::max<size_t>(smem, 1));
         per_sm = std::min(per_sm, 16);
+        if (a.grid_per_sm > 0) per_sm = std::min(per_sm, (int)a.grid_per_sm);
         int grid = (a.natoms + BP_WARPS - 1) / BP_WARPS;
         grid = std::min(grid, 152 * per_sm);
         ++::ann::g_launch_counter, kern<<<grid, BP_WARPS * 32, smem, st>>>(pot, a);

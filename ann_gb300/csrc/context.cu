@@ -45,6 +45,7 @@ static void reset_graph(ann_ctx* c) {
         c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, -1, 0};
     }
 }
+void drop_graphs(ann_ctx* c) { reset_graph(c); }
 void rebuild_plan(ann_ctx* c) {
     build_plan(c->pot, c->plan);
     build_tc_plan(c->plan.pot, c->plan.w, c->plan.b, c->plan.inpw, c->plan.inpb, c->max_smem, c->tc);
@@ -207,6 +208,7 @@ static NbrArgs nbr_args(ann_ctx* c, double rc) {
     NbrArgs a{};
     a.nstruc = c->S; a.natoms = c->N; a.ntypes = c->pot.ntypes(); a.cap = c->cap; a.rc = rc;
     a.off = c->off_d; a.cell = c->cell.as<double>(); a.pos = c->pos.as<double>(); a.type = c->type.as<int32_t>(); a.sid = c->sid.as<int32_t>();
+    a.grid_per_sm = c->tune_nbr;
     a.geo = c->geo.as<StrucGeo>(); a.pos4 = c->pos4.as<float4>(); a.abin = c->abin.as<int32_t>(); a.abc = c->abc.as<int32_t>(); a.am = c->am.as<int32_t>();
     a.aslot = c->aslot.as<int32_t>(); a.bcount = c->bcount.as<int32_t>(); a.bstart = c->bstart.as<int32_t>(); a.bidx = c->bidx.as<int32_t>();
     a.bm = c->bm.as<int32_t>(); a.bpos4 = c->bpos4.as<float4>(); a.bposd = c->bposd.as<double>(); a.nbins_cap = c->nbins_cap;

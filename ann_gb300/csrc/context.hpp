@@ -175,6 +175,9 @@ struct ann_ctx {
     bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
     int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
     int32_t* status_h = nullptr;    // page-locked copy of the status word
+    // launch shapes chosen by ann_autotune / ann_set_tuning (0: the built-in rule)
+    int32_t tune_tc[MAXT] = {0, 0, 0, 0};
+    int32_t tune_bp = 0, tune_nbr = 0;
     cudaEvent_t ev[16] = {};
 };
 
@@ -197,6 +200,8 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
 void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true);
 void finish_batch(ann_ctx* c);
 int32_t* status_host(ann_ctx* c);
+// drops the captured graphs (launch shapes changed)
+void drop_graphs(ann_ctx* c);
 
 template <typename real>
 inline BpArgs<real> bp_args(ann_ctx* c) {
@@ -206,6 +211,7 @@ inline BpArgs<real> bp_args(ann_ctx* c) {
     b.nr = c->nr.p; b.G = c->G.as<real>(); b.dEdG = c->dEdG.as<real>(); b.F = c->F.as<real>(); b.W = c->W.as<real>();
     b.lam = c->lam.as<real>(); b.U = c->U.as<real>();
     b.counter = c->counter.as<uint32_t>(); b.status = c->status.as<int32_t>();
+    b.grid_per_sm = c->tune_bp;
     return b;
 }
 
@@ -224,7 +230,7 @@ inline void enqueue_networks(ann_ctx* c, int natoms, DevBuf& G, DevBuf& dEdG, De
             ta.tstart = tstart.as<int32_t>(); ta.tlist = tlist.as<int32_t>();
             ta.G = G.as<float>(); ta.dEdG = dEdG.as<float>(); ta.Eatom = Eatom.as<double>();
             ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>();
-            launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->opt.tc_groups, c->tc.smem_bytes(ty), c->stream);
+            launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->stream);
         }
     } else {
         MlpArgs<real> m{};

@@ -50,6 +50,7 @@ struct NbrArgs {
     int32_t* scan_tmp;               // scratch for the bin scan
     uint32_t* counter;               // [1] work counter
     int32_t* status;                 // [8]
+    int32_t grid_per_sm;             // host side: blocks per SM of the search grid (0: 16)
 };
 void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st);
 // recompute nr from positions and stored images (Verlet-list refresh between rebuilds)
@@ -75,6 +76,7 @@ struct BpArgs {
     DevParams<real> prm;
     uint32_t* counter;
     int32_t* status;
+    int32_t grid_per_sm;             // host side: cap on resident blocks per SM (0: as many as fit)
 };
 template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_force(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);

@@ -293,6 +293,29 @@ int ann_md_get_state(ann_ctx* ctx, double* posn, double* vel, double* forces);
 int ann_network_noalloc(ann_ctx* ctx, int32_t natoms, const int32_t* type_dev, const void* G_dev,
                         double* Eatom_dev, void* dEdG_dev, int32_t precision);
 
+/* ---- launch-shape autotuner --------------------------------------------------------------------
+ * The run-time launch shapes of the E+F sequence are timed on the staged batch (the structures of
+ * the last ann_compute call), each through its own captured CUDA graph:
+ *   - per type, the warps per TMEM lane quadrant of the tensor-core network kernel: 1, 2 or 4,
+ *     giving 4, 2 or 1 CTAs per SM (MIXED on the tensor-core kernel only);
+ *   - the resident blocks per SM of the symmetry-function and force passes;
+ *   - the blocks per SM of the neighbour search.
+ * The search is coordinate-wise: each knob over its candidates with the others held, keeping a
+ * candidate only when it beats the best so far by more than 1 %. Each candidate takes the median
+ * of `reps` timed evaluations (CUDA events).
+ * The context keeps the choice for its later calls; 0 in a field is the built-in rule.
+ * ann_set_tuning applies a stored choice. The staged batch is recomputed, with the same results.
+ * Not in MD mode (ANN_ERR_STATE). */
+typedef struct ann_tuning {
+    int32_t tc_groups[4];          /* per type: 1, 2, 4, or 0 for the per-launch rule               */
+    int32_t bp_blocks_per_sm;      /* symmetry / force passes: 1..16, or 0 for as many as fit       */
+    int32_t nbr_blocks_per_sm;     /* neighbour search: 1..64, or 0 for 16                           */
+    double ms;                     /* ann_autotune: one evaluation with the chosen shapes (ms)       */
+    double ms_default;             /* ann_autotune: one evaluation with every field 0 (ms)           */
+} ann_tuning;
+int ann_autotune(ann_ctx* ctx, int32_t precision, int32_t reps, ann_tuning* out);
+int ann_set_tuning(ann_ctx* ctx, const ann_tuning* t);
+
 #ifdef __cplusplus
 }
 #endif
