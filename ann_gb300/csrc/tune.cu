@@ -75,36 +75,45 @@ int ann_autotune(ann_ctx* c, int32_t prec, int32_t reps, ann_tuning* out) {
         if (c->md_ready) throw ann_error(ANN_ERR_STATE, "the autotuner times a staged batch, not an MD run (ann_compute first)");
         if (!c->have_batch || c->N <= 0) throw ann_error(ANN_ERR_STATE, "no batch staged (ann_compute first)");
         reps = std::max(1, std::min((int)reps, 1000));
-        ann_tuning best{};
-        apply(c, best);
-        const double t_default = time_batch(c, prec, reps);
-        double t_best = t_default;
-        auto trial = [&](ann_tuning cand) {
-            apply(c, cand);
-            const double t = time_batch(c, prec, reps);
-            if (t < 0.99 * t_best) { t_best = t; best = cand; }
-        };
-        if (prec == ANN_MIXED && use_tc(c)) {
-            for (int ty = 0; ty < std::min(c->pot.ntypes(), 4); ++ty) {
-                const ann_tuning base = best;
-                for (int g : {1, 2, 4}) { ann_tuning cand = base; cand.tc_groups[ty] = g; trial(cand); }
+        ann_tuning prior{};
+        for (int k = 0; k < 4 && k < MAXT; ++k) prior.tc_groups[k] = c->tune_tc[k];
+        prior.bp_blocks_per_sm = c->tune_bp;
+        prior.nbr_blocks_per_sm = c->tune_nbr;
+        try {
+            ann_tuning best{};
+            apply(c, best);
+            const double t_default = time_batch(c, prec, reps);
+            double t_best = t_default;
+            auto trial = [&](ann_tuning cand) {
+                apply(c, cand);
+                const double t = time_batch(c, prec, reps);
+                if (t < 0.99 * t_best) { t_best = t; best = cand; }
+            };
+            if (prec == ANN_MIXED && use_tc(c)) {
+                for (int ty = 0; ty < std::min(c->pot.ntypes(), 4); ++ty) {
+                    const ann_tuning base = best;
+                    for (int g : {1, 2, 4}) { ann_tuning cand = base; cand.tc_groups[ty] = g; trial(cand); }
+                }
             }
+            {
+                const ann_tuning base = best;
+                for (int b : {2, 3, 4}) { ann_tuning cand = base; cand.bp_blocks_per_sm = b; trial(cand); }
+            }
+            {
+                const ann_tuning base = best;
+                for (int b : {4, 8, 32}) { ann_tuning cand = base; cand.nbr_blocks_per_sm = b; trial(cand); }
+            }
+            apply(c, best);
+            // leave the staged batch's results computed with the chosen shapes
+            run_batch(c, prec, true, true);
+            finish_batch(c);
+            best.ms = t_best;
+            best.ms_default = t_default;
+            if (out) *out = best;
+        } catch (...) {   // a failed search leaves the shapes the context had before it
+            apply(c, prior);
+            throw;
         }
-        {
-            const ann_tuning base = best;
-            for (int b : {2, 3, 4}) { ann_tuning cand = base; cand.bp_blocks_per_sm = b; trial(cand); }
-        }
-        {
-            const ann_tuning base = best;
-            for (int b : {4, 8, 32}) { ann_tuning cand = base; cand.nbr_blocks_per_sm = b; trial(cand); }
-        }
-        apply(c, best);
-        // leave the staged batch's results computed with the chosen shapes
-        run_batch(c, prec, true, true);
-        finish_batch(c);
-        best.ms = t_best;
-        best.ms_default = t_default;
-        if (out) *out = best;
     })
 }
 

@@ -303,7 +303,9 @@ int ann_network_noalloc(ann_ctx* ctx, int32_t natoms, const int32_t* type_dev, c
  * The search is coordinate-wise: each knob over its candidates with the others held, keeping a
  * candidate only when it beats the best so far by more than 1 %. Each candidate takes the median
  * of `reps` timed evaluations (CUDA events).
- * The context keeps the choice for its later calls; 0 in a field is the built-in rule.
+ * The context keeps the choice for its later calls. A 0 field is the built-in rule; for
+ * tc_groups that is ann_options.tc_groups, itself 0 for the per-launch rule. A failed search
+ * leaves the shapes the context had before it.
  * ann_set_tuning applies a stored choice. The staged batch is recomputed, with the same results.
  * Not in MD mode (ANN_ERR_STATE). */
 typedef struct ann_tuning {
