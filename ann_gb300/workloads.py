@@ -273,7 +273,10 @@ def linear_network(coef, nin: int, nodes, seed: int, scale: float = 0.003, out_b
     W1 = scale * np.outer(np.pad(coef, (0, nin - len(coef))), u)           # [in, out]
     W2 = rng.normal(0.0, 1.0 / np.sqrt(h1), (h1, h2))
     w3 = rng.normal(0.0, 1.0 / np.sqrt(h2), h2)
-    w3 /= scale * float(u @ W2 @ w3)
+    gain = scale * float(u @ W2 @ w3)
+    if abs(gain) < 1e-6 * scale:
+        raise ValueError("degenerate draw for the linear network: choose another seed")
+    w3 /= gain
     biases = np.concatenate([np.zeros(h1), np.zeros(h2), [out_bias]])
     return np.concatenate([biases, W1.reshape(-1), W2.reshape(-1), w3])
 
@@ -285,7 +288,8 @@ def lj_argon_text(cfg: int = 5, a: float = 5.26, seed: int | None = None) -> str
     angular inputs weighted zero, and c.G(a) as the output bias. Unlike randomly initialised
     weights, which attract atoms without bound, this keeps an FCC crystal stable under MD."""
     spec = CONFIG_POT[cfg]
-    assert len(spec["names"]) == 1 and spec["neuron"] == "TANH" and len(spec["nodes"]) == 3
+    if len(spec["names"]) != 1 or spec["neuron"] != "TANH" or len(spec["nodes"]) != 3:
+        raise ValueError("lj_argon_text needs a one-type configuration with two tanh hidden layers")
     rc, nr = spec["rc"], spec["n_radial"]
     eta = radial_eta(nr)
     c = lj_pair_coefficients(rc, eta)
