@@ -18,7 +18,9 @@ Configurations:
   3  64 structures as 2 with N~U{32..256}; Lennard-Jones labels (eps 0.0104 eV, sigma 3.4 A, cut 8.5 A)
   4  ternary 1:1:2, 40x40x20 simple-cubic sites (32,000 atoms), a=2.4264 A, jitter 0.15 A; rc=6;
      16 radial per species + 8 angular per pair = 96; 96-128-128-1 tanh
-  5  Ar FCC 64x32x32 cells = 262,144 atoms, a=5.26, Maxwell 80 K; configuration-1 basis, 16-32-32-1 tanh
+  5  Ar FCC 64x32x32 cells = 262,144 atoms, a=5.26, Maxwell 80 K; configuration-1 basis, 16-32-32-1 tanh;
+     for MD the networks carry a Lennard-Jones argon pair potential (lj_argon_text), since
+     randomly initialised weights attract atoms without bound
 """
 from __future__ import annotations
 
