@@ -252,3 +252,52 @@ def test_training_gradient_fd_activations(oracle, neuron):
         pot.set_params(p0)
         fd = (lp - lm) / (2 * hh)
         assert abs(fd - g[k]) <= 1e-6 * max(abs(fd), abs(g[k])) + 1e-7 * gscale, (neuron, k, fd, g[k])
+
+
+def test_angular_sums_equal_moment_contractions(pot2):
+    """The oracle's triplet sums of the GAUSS angular functions (|1/2 + lambda/2 cos|^zeta with
+    integer zeta, basis_angular.cpp:376-381, each unordered neighbour pair once) against an
+    independent form: with a_j = fc(r_j) exp(-r_j^2/eta^2) and moments M_a = sum_j a_j u_j^a over
+    multi-indices a, sum_pairs a_j a_k cos^m = sum_{|a|=m} (m!/a!) M^J_a M^K_a (same species: half
+    of it minus sum_j a_j^2); the binomial expansion in cos then gives every function."""
+    import itertools
+    import math
+    structs = W.config2(nstruc=1)
+    offs, posn, types, cell = pack_batch(structs)
+    G = pot2.compute(offs, posn, types, cell, symm=True)[3]
+    x, t, R = structs[0]
+    rc = 6.5
+    fc = lambda r: 0.5 * (np.cos(np.pi * r / rc) + 1.0)
+    etas = [float(f"{1 / np.sqrt(eb):f}") for eb in (0.003, 0.01)]
+    rows = [(e, z, lam) for e in etas for z in (1, 2, 4, 8) for lam in (1, -1)]
+    alphas = sorted({a for m in range(9) for a in itertools.product(range(m + 1), repeat=3) if sum(a) == m},
+                    key=lambda a: (sum(a), a))
+    mdeg = np.array([sum(a) for a in alphas])
+    mcoef = np.array([math.factorial(sum(a)) / math.prod(math.factorial(k) for k in a) for a in alphas])
+    shifts = np.array(list(itertools.product(range(-2, 3), repeat=3)), float) @ R
+    for i in (0, 7, len(x) - 1):
+        M = np.zeros((2, 2, len(alphas)))
+        S = np.zeros((2, 2))
+        for sh in shifts:
+            d = x[i] - x - sh
+            dd = np.linalg.norm(d, axis=1)
+            for j in np.nonzero((dd < rc) & (dd > 1e-9))[0]:
+                u = d[j] / dd[j]
+                mono = np.array([u[0] ** a[0] * u[1] ** a[1] * u[2] ** a[2] for a in alphas])
+                for g, e in enumerate(etas):
+                    a = fc(dd[j]) * np.exp(-dd[j] ** 2 / e ** 2)
+                    M[t[j], g] += a * mono
+                    S[t[j], g] += a * a
+        want = []
+        for J in range(2):
+            for K in range(J, 2):
+                for e, z, lam in rows:
+                    g = etas.index(e)
+                    v = 0.0
+                    for m in range(z + 1):
+                        sel = mdeg == m
+                        D = np.sum(mcoef[sel] * M[J, g, sel] * M[K, g, sel])
+                        v += math.comb(z, m) * 0.5 ** (z - m) * (0.5 * lam) ** m * (0.5 * (D - S[J, g]) if J == K else D)
+                    want.append(v)
+        got = G[i, 24:24 + len(want)]
+        np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-12)
