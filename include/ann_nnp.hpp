@@ -44,6 +44,13 @@ public:
     ann_ctx* ctx() const { return ctx_; }
     int index(const char* name) const { int32_t i = -1; check(ctx_, ann_type_index(ctx_, name, &i)); return i; }
     double rc() const { double r = 0; check(ctx_, ann_cutoff(ctx_, &r)); return r; }
+    // launch shapes timed on the structures of the last compute call (ann_autotune), kept for the
+    // context's later calls; no counterpart in the reference's NNP
+    ann_tuning autotune(int precision = -1, int reps = 5) {
+        ann_tuning t{};
+        check(ctx_, ann_autotune(ctx_, precision < 0 ? prec_ : precision, reps, &t));
+        return t;
+    }
 
     static void read(const char* file, NNP& nnp) { check(nnp.ctx_, ann_load_potential(nnp.ctx_, file)); }
     static void write(const char* file, const NNP& nnp) { check(nnp.ctx_, ann_write_potential(nnp.ctx_, file)); }
