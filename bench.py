@@ -279,6 +279,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nstruc", type=int, default=256)
     ap.add_argument("--no-extras", action="store_true", help="skip the training and MD legs")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the built-in launch shapes (no autotuner launches before the timed steps, e.g. for "
+                         "ncu captures that select launches by position)")
     ap.add_argument("--only", choices=["training", "md", "lammps"],
                     help="run one secondary leg alone with --steps / --warmup and print its JSON (for profiling)")
     args = ap.parse_args()
@@ -344,8 +347,11 @@ def main():
     # ---- launch shapes picked by the library's autotuner on this batch (outside the timed region,
     #      like the graph capture); the FP64 form gets its own when it is timed
     SHAPE_KEYS = ("tc_groups", "bp_blocks_per_sm", "nbr_blocks_per_sm")
-    ctx.compute(offs, posn, types, cell, precision=MIXED)
-    tuned = ctx.autotune(precision=MIXED, reps=5)
+    if args.no_tune:
+        tuned = {"tc_groups": [0, 0, 0, 0], "bp_blocks_per_sm": 0, "nbr_blocks_per_sm": 0, "ms": None, "ms_default": None}
+    else:
+        ctx.compute(offs, posn, types, cell, precision=MIXED)
+        tuned = ctx.autotune(precision=MIXED, reps=5)
     shapes = {k: tuned[k] for k in SHAPE_KEYS}
 
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -389,7 +395,7 @@ def main():
 
     # ---- plain FP64 form on the same batch, with its own tuned shapes
     ctx.set_tuning()
-    tuned64 = ctx.autotune(precision=FP64, reps=1)
+    tuned64 = dict(tuned) if args.no_tune else ctx.autotune(precision=FP64, reps=1)
     ms64 = timed_device(FP64, max(3, args.steps // 4), 2)
     fp64_value = N / (float(np.mean(ms64)) * 1e-3)
     ctx.set_tuning(**shapes)
