@@ -56,3 +56,40 @@ def test_split_never_exceeds_tensor_memory(rule):
             g = rule(cols, atoms)
             assert g in (1, 2, 4)
             assert (4 // g) * cols <= 512 or g == 4    # CTAs per SM x columns within 512
+
+
+LAYOUT = r'''
+#include <cstddef>
+#include <cstdio>
+#include "ann_gpu.h"
+#define F(T, m) std::printf(#T " " #m " %zu\n", offsetof(T, m))
+int main() {
+    std::printf("ann_options size %zu\n", sizeof(ann_options));
+    F(ann_options, device); F(ann_options, precision); F(ann_options, newton); F(ann_options, max_neighbors);
+    F(ann_options, use_graphs); F(ann_options, mlp_backend); F(ann_options, tc_groups);
+    std::printf("ann_tuning size %zu\n", sizeof(ann_tuning));
+    F(ann_tuning, tc_groups); F(ann_tuning, bp_blocks_per_sm); F(ann_tuning, nbr_blocks_per_sm);
+    F(ann_tuning, ms); F(ann_tuning, ms_default);
+    return 0;
+}
+'''
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """ann_options and ann_tuning as the ctypes binding declares them have the C header's layout."""
+    import ctypes as C
+    from ann_gb300.api import Options, Tuning
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no host compiler")
+    src, exe = tmp_path / "layout.cpp", tmp_path / "layout"
+    src.write_text(LAYOUT)
+    subprocess.run([cxx, "-std=c++17", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        a, b, v = ln.split()
+        got[(a, b)] = int(v)
+    for cls, name in ((Options, "ann_options"), (Tuning, "ann_tuning")):
+        assert got[(name, "size")] == C.sizeof(cls), name
+        for field, _ in cls._fields_:
+            assert got[(name, field)] == getattr(cls, field).offset, (name, field)
