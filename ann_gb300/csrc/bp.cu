@@ -897,7 +897,7 @@ static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t s
         per_sm = std::min(per_sm, 16);
         if (a.grid_per_sm > 0) per_sm = std::min(per_sm, (int)a.grid_per_sm);
         int grid = (a.natoms + BP_WARPS - 1) / BP_WARPS;
-        grid = std::min(grid, 152 * per_sm);
+        grid = std::min(grid, std::max(1, (int)a.nsm) * per_sm);
         ++::ann::g_launch_counter, kern<<<grid, BP_WARPS * 32, smem, st>>>(pot, a);
     };
     if (pot.fast) {

@@ -209,6 +209,7 @@ static NbrArgs nbr_args(ann_ctx* c, double rc) {
     a.nstruc = c->S; a.natoms = c->N; a.ntypes = c->pot.ntypes(); a.cap = c->cap; a.rc = rc;
     a.off = c->off_d; a.cell = c->cell.as<double>(); a.pos = c->pos.as<double>(); a.type = c->type.as<int32_t>(); a.sid = c->sid.as<int32_t>();
     a.grid_per_sm = c->tune_nbr;
+    a.nsm = c->nsm;
     a.geo = c->geo.as<StrucGeo>(); a.pos4 = c->pos4.as<float4>(); a.abin = c->abin.as<int32_t>(); a.abc = c->abc.as<int32_t>(); a.am = c->am.as<int32_t>();
     a.aslot = c->aslot.as<int32_t>(); a.bcount = c->bcount.as<int32_t>(); a.bstart = c->bstart.as<int32_t>(); a.bidx = c->bidx.as<int32_t>();
     a.bm = c->bm.as<int32_t>(); a.bpos4 = c->bpos4.as<float4>(); a.bposd = c->bposd.as<double>(); a.nbins_cap = c->nbins_cap;
@@ -406,6 +407,8 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         configure_kernels();
         cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->opt.device);
         cudaDeviceGetAttribute(&c->tc.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->opt.device);
+        ck(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->opt.device), "SM count");
+        if (c->nsm < 1) c->nsm = 1;
         if (c->opt.mlp_backend < 0 || c->opt.mlp_backend > 2) throw ann_error(ANN_ERR_ARG, "mlp_backend must be 0, 1 or 2");
         if (c->opt.tc_groups != 0 && c->opt.tc_groups != 1 && c->opt.tc_groups != 2 && c->opt.tc_groups != 4)
             throw ann_error(ANN_ERR_ARG, "tc_groups must be 0, 1, 2 or 4");

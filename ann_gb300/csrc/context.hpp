@@ -174,6 +174,7 @@ struct ann_ctx {
     bool profile = false;
     bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
     int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
+    int nsm = 1;                    // streaming multiprocessors of the device (persistent grids)
     int32_t* status_h = nullptr;    // page-locked copy of the status word
     // launch shapes chosen by ann_autotune / ann_set_tuning (0: the built-in rule)
     int32_t tune_tc[MAXT] = {0, 0, 0, 0};
@@ -212,6 +213,7 @@ inline BpArgs<real> bp_args(ann_ctx* c) {
     b.lam = c->lam.as<real>(); b.U = c->U.as<real>();
     b.counter = c->counter.as<uint32_t>(); b.status = c->status.as<int32_t>();
     b.grid_per_sm = c->tune_bp;
+    b.nsm = c->nsm;
     return b;
 }
 
@@ -230,7 +232,7 @@ inline void enqueue_networks(ann_ctx* c, int natoms, DevBuf& G, DevBuf& dEdG, De
             ta.tstart = tstart.as<int32_t>(); ta.tlist = tlist.as<int32_t>();
             ta.G = G.as<float>(); ta.dEdG = dEdG.as<float>(); ta.Eatom = Eatom.as<double>();
             ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>();
-            launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->stream);
+            launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->nsm, c->stream);
         }
     } else {
         MlpArgs<real> m{};

@@ -92,7 +92,7 @@ void launch_list_rows(const ListArgs& a, bool fp64, cudaStream_t st) {
     if (a.nrows <= 0) return;
     const int threads = LR_WARPS * 32;
     int grid = (a.nrows + LR_WARPS - 1) / LR_WARPS;
-    grid = std::min(grid, 152 * 8);
+    grid = std::min(grid, std::max(1, (int)a.nsm) * 8);
     if (fp64) ++::ann::g_launch_counter, k_list_rows<true><<<grid, threads, 0, st>>>(a);
     else ++::ann::g_launch_counter, k_list_rows<false><<<grid, threads, 0, st>>>(a);
 }
@@ -102,12 +102,12 @@ __global__ void k_to_double(size_t n, const real* in, double* out) {
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) out[k] = (double)in[k];
 }
 template <typename real>
-void launch_to_double(size_t n, const real* in, double* out, cudaStream_t st) {
+void launch_to_double(size_t n, const real* in, double* out, int nsm, cudaStream_t st) {
     if (n == 0) return;
-    const int grid = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)std::max(1, nsm) * 16);
     ++::ann::g_launch_counter, k_to_double<real><<<grid, 256, 0, st>>>(n, in, out);
 }
-template void launch_to_double<float>(size_t, const float*, double*, cudaStream_t);
-template void launch_to_double<double>(size_t, const double*, double*, cudaStream_t);
+template void launch_to_double<float>(size_t, const float*, double*, int, cudaStream_t);
+template void launch_to_double<double>(size_t, const double*, double*, int, cudaStream_t);
 
 }  // namespace ann

@@ -51,6 +51,7 @@ struct NbrArgs {
     uint32_t* counter;               // [1] work counter
     int32_t* status;                 // [8]
     int32_t grid_per_sm;             // host side: blocks per SM of the search grid (0: 16)
+    int32_t nsm;                     // host side: streaming multiprocessors of the device
 };
 void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st);
 // recompute nr from positions and stored images (Verlet-list refresh between rebuilds)
@@ -77,6 +78,7 @@ struct BpArgs {
     uint32_t* counter;
     int32_t* status;
     int32_t grid_per_sm;             // host side: cap on resident blocks per SM (0: as many as fit)
+    int32_t nsm;                     // host side: streaming multiprocessors of the device
 };
 template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_force(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
@@ -98,9 +100,10 @@ struct ListArgs {
     int32_t* nj;                     // [nrows*cap]
     void* nr;                        // [nrows*cap] real4 (rx, ry, rz, d), r = x_centre - x_neighbour
     int32_t* status;                 // [8]: [1] longest row on overflow, [2] longest row above hint
+    int32_t nsm;                     // host side: streaming multiprocessors of the device
 };
 void launch_list_rows(const ListArgs& a, bool fp64, cudaStream_t st);
-template <typename real> void launch_to_double(size_t n, const real* in, double* out, cudaStream_t st);
+template <typename real> void launch_to_double(size_t n, const real* in, double* out, int nsm, cudaStream_t st);
 
 // ---- optimiser steps (optim.cu) ---------------------------------------------------------------
 // algorithms with the values of opt::algo::Name (src/opt/algo.hpp:31-49)

@@ -20,6 +20,7 @@ static void enqueue_list(ann_ctx* c, int nrows, int nall, int cap, int nchunks, 
     b.G = c->lG.as<real>(); b.dEdG = c->ldEdG.as<real>(); b.F = c->lF.as<real>(); b.W = c->lW.as<real>();
     b.self = have_ilist ? c->lilist.as<int32_t>() : nullptr;
     b.counter = c->counter.as<uint32_t>(); b.status = c->status.as<int32_t>();
+    b.nsm = c->nsm;
     b.prm = params_of<real>(c->pf, c->pd);
     launch_symm<real>(pot, b, st);
     enqueue_networks<real>(c, nrows, c->lG, c->ldEdG, c->lEatom, c->ltstart, c->ltlist, b.prm);
@@ -31,7 +32,7 @@ static void enqueue_list(ann_ctx* c, int nrows, int nall, int cap, int nchunks, 
     t.nchunks = nchunks; t.schunk = c->ltables.as<int32_t>(); t.chunk = t.schunk + 2; t.partial = c->lpartial.as<double>();
     launch_reduce_structures<real>(1, t, c->lEatom.as<double>(), forces ? c->lW.as<real>() : nullptr, c->lF.as<real>(),
                                    c->lEs.as<double>(), c->lWs.as<double>(), nullptr, st);
-    if (forces) launch_to_double<real>(3 * (size_t)nall, c->lF.as<real>(), c->lFout.as<double>(), st);
+    if (forces) launch_to_double<real>(3 * (size_t)nall, c->lF.as<real>(), c->lFout.as<double>(), c->nsm, st);
 }
 
 extern "C" {
@@ -120,6 +121,7 @@ int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32
             la.ilist = have_ilist ? c->lilist.as<int32_t>() : nullptr; la.noff = c->lnoff.as<int64_t>(); la.neigh = c->lneigh.as<int32_t>();
             la.x = c->lx.as<double>(); la.type = c->ltype.as<int32_t>(); la.rtype = c->lrtype.as<int32_t>(); la.nn = c->lnn.as<int32_t>();
             la.ntc = c->lntc.as<int32_t>(); la.nj = c->lnj.as<int32_t>(); la.nr = c->lnr.p; la.status = c->status.as<int32_t>();
+            la.nsm = c->nsm;
             launch_list_rows(la, fp64, st);
             if (fp64) enqueue_list<double>(c, inum, nall, cap, nch, want_f, have_ilist);
             else enqueue_list<float>(c, inum, nall, cap, nch, want_f, have_ilist);

@@ -321,13 +321,14 @@ __global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constan
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)tt.tmem_cols) : "memory");
 }
 
-void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, cudaStream_t st) {
+void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, int nsm, cudaStream_t st) {
     if (a.natoms <= 0) return;
     // a forced split cannot oversubscribe tensor memory: smem_bytes admits at most 512 / tmem_cols
     // CTAs per SM whatever their width
-    const int g = groups ? groups : tc_groups(tt, est_atoms, 152);
+    nsm = std::max(1, nsm);
+    const int g = groups ? groups : tc_groups(tt, est_atoms, nsm);
     int grid = (a.natoms + TC_M - 1) / TC_M;
-    grid = std::min(grid, 152 * (4 / g));
+    grid = std::min(grid, nsm * (4 / g));
     ++::ann::g_launch_counter;
     if (g == 1) k_mlp_tc<1><<<grid, TC_M, smem, st>>>(tt, a);
     else if (g == 2) k_mlp_tc<2><<<grid, TC_M * 2, smem, st>>>(tt, a);

@@ -92,7 +92,8 @@ struct TcArgs {
 };
 // est_atoms: the expected atoms of the type (its count is known on the device only); groups:
 // 1, 2 or 4 to force the split, 0 to choose it (tc_groups)
-void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, cudaStream_t st);
+// nsm: streaming multiprocessors of the device (the persistent grid's size)
+void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, int nsm, cudaStream_t st);
 void configure_mlp_tc(int maxsmem);
 
 }  // namespace ann

@@ -400,7 +400,7 @@ void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st) {
     const int warps = NBR_WARPS;
     const size_t smem = (size_t)warps * (3 * a.cap + 3 * MAX_RANGES) * sizeof(int32_t);
     int grid = (a.natoms + warps - 1) / warps;
-    grid = std::min(grid, 152 * (a.grid_per_sm > 0 ? (int)a.grid_per_sm : 16));
+    grid = std::min(grid, std::max(1, (int)a.nsm) * (a.grid_per_sm > 0 ? (int)a.grid_per_sm : 16));
     if (grid < 1) grid = 1;
     if (fp64) ++::ann::g_launch_counter, k_neighbors<true><<<grid, warps * 32, smem, st>>>(a);
     else ++::ann::g_launch_counter, k_neighbors<false><<<grid, warps * 32, smem, st>>>(a);

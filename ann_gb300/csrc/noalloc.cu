@@ -21,17 +21,13 @@ static_assert(NA_BYTES <= ANN_NOALLOC_SCRATCH_BYTES, "no-allocation scratch layo
 }  // namespace
 static __device__ __align__(256) unsigned char g_noalloc_scratch[ANN_NOALLOC_SCRATCH_BYTES];
 
-// address of the scratch array on the current device, resolved once per device (the first call
-// on a device does it, so that call should come before any stream capture on the device)
-static unsigned char* noalloc_scratch(int device) {
-    static std::mutex mu;
-    static std::map<int, unsigned char*> addr;
-    std::lock_guard<std::mutex> g(mu);
-    auto it = addr.find(device);
-    if (it != addr.end()) return it->second;
+// device address of the scratch array in the current device's context. The host-side name
+// g_noalloc_scratch is only a stand-in, never a device address. The address is looked up on every
+// call (a host query that allocates nothing), so a context that the application destroyed and
+// re-created (cudaDeviceReset) never leaves a stale address behind
+static unsigned char* noalloc_scratch() {
     unsigned char* p = nullptr;
     ck(cudaGetSymbolAddress((void**)&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-allocation scratch)");
-    addr[device] = p;
     return p;
 }
 
@@ -53,7 +49,7 @@ int ann_network_noalloc(ann_ctx* c, int32_t natoms, const int32_t* type_dev, con
         const DevPot& pot = c->plan.pot;
         if (!tc && mlp_smem_bytes(pot, fp64, false) + 1024 > (size_t)c->max_smem)
             throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
-        unsigned char* s = noalloc_scratch(c->opt.device);
+        unsigned char* s = noalloc_scratch();
         int32_t* status = reinterpret_cast<int32_t*>(s + NA_STATUS);
         int32_t* tstart = reinterpret_cast<int32_t*>(s + NA_TSTART);
         int32_t* tcount = reinterpret_cast<int32_t*>(s + NA_TCOUNT);
@@ -70,7 +66,7 @@ int ann_network_noalloc(ann_ctx* c, int32_t natoms, const int32_t* type_dev, con
                 ta.tstart = tstart; ta.tlist = tlist;
                 ta.G = static_cast<const float*>(G_dev); ta.dEdG = static_cast<float*>(dEdG_dev); ta.Eatom = Eatom_dev;
                 ta.image = c->tcimg.as<uint8_t>(); ta.status = status;
-                launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), st);
+                launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->nsm, st);
             }
         } else if (fp64) {
             MlpArgs<double> m{};

@@ -31,7 +31,9 @@ static void apply(ann_ctx* c, const ann_tuning& t) {
     drop_graphs(c);
 }
 
-// one evaluation of the staged batch with the context's current shapes (ms, median of reps)
+// one evaluation of the staged batch with the context's current shapes (ms, median of reps). Every
+// replay clears the status word, so each one's status is read after it: a negative result means
+// that a replay's bounded device waits gave up (its early return would look fast)
 static double time_batch(ann_ctx* c, int prec, int reps) {
     run_batch(c, prec, true, true);
     finish_batch(c);
@@ -39,6 +41,7 @@ static double time_batch(ann_ctx* c, int prec, int reps) {
     ck(cudaEventCreate(&e0), "event create");
     ck(cudaEventCreate(&e1), "event create");
     std::vector<float> t(reps);
+    bool gave_up = false;
     try {
         for (int r = 0; r < reps; ++r) {
             ck(cudaEventRecord(e0, c->stream), "event record");
@@ -46,6 +49,10 @@ static double time_batch(ann_ctx* c, int prec, int reps) {
             ck(cudaEventRecord(e1, c->stream), "event record");
             ck(cudaEventSynchronize(e1), "event synchronize");
             ck(cudaEventElapsedTime(&t[r], e0, e1), "event time");
+            int32_t s0 = 0;
+            ck(cudaMemcpyAsync(&s0, c->status.p, sizeof(s0), cudaMemcpyDeviceToHost, c->stream), "D2H status");
+            ck(cudaStreamSynchronize(c->stream), "synchronize");
+            if (s0 & ST_TIMEOUT) gave_up = true;
         }
         finish_batch(c);
     } catch (...) {
@@ -53,6 +60,7 @@ static double time_batch(ann_ctx* c, int prec, int reps) {
         throw;
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (gave_up) return -1.0;
     std::nth_element(t.begin(), t.begin() + reps / 2, t.end());
     return t[reps / 2];
 }
@@ -83,11 +91,15 @@ int ann_autotune(ann_ctx* c, int32_t prec, int32_t reps, ann_tuning* out) {
             ann_tuning best{};
             apply(c, best);
             const double t_default = time_batch(c, prec, reps);
+            if (t_default < 0) throw ann_error(ANN_ERR_TIMEOUT, "a bounded device wait gave up with the built-in launch shapes");
             double t_best = t_default;
+            // a candidate whose bounded waits gave up is dropped, not kept as fast, and the search goes on
             auto trial = [&](ann_tuning cand) {
                 apply(c, cand);
-                const double t = time_batch(c, prec, reps);
-                if (t < 0.99 * t_best) { t_best = t; best = cand; }
+                double t = -1.0;
+                try { t = time_batch(c, prec, reps); }
+                catch (ann_error& e) { if (e.code != ANN_ERR_TIMEOUT) throw; }
+                if (t > 0 && t < 0.99 * t_best) { t_best = t; best = cand; }
             };
             if (prec == ANN_MIXED && use_tc(c)) {
                 for (int ty = 0; ty < std::min(c->pot.ntypes(), 4); ++ty) {

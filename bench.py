@@ -133,7 +133,7 @@ def cpu_reference(offs, posn, types, cell, pot_text, budget_s=12.0, steps=1, war
     sample of the workload's structures; returns atom-evals/s and the sample description."""
     sys.path.insert(0, str(ROOT / "tests"))
     from oracle_lib import Oracle
-    orc = Oracle()
+    orc = Oracle(timed=True)
     pot = orc.load_text(pot_text)
     threads = threads or os.cpu_count() or 1
     S = len(offs) - 1
@@ -420,8 +420,9 @@ def main():
     pk = peaks()
     t_force = ph[4] * 1e-3
     sm_mhz = clk.get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12           # TFLOP/s (FMA = 2 flop) at the sampled clock
-    mufu_peak = 152 * 16 * sm_mhz * 1e6 / 1e12                 # T ops/s
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count   # cudaDevAttrMultiProcessorCount
+    fp32_peak = nsm * 128 * 2 * sm_mhz * 1e6 / 1e12           # TFLOP/s (FMA = 2 flop) at the sampled clock
+    mufu_peak = nsm * 16 * sm_mhz * 1e6 / 1e12                 # T ops/s
     # DRAM bytes of one force-pass launch: the per-atom figure of the committed ncu capture (small
     # case of the same workload) times the atoms of this launch
     traffic, traffic_src = None, None
@@ -440,7 +441,7 @@ def main():
                         "frac_fp32": work["force_flops"] / t_force / 1e12 / fp32_peak,
                         "mufu_tops": work["force_mufu"] / t_force / 1e12, "mufu_peak_tops": mufu_peak,
                         "frac_mufu": work["force_mufu"] / t_force / 1e12 / mufu_peak,
-                        "note": "peaks = 152 SMs x (128 FP32 lanes x 2 | 16 MUFU) x sampled SM clock; algorithmic counts "
+                        "note": f"peaks = {nsm} SMs (queried) x (128 FP32 lanes x 2 | 16 MUFU) x sampled SM clock; algorithmic counts "
                                 "(angular pow = 2 MUFU) though the kernel replaces pow by squaring chains"}
 
     # ---- end to end through the C ABI: the batch in page-locked host memory (as a data loader
@@ -463,7 +464,7 @@ def main():
             "ms_per_step": tmax, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "natoms": N, "nstruc": len(structs), "precision": "mixed (FP32 basis/forces/networks, FP64 energy sums)",
-                       "l2": "flushed between steps (256 MiB write outside the timed events)", "graphs": True,
+                       "l2": "flushed between steps (256 MiB write outside the timed events)", "graphs": True, "sm_count": nsm,
                        "launch_shapes": {"mixed": dict(shapes, ms=tuned["ms"], ms_default=tuned["ms_default"]),
                                          "fp64": {k: tuned64[k] for k in SHAPE_KEYS}},
                        "parallelism": f"replicas x{world} (structures sharded, no collective)"},

@@ -286,8 +286,11 @@ int ann_md_get_state(ann_ctx* ctx, double* posn, double* vel, double* forces);
  * device and can fail mid-run). Its scratch is one static device array of the library,
  * ANN_NOALLOC_SCRATCH_BYTES, shared by every call on a device: calls that overlap in time
  * (other threads, contexts or streams) race on it and must be serialised by the caller.
- * natoms > ANN_NOALLOC_MAX_ATOMS returns ANN_ERR_CAPACITY. The first call on each device resolves
- * the array's address (cudaGetSymbolAddress); make that first call before any stream capture.  */
+ * natoms > ANN_NOALLOC_MAX_ATOMS returns ANN_ERR_CAPACITY; natoms = 0 does nothing. Every call
+ * looks the array's device address up (cudaGetSymbolAddress, a host query that allocates nothing).
+ * The call is synchronous: it ends with a copy of the status word to host memory and a stream
+ * synchronisation, so it must not be called while ann_stream(ctx), or the legacy default stream,
+ * is being captured into a CUDA graph.                                                          */
 #define ANN_NOALLOC_MAX_ATOMS 262144
 #define ANN_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024 + 4096)
 int ann_network_noalloc(ann_ctx* ctx, int32_t natoms, const int32_t* type_dev, const void* G_dev,

@@ -17,7 +17,22 @@ ROOT = Path(__file__).resolve().parents[1]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_SO = ORACLE_DIR / "_build" / "libann_oracle.so"
 REF_SO = ORACLE_DIR / "_ref" / "libref_basis.so"
-REF_SRC = Path(os.environ.get("ANN_REFERENCE_SRC", "/root/reference/src"))
+ORACLE_TIMED_SO = ORACLE_DIR / "_build" / "libann_oracle_timed.so"
+
+
+def _reference_src() -> Path:
+    """The reference's src/ directory: ANN_REFERENCE_SRC, else the oracle recipe's default."""
+    env = os.environ.get("ANN_REFERENCE_SRC")
+    if env:
+        return Path(env)
+    try:
+        out = subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "print-ref"], capture_output=True, text=True, check=True)
+        return Path(out.stdout.strip())
+    except (OSError, subprocess.CalledProcessError):
+        return Path(os.devnull) / "missing"
+
+
+REF_SRC = _reference_src()
 
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -38,14 +53,18 @@ def _l(a):
 
 def build_oracle(ref: bool = False) -> None:
     target = ["oracle"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), *target, f"REF={REF_SRC}"], check=True)
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), *target], check=True)
 
 
 class Oracle:
-    def __init__(self):
-        if not ORACLE_SO.exists() or ORACLE_SO.stat().st_mtime < (ORACLE_DIR / "ann_oracle.cpp").stat().st_mtime:
+    """timed=True loads the build with the reference's optimisation flags and FP contraction
+    (for timing the CPU baseline only; its results may differ in the last bits)."""
+
+    def __init__(self, timed: bool = False):
+        so = ORACLE_TIMED_SO if timed else ORACLE_SO
+        if not so.exists() or so.stat().st_mtime < (ORACLE_DIR / "ann_oracle.cpp").stat().st_mtime:
             build_oracle()
-        L = self.L = C.CDLL(str(ORACLE_SO))
+        L = self.L = C.CDLL(str(so))
         L.orc_last_error.restype = C.c_char_p
         L.orc_load_text.restype = C.c_void_p
         L.orc_load_text.argtypes = [C.c_char_p]
