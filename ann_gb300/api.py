@@ -31,7 +31,7 @@ class AnnError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("newton", C.c_int32), ("max_neighbors", C.c_int32),
-                ("use_graphs", C.c_int32), ("mlp_backend", C.c_int32), ("tc_groups", C.c_int32)]
+                ("use_graphs", C.c_int32), ("mlp_backend", C.c_int32), ("tc_groups", C.c_int32), ("tc_split", C.c_int32)]
 
 
 def library_path() -> Path:
@@ -63,6 +63,7 @@ _SIGS = {
     "ann_cutoff": (C.c_int, [_V, _D]),
     "ann_num_inputs": (C.c_int, [_V, C.c_int32, _I32]),
     "ann_num_params": (C.c_int, [_V, _I64]),
+    "ann_network_form": (C.c_int, [_V, C.c_int32, _I32, _I32]),
     "ann_get_params": (C.c_int, [_V, _D, C.c_int64]),
     "ann_set_params": (C.c_int, [_V, _D, C.c_int64]),
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
@@ -185,12 +186,12 @@ class Context:
     """One device context: a loaded potential plus device buffers (one per host thread)."""
 
     def __init__(self, device: int = 0, precision: int = MIXED, newton: int = NEWTON_ALL_IMAGES, max_neighbors: int = 0,
-                 use_graphs: bool = True, mlp_backend: int = 0, tc_groups: int = 0):
+                 use_graphs: bool = True, mlp_backend: int = 0, tc_groups: int = 0, tc_split: int = 0):
         self.lib = load_library()
         o = Options()
         self.lib.ann_default_options(C.byref(o))
         o.device, o.precision, o.newton, o.max_neighbors = device, precision, newton, max_neighbors
-        o.use_graphs, o.mlp_backend, o.tc_groups = int(use_graphs), mlp_backend, tc_groups
+        o.use_graphs, o.mlp_backend, o.tc_groups, o.tc_split = int(use_graphs), mlp_backend, tc_groups, tc_split
         h = _V()
         rc = self.lib.ann_create(C.byref(h), C.byref(o))
         if rc != 0:
@@ -252,6 +253,13 @@ class Context:
         v = C.c_double()
         self._ck(self.lib.ann_cutoff(self.h, C.byref(v)))
         return v.value
+
+    def network_form(self, t: int):
+        """(backend, split) of the MIXED network pass for type t: backend 2 = tensor cores with
+        split 1, 2 or 3, backend 1 = SIMT (split 0)."""
+        b, s = C.c_int32(), C.c_int32()
+        self._ck(self.lib.ann_network_form(self.h, t, C.byref(b), C.byref(s)))
+        return b.value, s.value
 
     def num_inputs(self, t: int) -> int:
         n = C.c_int32()

@@ -48,7 +48,7 @@ static void reset_graph(ann_ctx* c) {
 void drop_graphs(ann_ctx* c) { reset_graph(c); }
 void rebuild_plan(ann_ctx* c) {
     build_plan(c->pot, c->plan);
-    build_tc_plan(c->plan.pot, c->plan.w, c->plan.b, c->plan.inpw, c->plan.inpb, c->max_smem, c->tc);
+    build_tc_plan(c->plan.pot, c->plan.w, c->plan.b, c->plan.inpw, c->plan.inpb, c->max_smem, c->opt.tc_split, c->tc);
     if (c->opt.mlp_backend == 2 && !c->tc.ok)
         throw ann_error(ANN_ERR_UNSUPPORTED, "the networks do not fit the tensor-core kernel (hidden layers 1..5, widths <= 256)");
     c->tcimg.ensure(c->tc.image.size());
@@ -385,7 +385,7 @@ extern "C" {
 void ann_default_options(ann_options* o) {
     if (!o) return;
     o->device = 0; o->precision = ANN_MIXED; o->newton = ANN_NEWTON_ALL_IMAGES; o->max_neighbors = 0; o->use_graphs = 1; o->mlp_backend = 0;
-    o->tc_groups = 0;
+    o->tc_groups = 0; o->tc_split = 0;
 }
 int ann_abi_version(void) { return ANN_GPU_ABI_VERSION; }
 
@@ -412,6 +412,7 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         if (c->opt.mlp_backend < 0 || c->opt.mlp_backend > 2) throw ann_error(ANN_ERR_ARG, "mlp_backend must be 0, 1 or 2");
         if (c->opt.tc_groups != 0 && c->opt.tc_groups != 1 && c->opt.tc_groups != 2 && c->opt.tc_groups != 4)
             throw ann_error(ANN_ERR_ARG, "tc_groups must be 0, 1, 2 or 4");
+        if (c->opt.tc_split < 0 || c->opt.tc_split > 3) throw ann_error(ANN_ERR_ARG, "tc_split must be 0, 1, 2 or 3");
         const char* dbg = std::getenv("ANN_DEBUG");
         c->debug = dbg && dbg[0] == '1';
         if (c->debug) c->opt.use_graphs = 0;
@@ -521,6 +522,15 @@ int ann_num_inputs(ann_ctx* c, int32_t t, int32_t* n) {
     if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
     if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
     *n = c->pot.sp[t].nInput;
+    return ANN_OK;
+}
+int ann_network_form(ann_ctx* c, int32_t t, int32_t* backend, int32_t* split) {
+    if (!c || !backend || !split) return fail(c, ANN_ERR_ARG, "NULL argument");
+    if (!c->have_pot) return fail(c, ANN_ERR_STATE, "no potential loaded");
+    if (t < 0 || t >= c->pot.ntypes()) return fail(c, ANN_ERR_ARG, "type index out of range");
+    const bool tc = use_tc(c);
+    *backend = tc ? 2 : 1;
+    *split = tc ? c->tc.t[t].split : 0;
     return ANN_OK;
 }
 int ann_num_params(ann_ctx* c, int64_t* n) {

@@ -8,7 +8,8 @@
 // an SM when tensor memory allows and the type has tiles enough; tile row r <-> TMEM lane r),
 // persistent over the type's tiles:
 //   weights   : one bulk asynchronous copy (cp.async.bulk + mbarrier) of the type's image
-//               (B operands W_l and W_l^T in the canonical K-major no-swizzle layout, BF16 hi/lo).
+//               (B operands W_l in the canonical K-major no-swizzle layout, BF16 hi/lo; the
+//               backward GEMMs read the same bytes as the MN-major operand W_l^T).
 //   per tile  : A0 = inpw*(G+inpb) split into BF16 hi+lo rows, then for every hidden layer
 //               D = A W_l^T (tcgen05.mma kind::f16, M=128, issued by one thread, completion via
 //               tcgen05.commit on an mbarrier); the epilogue (tcgen05.ld, bias, activation, next A)
@@ -54,9 +55,10 @@ static __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo
     return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
-// instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, N and M=128
-static __device__ __forceinline__ uint32_t idesc_bf16(int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+// instruction descriptor of kind::f16: D FP32, A and B BF16, A K-major, B K-major (bT = false) or
+// MN-major (bT = true, bit 16), N and M=128
+static __device__ __forceinline__ uint32_t idesc_bf16(int N, bool bT) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (bT ? (1u << 16) : 0u) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 }
 static __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
     asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
@@ -188,21 +190,26 @@ __global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constan
     const float c = tt.c;
     const uint32_t img_s = su32(img), ahi_s = su32(Ahi), alo_s = Alo ? su32(Alo) : 0u;
 
-    // one GEMM: D[tmem col] = A (rows x K) . B^T (B: N x K image), accumulate hi/lo parts
-    auto gemm = [&](uint32_t b_hi, uint32_t b_lo, int K, int N, uint32_t dcol) -> bool {
+    // one GEMM: D[tmem col] = A (rows x K) . B^T, accumulating the hi/lo parts. Forward (bT false):
+    // B is W (N x K) in the canonical K-major layout. Backward (bT true): B is W^T (N = the layer's
+    // inputs, K = its outputs), read from the same image of W as an MN-major operand: there the 8
+    // contiguous elements of a core matrix run along N and its 8 rows along K, core matrices are
+    // 128 B apart along N (stride byte offset) and N/8 * 128 B apart along K (leading byte offset)
+    auto gemm = [&](uint32_t b_hi, uint32_t b_lo, int K, int N, uint32_t dcol, bool bT) -> bool {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
         if (t == 0) {
-            const uint32_t idesc = idesc_bf16(N);
-            const uint32_t bsbo = (uint32_t)(K / 8) * 128u;
+            const uint32_t idesc = idesc_bf16(N, bT);
+            const uint32_t bk = bT ? (uint32_t)(N / 8) * 128u : 128u;           // between core matrices along K
+            const uint32_t bn = bT ? 128u : (uint32_t)(K / 8) * 128u;           // between core matrices along N
             for (int s = 0; s < K / 16; ++s) {
                 const uint64_t ad = smem_desc(ahi_s + 256u * s, 128u, asbo);
-                const uint64_t bd = smem_desc(img_s + b_hi + 256u * s, 128u, bsbo);
+                const uint64_t bd = smem_desc(img_s + b_hi + 2u * bk * s, bk, bn);
                 tc_mma(tmem + dcol, ad, bd, idesc, s > 0 ? 1u : 0u);
                 if (tt.split >= 2) tc_mma(tmem + dcol, smem_desc(alo_s + 256u * s, 128u, asbo), bd, idesc, 1u);
-                if (tt.split >= 3) tc_mma(tmem + dcol, ad, smem_desc(img_s + b_lo + 256u * s, 128u, bsbo), idesc, 1u);
+                if (tt.split >= 3) tc_mma(tmem + dcol, ad, smem_desc(img_s + b_lo + 2u * bk * s, bk, bn), idesc, 1u);
             }
             tc_commit(&bar[1]);
         }
@@ -241,7 +248,7 @@ __global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constan
         for (int l = 0; l < tt.nhidden && good; ++l) {
             const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
             const int N = tt.width[l];
-            good = gemm(tt.fwd_hi[l], tt.fwd_lo[l], Kin, N, (uint32_t)tt.fwd_col[l]);
+            good = gemm(tt.fwd_hi[l], tt.fwd_lo[l], Kin, N, (uint32_t)tt.fwd_col[l], false);
             if (!good) break;
             const float* bias = reinterpret_cast<const float*>(img + tt.bias[l]);
             const bool last = (l == tt.nhidden - 1);
@@ -269,7 +276,7 @@ __global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constan
         // ---- backward: A holds delta of hidden layer l
         for (int l = tt.nhidden - 1; l >= 0 && good; --l) {
             const int Nout = (l == 0) ? tt.K0 : tt.width[l - 1];
-            good = gemm(tt.bwd_hi[l], tt.bwd_lo[l], tt.width[l], Nout, (uint32_t)tt.bwd_col);
+            good = gemm(tt.fwd_hi[l], tt.fwd_lo[l], tt.width[l], Nout, (uint32_t)tt.bwd_col, true);
             if (!good) break;
             if (l == tt.nhidden - 1 && grp == 0 && at >= 0) {   // ered is complete after the GEMM's barrier
                 float e = 0.0f;

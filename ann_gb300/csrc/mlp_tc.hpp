@@ -17,15 +17,15 @@ constexpr int TC_TAIL_BYTES = 32 + 4 * TC_GROUPS * TC_M;
 // Operands live in shared memory in the canonical K-major no-swizzle layout of tcgen05:
 // 8-row x 16-byte core matrices (128 B each); along K adjacent core matrices are 128 B apart
 // (leading byte offset), along rows the 8-row groups are K/8 * 128 B apart (stride byte offset).
-// The image of one type holds, for every hidden layer l, the B operands of the forward GEMM
-// (W_l, N = nodes[l] x K = ni(l)) and of the backward GEMM (W_l^T, N = ni(l) x K = nodes[l]),
-// each as BF16 hi and (split > 1) lo parts, followed by FP32 vectors.
+// The image of one type holds, for every hidden layer l, the B operand of the forward GEMM
+// (W_l, N = nodes[l] x K = ni(l)) as BF16 hi and (split 3) lo parts, followed by FP32 vectors. The
+// backward GEMM's operand W_l^T is the same bytes read as an MN-major operand.
 struct TcType {
     int32_t nhidden;                 // hidden layers (the last layer is a dot product)
     int32_t nin, K0;                 // inputs and inputs padded to 16
     int32_t width[TC_MAXH];          // padded width of hidden layer l
     int32_t nodes[TC_MAXH];          // true width of hidden layer l
-    uint32_t fwd_hi[TC_MAXH], fwd_lo[TC_MAXH], bwd_hi[TC_MAXH], bwd_lo[TC_MAXH];  // byte offsets in the image
+    uint32_t fwd_hi[TC_MAXH], fwd_lo[TC_MAXH];   // byte offsets of W_l's hi / lo parts in the image (lo = hi unless split 3)
     uint32_t bias[TC_MAXH];          // byte offset of the FP32 bias of hidden layer l (padded width)
     uint32_t wlast;                  // FP32 weights of the last layer (padded width of the last hidden layer)
     uint32_t inpw, inpb;             // FP32 input scaling (K0 entries)
@@ -65,7 +65,7 @@ struct TcPlan {
 
 // builds the images from the row-major FP64 weights of the plan (w[l][n*ni+m], b[l][n])
 void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::vector<double>& b,
-                   const std::vector<double>& inpw, const std::vector<double>& inpb, int max_smem, TcPlan& out);
+                   const std::vector<double>& inpw, const std::vector<double>& inpb, int max_smem, int split_pref, TcPlan& out);
 
 // Where every network parameter lives on the device, in the packing order of ann_get_params
 // (per type: biases layer by layer, then weights layer by layer with the input index outer,
@@ -77,7 +77,8 @@ enum RegKind { REG_LASSO = 0, REG_RIDGE = 1, REG_HUBER = 2, REG_ASINH = 3, REG_N
 // PM_I64: index into the FP64/FP32 bias or row-major weight arrays; PM_IT: index into the
 // transposed weights; PM_F32: byte offset of an FP32 copy in the tensor-core images (hidden bias,
 // last-layer weight or bias); PM_FH/FL, PM_BH/BL: byte offsets of the BF16 hi/lo entries of the
-// forward (W) and backward (W^T) operands
+// forward operand W (FL -1 unless the type's weights are split); PM_BH/BL are not used (-1): the
+// backward GEMM reads W's image as W^T
 void build_param_map(const DevPot& pot, const TcPlan& tc, std::vector<int32_t>& map);
 
 struct TcArgs {

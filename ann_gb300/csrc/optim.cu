@@ -123,9 +123,9 @@ __global__ void k_param_refresh(int64_t n, const double* p, const int32_t* map, 
         const __nv_bfloat16 hi = __float2bfloat16_rn(vf);
         const __nv_bfloat16 lo = __float2bfloat16_rn(vf - __bfloat162float(hi));
         *reinterpret_cast<__nv_bfloat16*>(img + e[PM_FH]) = hi;
-        *reinterpret_cast<__nv_bfloat16*>(img + e[PM_FL]) = lo;
-        *reinterpret_cast<__nv_bfloat16*>(img + e[PM_BH]) = hi;
-        *reinterpret_cast<__nv_bfloat16*>(img + e[PM_BL]) = lo;
+        if (e[PM_FL] >= 0) *reinterpret_cast<__nv_bfloat16*>(img + e[PM_FL]) = lo;
+        if (e[PM_BH] >= 0) *reinterpret_cast<__nv_bfloat16*>(img + e[PM_BH]) = hi;
+        if (e[PM_BL] >= 0) *reinterpret_cast<__nv_bfloat16*>(img + e[PM_BL]) = lo;
     }
 }
 

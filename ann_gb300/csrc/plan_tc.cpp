@@ -38,7 +38,7 @@ size_t TcPlan::smem_bytes(int type) const {
 }
 
 void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::vector<double>& b,
-                   const std::vector<double>& inpw, const std::vector<double>& inpb, int max_smem, TcPlan& out) {
+                   const std::vector<double>& inpw, const std::vector<double>& inpb, int max_smem, int split_pref, TcPlan& out) {
     out.ok = true;
     out.image.clear();
     std::memset(out.t, 0, sizeof(out.t));
@@ -75,7 +75,7 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
         size_t bf = 0;
         for (int l = 0; l < tt.nhidden; ++l) {
             const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
-            bf += (size_t)tt.width[l] * Kin * 2 * 2;  // forward + backward
+            bf += (size_t)tt.width[l] * Kin * 2;      // W_l (the backward pass reads it as W_l^T)
         }
         size_t vec = 0;
         for (int l = 0; l < tt.nhidden; ++l) vec += (size_t)tt.width[l] * 4;
@@ -84,11 +84,15 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
             const size_t img = bf * (split == 3 ? 2 : 1) + vec + 16 * (4 * TC_MAXH + 5);
             return (img + 127) / 128 * 128 + (size_t)TC_M * tt.wmax * 2 * (split >= 2 ? 2 : 1) + TC_TAIL_BYTES;
         };
-        // both operands split (three MMAs per k-step) keep the products within ~1e-5 relative of
-        // FP32; a single-BF16 weight image (2^-9 relative) is not accurate enough for the forces,
-        // so networks whose split image does not fit run on the SIMT kernel instead
-        tt.split = 3;
-        if (total(3) + 1024 > (size_t)max_smem) { out.ok = false; continue; }
+        // operand form: split 3 (A and W as BF16 hi + lo, three MMAs per k-step) keeps the products
+        // within ~1e-5 relative of FP32; split 2 (A split, W single BF16) halves the image and the
+        // MMAs; split 1 is plain BF16 x BF16 with FP32 accumulation. split_pref 0 takes the most
+        // accurate form whose image fits a block's shared memory; a forced form that does not fit
+        // leaves the type to the SIMT kernel
+        tt.split = 0;
+        for (int s = split_pref ? split_pref : 3; s >= (split_pref ? split_pref : 1); --s)
+            if (total(s) + 1024 <= (size_t)max_smem) { tt.split = s; break; }
+        if (tt.split == 0) { out.ok = false; continue; }
         // image
         std::vector<uint8_t> img;
         auto align16 = [&]() { while (img.size() % 16) img.push_back(0); };
@@ -118,11 +122,8 @@ void build_tc_plan(const DevPot& pot, const std::vector<double>& w, const std::v
             const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
             const double* W = w.data() + net.woff[l];   // W[n*ni + m]
             auto fwd = [&](int r, int k) { return (r < no && k < ni) ? W[(size_t)r * ni + k] : 0.0; };
-            auto bwd = [&](int r, int k) { return (r < ni && k < no) ? W[(size_t)k * ni + r] : 0.0; };
             tt.fwd_hi[l] = put_operand(tt.width[l], Kin, fwd, false);
             tt.fwd_lo[l] = (tt.split == 3) ? put_operand(tt.width[l], Kin, fwd, true) : tt.fwd_hi[l];
-            tt.bwd_hi[l] = put_operand(Kin, tt.width[l], bwd, false);
-            tt.bwd_lo[l] = (tt.split == 3) ? put_operand(Kin, tt.width[l], bwd, true) : tt.bwd_hi[l];
         }
         for (int l = 0; l < tt.nhidden; ++l) {
             const int no = net.nodes[l];
@@ -168,17 +169,15 @@ void build_param_map(const DevPot& pot, const TcPlan& tc, std::vector<int32_t>& 
             const int ni = (l == 0) ? net.nin : net.nodes[l - 1], no = net.nodes[l];
             for (int m = 0; m < ni; ++m)
                 for (int n = 0; n < no; ++n) {
-                    int64_t f32 = -1, fh = -1, fl = -1, bh = -1, bl = -1;
+                    int64_t f32 = -1, fh = -1, fl = -1;
                     if (img && l < tt.nhidden) {
                         const int Kin = (l == 0) ? tt.K0 : tt.width[l - 1];
                         fh = base + tt.fwd_hi[l] + canon(n, m, Kin);
-                        fl = base + tt.fwd_lo[l] + canon(n, m, Kin);
-                        bh = base + tt.bwd_hi[l] + canon(m, n, tt.width[l]);
-                        bl = base + tt.bwd_lo[l] + canon(m, n, tt.width[l]);
+                        if (tt.split == 3) fl = base + tt.fwd_lo[l] + canon(n, m, Kin);   // lo parts only when split
                     } else if (img) {
                         f32 = base + tt.wlast + 4 * m;   // last layer: one output
                     }
-                    put(PK_WEIGHT, net.woff[l] + n * ni + m, net.woff[l] + m * no + n, f32, fh, fl, bh, bl);
+                    put(PK_WEIGHT, net.woff[l] + n * ni + m, net.woff[l] + m * no + n, f32, fh, fl, -1, -1);
                 }
         }
     }

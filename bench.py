@@ -162,6 +162,160 @@ def cpu_reference(offs, posn, types, cell, pot_text, budget_s=12.0, steps=1, war
                        f"structures block-distributed over threads (thread::Dist rule)")
 
 
+def oracle_parity(offs, posn, types, cell, pot_text, E64, F64, W64, Emx, Fmx, Wmx, threads=None):
+    """The FP64 oracle (accurate build, no FP contraction) on the whole batch, all host cores: the
+    FP64 GPU form's largest relative errors (bars: 1e-10) and the mixed form's errors in meV/atom
+    and meV/A (bars: 1 and 10), both against the oracle."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import Oracle
+    pot = Oracle().load_text(pot_text)
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    Eo, Fo, Wo, _, _ = pot.compute(offs, posn, types, cell, forces=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+    nat = np.diff(offs)
+    fp64 = {"e_rel_max": rel(E64, Eo), "f_rel_max": rel(F64, Fo), "w_rel_max": rel(W64, Wo), "bar": 1e-10}
+    fp64["within_bar"] = bool(max(fp64["e_rel_max"], fp64["f_rel_max"], fp64["w_rel_max"]) < 1e-10)
+    mixed = {"e_mev_atom_max": float(np.max(np.abs(Emx - Eo) / nat) * 1e3),
+             "f_mev_A_max": float(np.max(np.abs(Fmx - Fo)) * 1e3),
+             "f_mev_A_rms": float(np.sqrt(np.mean((Fmx - Fo) ** 2)) * 1e3),
+             "w_rel_max": rel(Wmx, Wo), "bars": "1 meV/atom, 10 meV/A"}
+    mixed["within_bar"] = bool(mixed["e_mev_atom_max"] < 1.0 and mixed["f_mev_A_max"] < 10.0)
+    return {"reference": f"FP64 oracle (CPU restatement of the reference path) on all {len(nat)} structures "
+                         f"({int(offs[-1])} atoms), {threads} threads, {dt:.1f} s",
+            "fp64_gpu_vs_oracle": fp64, "mixed_vs_oracle": mixed}, Eo, Fo
+
+
+def resident_timer(ctx, dev):
+    """CUDA-event times (ms) of E+F evaluations of a batch resident in HBM, on the library's stream,
+    with the L2 cache flushed by a 256 MiB write between steps, outside the timed events."""
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def run(offs, posn, types, cell, prec, steps, warm):
+        ctx.upload(offs, posn, types, cell)
+        for _ in range(warm):
+            ctx.compute_resident(prec)
+        ctx.download(forces=False, virial=False)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize(dev)
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+            ctx.compute_resident(prec)
+            ev[k][1].record(stream)
+        ctx.download(forces=False, virial=False)
+        torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in ev]
+
+    def phases(offs, posn, types, cell, prec, steps, warm):
+        ctx.profile_phases(True)
+        ctx.upload(offs, posn, types, cell)
+        out = []
+        for k in range(warm + steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ctx.compute_resident(prec)
+            ctx.synchronize()
+            if k >= warm:
+                out.append(ctx.phase_times())
+        ctx.profile_phases(False)
+        return dict(zip(PHASES, map(float, np.mean(np.array(out), axis=0))))
+
+    run.phases = phases
+    return run
+
+
+PHASES = ["neighbour_list", "type_lists", "symmetry_functions", "networks", "forces", "reductions"]
+
+
+def _errors_vs(E, F, Eo, Fo, offs):
+    nat = np.diff(offs)
+    return {"e_mev_atom_max": float(np.max(np.abs(E - Eo) / nat) * 1e3), "f_mev_A_max": float(np.max(np.abs(F - Fo)) * 1e3),
+            "f_mev_A_rms": float(np.sqrt(np.mean((F - Fo) ** 2)) * 1e3)}
+
+
+def network_forms_leg(dev, offs, posn, types, cell, pot_text, Eo, Fo, steps=10, warmup=3):
+    """The E+F workload with each operand form of the tensor-core networks (1: BF16 activations and
+    weights; 2: activations split hi + lo; 3: both split), FP32 accumulation throughout: step time
+    and network-phase time (CUDA events) and the errors against the FP64 oracle."""
+    from ann_gb300 import MIXED, Context
+    out = {"workload": "the E+F workload above", "reference": "FP64 oracle on the whole batch"}
+    N = int(offs[-1])
+    for split in (1, 2, 3):
+        ctx = Context(device=dev, mlp_backend=2, tc_split=split)
+        try:
+            ctx.load_text(pot_text)
+            E, F, _ = ctx.compute(offs, posn, types, cell, precision=MIXED)
+            run = resident_timer(ctx, dev)
+            ms = float(np.mean(run(offs, posn, types, cell, MIXED, steps, warmup)))
+            ph = run.phases(offs, posn, types, cell, MIXED, steps, warmup)
+            out[f"split{split}"] = dict(_errors_vs(E, F, Eo, Fo, offs), ms_per_step=ms, atom_evals_per_s=N / (ms * 1e-3),
+                                        networks_ms=ph["networks"], forms=[ctx.network_form(t) for t in range(ctx.ntypes)])
+        finally:
+            ctx.close()
+    return out
+
+
+def precision_study_leg(dev, steps=10, warmup=3):
+    """The large-frame precision study: one ternary A:B:C = 1:1:2 periodic box of 32,000 atoms (jittered
+    simple-cubic lattice 40 x 40 x 20 at 0.07 /A^3, sigma 0.15 A), rc = 6 A, 96 inputs (16 radial per
+    species, 8 angular per pair), 96-128-128-1 tanh networks. The FP64 oracle (atoms split over all
+    host cores) against the FP64 GPU form (relative errors) and against each mixed form (meV/atom,
+    meV/A), with their E+F throughput (CUDA events, box resident, L2 flushed between steps)."""
+    import tempfile
+    from ann_gb300 import FP64, MIXED, Context
+    from ann_gb300 import workloads as WL
+    from ann_gb300.api import pack_batch
+    structs = WL.config4()
+    offs, posn, types, cell = pack_batch(structs)
+    N = int(offs[-1])
+    ctx = Context(device=dev)
+    WL.make_potential(ctx, 4)
+    WL.precondition(ctx, offs, posn, types, cell)
+    with tempfile.TemporaryDirectory() as td:
+        p = Path(td) / "pot.ann"
+        ctx.write(p)
+        pot_text = p.read_text()
+    ctx.close()
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_lib import Oracle
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    Eo, Fo, Wo, _, _ = Oracle().load_text(pot_text).compute(offs, posn, types, cell, nthreads=threads)
+    t_orc = time.perf_counter() - t0
+    out = {"workload": f"ternary box, {N} atoms (1:1:2), rho 0.07/A^3, rc 6 A, 96 inputs, 96-128-128-1 tanh",
+           "reference": f"FP64 oracle, atoms split over {threads} threads, {t_orc:.1f} s"}
+    forms = (("fp64", FP64, {}), ("mixed_tc_split3", MIXED, {"mlp_backend": 2, "tc_split": 3}),
+             ("mixed_tc_split2", MIXED, {"mlp_backend": 2, "tc_split": 2}),
+             ("mixed_tc_split1", MIXED, {"mlp_backend": 2, "tc_split": 1}), ("mixed_simt", MIXED, {"mlp_backend": 1}))
+    for name, prec, kw in forms:
+        ctx = Context(device=dev, **kw)
+        try:
+            ctx.load_text(pot_text)
+            E, F, Wv = ctx.compute(offs, posn, types, cell, precision=prec)
+            run = resident_timer(ctx, dev)
+            ms = float(np.mean(run(offs, posn, types, cell, prec, steps, warmup)))
+            ph = run.phases(offs, posn, types, cell, prec, steps, warmup)
+            r = dict(_errors_vs(E, F, Eo, Fo, offs), ms_per_step=ms, atom_evals_per_s=N / (ms * 1e-3), phase_ms=ph)
+            if prec == FP64:
+                r["e_rel"] = float(abs(E[0] - Eo[0]) / abs(Eo[0]))
+                r["f_rel_max"] = float(np.max(np.abs(F - Fo)) / np.max(np.abs(Fo)))
+                r["w_rel_max"] = float(np.max(np.abs(Wv - Wo)) / np.max(np.abs(Wo)))
+            else:
+                r["forms"] = [ctx.network_form(t) for t in range(ctx.ntypes)]
+            out[name] = r
+        finally:
+            ctx.close()
+    return out
+
+
 def training_leg(dev, steps=10, warmup=3):
     """Training throughput on the 64-structure binary batch with Lennard-Jones labels: one
     ann_train_forward + ann_train_backward (loss, adjoint, parameter gradient) + ann_adam_step
@@ -277,18 +431,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the FP64 oracle run over the whole batch (accuracy and parity)")
     ap.add_argument("--nstruc", type=int, default=256)
     ap.add_argument("--no-extras", action="store_true", help="skip the training and MD legs")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the built-in launch shapes (no autotuner launches before the timed steps, e.g. for "
                          "ncu captures that select launches by position)")
-    ap.add_argument("--only", choices=["training", "md", "lammps"],
+    ap.add_argument("--only", choices=["training", "md", "lammps", "precision"],
                     help="run one secondary leg alone with --steps / --warmup and print its JSON (for profiling)")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     W_ = max(args.warmup, 3)
     if args.only:
-        leg = {"training": training_leg, "md": md_leg, "lammps": lammps_leg}[args.only]
+        leg = {"training": training_leg, "md": md_leg, "lammps": lammps_leg, "precision": precision_study_leg}[args.only]
         print(json.dumps({args.only: leg(local if world > 1 else 0, steps=args.steps, warmup=args.warmup)}))
         return
 
@@ -335,13 +490,13 @@ def main():
     ctx.load_text(pot_text)
 
     # ---- accuracy of the mixed path vs the FP64 path on the same batch
-    E64, F64, _ = ctx.compute(offs, posn, types, cell, precision=FP64)
-    Emx, Fmx, _ = ctx.compute(offs, posn, types, cell, precision=MIXED)
+    E64, F64, W64 = ctx.compute(offs, posn, types, cell, precision=FP64)
+    Emx, Fmx, Wmx = ctx.compute(offs, posn, types, cell, precision=MIXED)
     nat = np.diff(offs)
-    acc = {"e_mev_atom_max": float(np.max(np.abs(Emx - E64) / nat) * 1e3),
-           "f_mev_A_max": float(np.max(np.abs(Fmx - F64)) * 1e3),
-           "f_mev_A_rms": float(np.sqrt(np.mean((Fmx - F64) ** 2)) * 1e3),
-           "reference": "plain FP64 GPU form on the same batch"}
+    acc_fp64 = {"e_mev_atom_max": float(np.max(np.abs(Emx - E64) / nat) * 1e3),
+                "f_mev_A_max": float(np.max(np.abs(Fmx - F64)) * 1e3),
+                "f_mev_A_rms": float(np.sqrt(np.mean((Fmx - F64) ** 2)) * 1e3),
+                "reference": "plain FP64 GPU form on the same batch"}
     work = algorithmic_work(ctx, offs, posn, types, cell)
 
     # ---- launch shapes picked by the library's autotuner on this batch (outside the timed region,
@@ -354,25 +509,10 @@ def main():
         tuned = ctx.autotune(precision=MIXED, reps=5)
     shapes = {k: tuned[k] for k in SHAPE_KEYS}
 
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    timer = resident_timer(ctx, dev)
 
     def timed_device(prec, steps, warm):
-        ctx.upload(offs, posn, types, cell)
-        for _ in range(warm):
-            ctx.compute_resident(prec)
-        ctx.download(forces=False, virial=False)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        torch.cuda.synchronize(dev)
-        for k in range(steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                ev[k][0].record(stream)
-            ctx.compute_resident(prec)
-            ev[k][1].record(stream)
-        ctx.download(forces=False, virial=False)
-        torch.cuda.synchronize(dev)
-        return [a.elapsed_time(b) for a, b in ev]
+        return timer(offs, posn, types, cell, prec, steps, warm)
 
     if world > 1:
         import torch.distributed as dist
@@ -401,20 +541,9 @@ def main():
     ctx.set_tuning(**shapes)
 
     # ---- per-phase kernel durations (CUDA events around each phase on the library stream)
-    ctx.profile_phases(True)
-    ctx.upload(offs, posn, types, cell)
-    phases = []
-    for k in range(W_ + args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        ctx.compute_resident(MIXED)
-        ctx.synchronize()
-        if k >= W_:
-            phases.append(ctx.phase_times())
-    ctx.profile_phases(False)
-    ph = np.mean(np.array(phases), axis=0)
-    names = ["neighbour_list", "type_lists", "symmetry_functions", "networks", "forces", "reductions"]
-    phase_ms = {n: float(v) for n, v in zip(names, ph)}
+    phase_ms = timer.phases(offs, posn, types, cell, MIXED, args.steps, W_)
+    names = PHASES
+    ph = np.array([phase_ms[n] for n in names])
     dom = int(np.argmax(ph))
     from ann_gb300.api import peaks
     pk = peaks()
@@ -469,15 +598,22 @@ def main():
                                          "fp64": {k: tuned64[k] for k in SHAPE_KEYS}},
                        "parallelism": f"replicas x{world} (structures sharded, no collective)"},
             "fp64_value": fp64_value, "speedup_vs_fp64": value / world / fp64_value,
-            "accuracy": acc, "phase_ms": phase_ms, "work": work,
+            "accuracy_vs_fp64_gpu": acc_fp64, "phase_ms": phase_ms, "work": work,
             "roofline": roofline, "roofline_compute": roofline_compute,
             "e2e": {"value": N / t_e2e, "unit": "atom-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk, "wall_s_timed_region": t_wall}
+    if rank == 0 and not args.no_parity:
+        par, Eo, Fo = oracle_parity(offs, posn, types, cell, pot_text, E64, F64, W64, Emx, Fmx, Wmx)
+        line["accuracy"] = dict(par["mixed_vs_oracle"], reference=par["reference"])
+        line["parity"] = par
+        if world == 1 and not args.no_extras:
+            line["network_forms"] = network_forms_leg(dev, offs, posn, types, cell, pot_text, Eo, Fo)
     if rank == 0 and world == 1 and not args.no_extras:
         line["training"] = training_leg(dev)
         line["md"] = md_leg(dev)
         line["lammps"] = lammps_leg(dev)
+        line["precision_study"] = precision_study_leg(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(offs, posn, types, cell, pot_text)
     if rank == 0:

@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define ANN_GPU_ABI_VERSION 2
+#define ANN_GPU_ABI_VERSION 3
 
 enum ann_status {
     ANN_OK = 0,
@@ -71,6 +71,10 @@ typedef struct ann_options {
     int32_t mlp_backend;         /* 0 = auto, 1 = SIMT kernels, 2 = tcgen05 tensor-core kernels (MIXED) */
     int32_t tc_groups;           /* tensor-core network kernel: warps per TMEM lane quadrant, 1, 2 or 4 */
                                  /* (4 / tc_groups CTAs per SM); 0 = chosen per launch                 */
+    int32_t tc_split;            /* tensor-core network operands: 1 = single BF16 activations and       */
+                                 /* weights, 2 = activations split hi + lo (2 MMAs per k-step), 3 = both */
+                                 /* split (3 MMAs); 0 = the most accurate form whose image fits shared  */
+                                 /* memory. A type whose networks fit no allowed form runs on SIMT      */
 } ann_options;
 
 typedef struct ann_ctx ann_ctx;
@@ -91,6 +95,9 @@ int ann_type_index(ann_ctx* ctx, const char* name, int32_t* index);   /* NNP::in
 int ann_type_name(ann_ctx* ctx, int32_t index, char* buf, int32_t buflen);
 int ann_cutoff(ann_ctx* ctx, double* rc);
 int ann_num_inputs(ann_ctx* ctx, int32_t type, int32_t* ninput);       /* NNH::nInput               */
+/* The form the MIXED network pass takes for a type (no reference counterpart): backend 2 = tcgen05
+ * tensor cores with split = 1, 2 or 3 (ann_options.tc_split), 1 = SIMT kernel (split 0).          */
+int ann_network_form(ann_ctx* ctx, int32_t type, int32_t* backend, int32_t* split);
 int ann_num_params(ann_ctx* ctx, int64_t* nparams);                     /* NNP::size (nnp.cpp:47-53) */
 int ann_get_params(ann_ctx* ctx, double* params, int64_t nparams);      /* types in NNP order        */
 int ann_set_params(ann_ctx* ctx, const double* params, int64_t nparams);

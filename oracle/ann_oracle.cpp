@@ -22,6 +22,7 @@
 // The canonical arithmetic (no fused multiply-add, fixed association) is shared with the GPU
 // FP64 path so that the two lists agree bit for bit.
 // ============================================================================================
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -790,8 +791,112 @@ static inline void pair_vec(const double* xi, const double* xj, const double* R,
     }
     d2 = (r[0] * r[0] + r[1] * r[1]) + r[2] * r[2];
 }
-// brute force over all atoms and all images; order: j ascending, then n lexicographic
+// The periodic-image neighbour list (the NeighborList(struc, rc) contract): every (j, n) with
+// |x_i - x_j - R n| < rc except (i, 0), each row ordered by j ascending, then n lexicographic.
+// Rows [i0, i1) are filled (out sized to N by the caller), so threads can share one structure.
+// Small cells (fewer than three bins of width >= rc along some lattice direction) take the brute
+// force over all atoms and images; larger ones a cell-binned search that tests the same pairs with
+// the same formula and sorts each row into the same order.
+struct NeighborGrid {
+    int N = 0;
+    const double* x = nullptr;
+    const double* R = nullptr;
+    double rc = 0, Ri[9], gn[3];
+    std::vector<double> s;                 // fractional coordinates
+    bool binned = false;
+    int nb[3] = {1, 1, 1};
+    std::vector<int> k, bin, start, list;  // floor(s) per atom and direction; bin of each atom; CSR of the bins
+    NeighborGrid(int N_, const double* x_, const double* R_, double rc_) : N(N_), x(x_), R(R_), rc(rc_) {
+        inv3(R, Ri);
+        for (int d = 0; d < 3; ++d) gn[d] = std::sqrt(Ri[d] * Ri[d] + Ri[3 + d] * Ri[3 + d] + Ri[6 + d] * Ri[6 + d]);
+        s.resize(3 * (size_t)N);
+        for (int i = 0; i < N; ++i) for (int d = 0; d < 3; ++d) s[3 * i + d] = Ri[d] * x[3 * i] + Ri[3 + d] * x[3 * i + 1] + Ri[6 + d] * x[3 * i + 2];
+        binned = N > 512;
+        for (int d = 0; d < 3; ++d) {
+            // bins at least rc (plus a margin for rounding) high along lattice direction d
+            nb[d] = (int)std::floor(1.0 / (rc * gn[d] * (1.0 + 1e-9)));
+            if (nb[d] < 3) binned = false;
+        }
+        if (!binned) return;
+        k.resize(3 * (size_t)N);
+        bin.resize(N);
+        const long long nbins = (long long)nb[0] * nb[1] * nb[2];
+        start.assign(nbins + 1, 0);
+        for (int i = 0; i < N; ++i) {
+            int b[3];
+            for (int d = 0; d < 3; ++d) {
+                const double fl = std::floor(s[3 * i + d]);
+                k[3 * i + d] = (int)fl;
+                b[d] = std::min(nb[d] - 1, std::max(0, (int)std::floor((s[3 * i + d] - fl) * nb[d])));
+            }
+            bin[i] = (b[0] * nb[1] + b[1]) * nb[2] + b[2];
+            ++start[bin[i] + 1];
+        }
+        for (long long q = 0; q < nbins; ++q) start[q + 1] += start[q];
+        list.resize(N);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int i = 0; i < N; ++i) list[fill[bin[i]]++] = i;
+    }
+    void test(int i, int j, const int* n, std::vector<Neigh>& row) const {
+        if (j == i && n[0] == 0 && n[1] == 0 && n[2] == 0) return;
+        Neigh e; double d2;
+        pair_vec(x + 3 * i, x + 3 * j, R, n, e.r, d2);
+        if (d2 < rc * rc) { e.j = j; e.n[0] = n[0]; e.n[1] = n[1]; e.n[2] = n[2]; e.d = std::sqrt(d2); row.push_back(e); }
+    }
+    void rows(int i0, int i1, std::vector<std::vector<Neigh>>& out) const {
+        for (int i = i0; i < i1; ++i) {
+            std::vector<Neigh>& row = out[i];
+            row.clear();
+            if (!binned) {
+                for (int j = 0; j < N; ++j) {
+                    int lo[3], hi[3];
+                    for (int d = 0; d < 3; ++d) {
+                        const double ds = s[3 * i + d] - s[3 * j + d];
+                        const double rr = rc * gn[d];
+                        lo[d] = (int)std::floor(ds - rr) - 1; hi[d] = (int)std::ceil(ds + rr) + 1;
+                    }
+                    int n[3];
+                    for (n[0] = lo[0]; n[0] <= hi[0]; ++n[0]) for (n[1] = lo[1]; n[1] <= hi[1]; ++n[1]) for (n[2] = lo[2]; n[2] <= hi[2]; ++n[2])
+                        test(i, j, n, row);
+                }
+                continue;
+            }
+            // the 27 bins around i's (nb >= 3: each neighbour bin and image shift is visited once);
+            // an atom j of bin t' = t mod nb, reached through t = b_i + delta, is the image whose
+            // wrapped fractional position lies in t: n = floor(t / nb) + floor(s_i) - floor(s_j)
+            const int bi = bin[i];
+            const int b0 = bi / (nb[1] * nb[2]), b1 = (bi / nb[2]) % nb[1], b2 = bi % nb[2];
+            for (int d0 = -1; d0 <= 1; ++d0) for (int d1 = -1; d1 <= 1; ++d1) for (int d2 = -1; d2 <= 1; ++d2) {
+                const int t[3] = {b0 + d0, b1 + d1, b2 + d2};
+                int tw[3], wrap[3];
+                for (int d = 0; d < 3; ++d) {
+                    wrap[d] = (t[d] < 0) ? -1 : (t[d] >= nb[d]) ? 1 : 0;
+                    tw[d] = t[d] - wrap[d] * nb[d];
+                }
+                const int tb = (tw[0] * nb[1] + tw[1]) * nb[2] + tw[2];
+                for (int q = start[tb]; q < start[tb + 1]; ++q) {
+                    const int j = list[q];
+                    int n[3];
+                    for (int d = 0; d < 3; ++d) n[d] = wrap[d] + k[3 * i + d] - k[3 * j + d];
+                    test(i, j, n, row);
+                }
+            }
+            std::sort(row.begin(), row.end(), [](const Neigh& a, const Neigh& b) {
+                if (a.j != b.j) return a.j < b.j;
+                if (a.n[0] != b.n[0]) return a.n[0] < b.n[0];
+                if (a.n[1] != b.n[1]) return a.n[1] < b.n[1];
+                return a.n[2] < b.n[2];
+            });
+        }
+    }
+};
 static void neighbors(int N, const double* x, const double* R, double rc, std::vector<std::vector<Neigh>>& out) {
+    NeighborGrid g(N, x, R, rc);
+    out.assign(N, {});
+    g.rows(0, N, out);
+}
+// brute force over all atoms and all images (kept as the definition the binned search is checked against)
+static void neighbors_brute(int N, const double* x, const double* R, double rc, std::vector<std::vector<Neigh>>& out) {
     double Ri[9];
     inv3(R, Ri);
     double gn[3];
@@ -828,11 +933,10 @@ struct Struc {
     std::vector<std::vector<Neigh>> nl;
     std::vector<std::vector<double>> symm;
 };
-// NNP::symm (nnp.cpp:333-375)
-static void compute_symm(const NNP& p, Struc& s) {
-    s.symm.assign(s.N, {});
+// NNP::symm (nnp.cpp:333-375), rows [i0, i1) (s.symm sized to N by the caller)
+static void compute_symm_rows(const NNP& p, Struc& s, int i0, int i1) {
     std::vector<double> buf(256);
-    for (int i = 0; i < s.N; ++i) {
+    for (int i = i0; i < i1; ++i) {
         const NNH& h = p.h[s.type[i]];
         std::vector<double>& G = s.symm[i];
         G.assign(h.nInput, 0.0);
@@ -856,19 +960,22 @@ static void compute_symm(const NNP& p, Struc& s) {
         }
     }
 }
+static void compute_symm(const NNP& p, Struc& s) {
+    s.symm.assign(s.N, {});
+    compute_symm_rows(p, s, 0, s.N);
+}
 // newton: 1 = Newton-3rd term for every neighbour entry (images included);
 //         0 = only for the untranslated image n == 0 (the verlet::List rule of nnp.cpp:550)
 // Returns E (network outputs + per-type vacuum energies, as NNH::energy nnh.cpp:118-121 /
 // PotNNPE::compute pot_nnpe.cpp:220); forces into F (3N); virial W = sum r_ij (x) v_ij into W (9, row-major W[a*3+b]).
 // Optional: dEdG per atom (out), atomic energies.
-static double compute_force(NNP& p, Struc& s, double* F, double* W, int newton,
-                            std::vector<std::vector<double>>* dEdG_out = nullptr, double* Eatom = nullptr) {
+// compute_force_rows adds the contributions of centre atoms [i0, i1) to F and W and returns their
+// energy (dEdG_out sized to N by the caller).
+static double compute_force_rows(NNP& p, Struc& s, double* F, double* W, int newton, std::vector<std::vector<double>>* dEdG_out,
+                                 double* Eatom, int i0, int i1) {
     double E = 0;
-    for (int i = 0; i < 3 * s.N; ++i) F[i] = 0;
-    if (W) for (int i = 0; i < 9; ++i) W[i] = 0;
-    if (dEdG_out) dEdG_out->assign(s.N, {});
     std::vector<double> dEdG;
-    for (int i = 0; i < s.N; ++i) {
+    for (int i = i0; i < i1; ++i) {
         NNH& h = p.h[s.type[i]];
         const double ei = h.nn.forward(s.symm[i].data()) + h.energy;
         E += ei;
@@ -907,6 +1014,60 @@ static double compute_force(NNP& p, Struc& s, double* F, double* W, int newton,
                 if (W) for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) W[3 * a + b] += rIJ[a] * vj[b] + rIK[a] * vk[b];
             }
         }
+    }
+    return E;
+}
+static double compute_force(NNP& p, Struc& s, double* F, double* W, int newton,
+                            std::vector<std::vector<double>>* dEdG_out = nullptr, double* Eatom = nullptr) {
+    for (int i = 0; i < 3 * s.N; ++i) F[i] = 0;
+    if (W) for (int i = 0; i < 9; ++i) W[i] = 0;
+    if (dEdG_out) dEdG_out->assign(s.N, {});
+    return compute_force_rows(p, s, F, W, newton, dEdG_out, Eatom, 0, s.N);
+}
+// One structure on nthreads threads, its atoms in contiguous blocks (the atom split of the
+// reference's two-tier parallelism, nnptef.cpp:1607-1669): neighbour rows, symmetry functions and
+// force contributions per block, each thread with its own NNP copy and force / virial buffers, the
+// blocks' sums added in block order. Fills s.nl and s.symm; returns E.
+static double compute_struc_threaded(const NNP& p0, Struc& s, double* F, double* W, int newton,
+                                     std::vector<std::vector<double>>* dEdG_out, int nthreads) {
+    const int N = s.N;
+    nthreads = std::max(1, std::min(nthreads, N));
+    auto block = [&](int t, int& lo, int& hi) {
+        const int q = N / nthreads, r = N % nthreads;
+        lo = t * q + std::min(t, r); hi = lo + q + (t < r ? 1 : 0);
+    };
+    std::vector<std::string> errs(nthreads);
+    auto par = [&](auto fn) {
+        std::vector<std::thread> th;
+        auto run = [&](int t) { try { int lo, hi; block(t, lo, hi); fn(t, lo, hi); } catch (std::exception& e) { errs[t] = e.what(); } };
+        for (int t = 1; t < nthreads; ++t) th.emplace_back(run, t);
+        run(0);
+        for (auto& x : th) x.join();
+        for (auto& e : errs) if (!e.empty()) throw std::runtime_error(e);
+    };
+    NeighborGrid g(N, s.x, s.R, p0.rc);
+    s.nl.assign(N, {});
+    par([&](int, int lo, int hi) { g.rows(lo, hi, s.nl); });
+    s.symm.assign(N, {});
+    par([&](int, int lo, int hi) { compute_symm_rows(p0, s, lo, hi); });
+    if (dEdG_out) dEdG_out->assign(N, {});
+    std::vector<std::vector<double>> Ft(nthreads, std::vector<double>(F ? 3 * (size_t)N : 0, 0.0));
+    std::vector<std::array<double, 9>> Wt(nthreads);
+    std::vector<double> Et(nthreads, 0.0);
+    par([&](int t, int lo, int hi) {
+        NNP p = p0;
+        Wt[t].fill(0.0);
+        std::vector<double> Fl;
+        double* Fp = F ? Ft[t].data() : (Fl.assign(3 * (size_t)N, 0.0), Fl.data());
+        Et[t] = compute_force_rows(p, s, Fp, Wt[t].data(), newton, dEdG_out, nullptr, lo, hi);
+    });
+    double E = 0;
+    if (F) for (size_t a = 0; a < 3 * (size_t)N; ++a) F[a] = 0;
+    if (W) for (int a = 0; a < 9; ++a) W[a] = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        E += Et[t];
+        if (F) for (size_t a = 0; a < 3 * (size_t)N; ++a) F[a] += Ft[t][a];
+        if (W) for (int a = 0; a < 9; ++a) W[a] += Wt[t][a];
     }
     return E;
 }
@@ -1027,12 +1188,14 @@ int orc_basisA(int cutname, double rc, int name, int n, const double* eta, const
     } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
 
-// neighbour list of one structure; returns the count, or -(count) if cap is too small
+// neighbour list of one structure; returns the count, or -(count) if cap is too small.
+// brute = 1 takes the all-pairs search whatever the cell (the definition the binned search must equal)
 long long orc_neighbors(int N, const double* x, const double* R, double rc, long long cap,
-                        int* iout, int* jout, int* nout, double* rout, double* dout) {
+                        int* iout, int* jout, int* nout, double* rout, double* dout, int brute) {
     try {
         std::vector<std::vector<Neigh>> nl;
-        neighbors(N, x, R, rc, nl);
+        if (brute) neighbors_brute(N, x, R, rc, nl);
+        else neighbors(N, x, R, rc, nl);
         long long cnt = 0;
         for (int i = 0; i < N; ++i) cnt += nl[i].size();
         if (cnt > cap) return -cnt;
@@ -1048,10 +1211,28 @@ long long orc_neighbors(int N, const double* x, const double* R, double rc, long
 
 // batched E(+F, virial, symmetry functions, dE/dG); structures split over nthreads with the
 // thread::Dist block rule (thread/dist.hpp:21-53, nnpce.cpp:228): thread t owns a contiguous block.
+// With fewer structures than threads, each structure is split into atom blocks instead.
 int orc_compute(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
                 double* energy, double* forces, double* virial, double* symm, double* dedg, int imax, int newton, int nthreads) {
     NNP* p0 = (NNP*)pp;
     if (nthreads < 1) nthreads = 1;
+    if (nthreads > 1 && nstruc < nthreads) {
+        try {
+            for (int si = 0; si < nstruc; ++si) {
+                Struc s; s.N = (int)(off[si + 1] - off[si]);
+                s.x = x + 3 * off[si]; s.type = type + off[si]; s.R = cell + 9 * si;
+                for (int i = 0; i < s.N; ++i) if (s.type[i] < 0 || s.type[i] >= p0->ntypes()) throw std::invalid_argument("invalid type index");
+                if (s.N == 0) { energy[si] = 0; if (virial) for (int a = 0; a < 9; ++a) virial[9 * si + a] = 0; continue; }
+                std::vector<std::vector<double>> dE;
+                double W[9];
+                energy[si] = compute_struc_threaded(*p0, s, forces ? forces + 3 * off[si] : nullptr, W, newton, dedg ? &dE : nullptr, nthreads);
+                if (virial) std::memcpy(virial + 9 * si, W, sizeof(W));
+                if (symm) for (int i = 0; i < s.N; ++i) { double* row = symm + (size_t)(off[si] + i) * imax; for (int m = 0; m < imax; ++m) row[m] = m < (int)s.symm[i].size() ? s.symm[i][m] : 0.0; }
+                if (dedg) for (int i = 0; i < s.N; ++i) { double* row = dedg + (size_t)(off[si] + i) * imax; for (int m = 0; m < imax; ++m) row[m] = m < (int)dE[i].size() ? dE[i][m] : 0.0; }
+            }
+            return 0;
+        } catch (std::exception& e) { g_err = e.what(); return 1; }
+    }
     if (nthreads > nstruc) nthreads = nstruc > 0 ? nstruc : 1;
     std::vector<std::string> errs(nthreads);
     auto work = [&](int t) {
@@ -1127,41 +1308,68 @@ static void energy_loss(int loss, int norm, double delta, double dE, double nAto
     }
 }
 
+// Structures are split over nthreads with the thread::Dist block rule (each thread its own NNP copy
+// and gradient); the per-thread sums are added in thread order, as the reference's MPI_Reduce adds
+// the ranks' gradients (nnptefr2.cpp:984).
 int orc_train_ex(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
                  const double* Eref, const double* Fref, double wE, double wF, int loss, int norm, double delta, double* loss3,
-                 double* grad) {
+                 double* grad, int nthreads) {
     try {
-        NNP& p = *(NNP*)pp;
-        const int P = p.nparams();
-        std::vector<int> poff(p.ntypes() + 1, 0);
-        for (int t = 0; t < p.ntypes(); ++t) poff[t + 1] = poff[t] + p.h[t].nn.size();
+        NNP& p0 = *(NNP*)pp;
+        const int P = p0.nparams();
+        std::vector<int> poff(p0.ntypes() + 1, 0);
+        for (int t = 0; t < p0.ntypes(); ++t) poff[t + 1] = poff[t] + p0.h[t].nn.size();
         for (int k = 0; k < P; ++k) grad[k] = 0;
         const long long Ntot = off[nstruc];
+        if (nthreads < 1) nthreads = 1;
+        if (nthreads > nstruc) nthreads = nstruc > 0 ? nstruc : 1;
+        std::vector<std::vector<double>> gt(nthreads, std::vector<double>(P, 0.0));
+        std::vector<double> LEt(nthreads, 0.0), LFt(nthreads, 0.0);
+        std::vector<std::string> errs(nthreads);
+        auto work = [&](int th) {
+          try {
+            NNP p = p0;
+            double* g = gt[th].data();
+            double LE = 0, LF = 0;
+            const int q = nstruc / nthreads, r = nstruc % nthreads;
+            const int lo = th * q + std::min(th, r), hi = lo + q + (th < r ? 1 : 0);
+            for (int si = lo; si < hi; ++si) {
+                Struc s; s.N = (int)(off[si + 1] - off[si]);
+                s.x = x + 3 * off[si]; s.type = type + off[si]; s.R = cell + 9 * si;
+                neighbors(s.N, s.x, s.R, p.rc, s.nl);
+                compute_symm(p, s);
+                std::vector<double> F(3 * (size_t)s.N);
+                const double E = compute_force(p, s, F.data(), nullptr, 1);
+                double Ls, gfac;
+                energy_loss(loss, norm, delta, E - Eref[si], (double)s.N, Ls, gfac);
+                LE += Ls;
+                const double ce = wE / nstruc * gfac;
+                std::vector<double> lam(3 * (size_t)s.N);
+                for (int a = 0; a < 3 * s.N; ++a) {
+                    const double df = F[a] - Fref[3 * off[si] + a];
+                    LF += 0.5 * df * df;
+                    lam[a] = wF / (3.0 * Ntot) * df;
+                }
+                std::vector<std::vector<double>> u;
+                symm_jvp(p, s, lam.data(), u);
+                for (int i = 0; i < s.N; ++i) {
+                    const int t = s.type[i];
+                    p.h[t].nn.forward(s.symm[i].data());
+                    p.h[t].nn.jvp_grad(u[i].data(), ce, -1.0, g + poff[t]);
+                }
+            }
+            LEt[th] = LE; LFt[th] = LF;
+          } catch (std::exception& e) { errs[th] = e.what(); }
+        };
+        std::vector<std::thread> ths;
+        for (int th = 1; th < nthreads; ++th) ths.emplace_back(work, th);
+        work(0);
+        for (auto& tt : ths) tt.join();
+        for (auto& e : errs) if (!e.empty()) throw std::runtime_error(e);
         double LE = 0, LF = 0;
-        for (int si = 0; si < nstruc; ++si) {
-            Struc s; s.N = (int)(off[si + 1] - off[si]);
-            s.x = x + 3 * off[si]; s.type = type + off[si]; s.R = cell + 9 * si;
-            neighbors(s.N, s.x, s.R, p.rc, s.nl);
-            compute_symm(p, s);
-            std::vector<double> F(3 * (size_t)s.N);
-            const double E = compute_force(p, s, F.data(), nullptr, 1);
-            double Ls, gfac;
-            energy_loss(loss, norm, delta, E - Eref[si], (double)s.N, Ls, gfac);
-            LE += Ls;
-            const double ce = wE / nstruc * gfac;
-            std::vector<double> lam(3 * (size_t)s.N);
-            for (int a = 0; a < 3 * s.N; ++a) {
-                const double df = F[a] - Fref[3 * off[si] + a];
-                LF += 0.5 * df * df;
-                lam[a] = wF / (3.0 * Ntot) * df;
-            }
-            std::vector<std::vector<double>> u;
-            symm_jvp(p, s, lam.data(), u);
-            for (int i = 0; i < s.N; ++i) {
-                const int t = s.type[i];
-                p.h[t].nn.forward(s.symm[i].data());
-                p.h[t].nn.jvp_grad(u[i].data(), ce, -1.0, grad + poff[t]);
-            }
+        for (int th = 0; th < nthreads; ++th) {
+            LE += LEt[th]; LF += LFt[th];
+            for (int k = 0; k < P; ++k) grad[k] += gt[th][k];
         }
         LE *= wE / nstruc;
         LF *= wF / (3.0 * Ntot);
@@ -1172,7 +1380,7 @@ int orc_train_ex(void* pp, int nstruc, const long long* off, const double* x, co
 
 int orc_train(void* pp, int nstruc, const long long* off, const double* x, const int* type, const double* cell,
               const double* Eref, const double* Fref, double wE, double wF, double* loss3, double* grad) {
-    return orc_train_ex(pp, nstruc, off, x, type, cell, Eref, Fref, wE, wF, 1, 1, 1.0, loss3, grad);
+    return orc_train_ex(pp, nstruc, off, x, type, cell, Eref, Fref, wE, wF, 1, 1, 1.0, loss3, grad, 1);
 }
 
 // NNPTEFR::error_cost_o1 restated literally (energy only, nnptefr2.cpp:1321-1374; MSE, LINEAR norm

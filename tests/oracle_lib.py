@@ -84,12 +84,13 @@ class Oracle:
         L.orc_basisR.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, C.c_double, _D, _D, _D, _D]
         L.orc_basisA.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, _I, C.c_double, C.c_double, C.c_double, _D, _D, _D, _D, _D]
         L.orc_neighbors.restype = C.c_longlong
-        L.orc_neighbors.argtypes = [C.c_int, _D, _D, C.c_double, C.c_longlong, _I, _I, _I, _D, _D]
+        L.orc_neighbors.argtypes = [C.c_int, _D, _D, C.c_double, C.c_longlong, _I, _I, _I, _D, _D, C.c_int]
         L.orc_compute.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int]
         L.orc_train.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_double, C.c_double, _D, _D]
         L.orc_error_cost_o1.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, _D]
         L.orc_error_cost_o1_ex.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, C.c_int, C.c_int, C.c_double, _D, _D]
-        L.orc_train_ex.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_double, C.c_double, C.c_int, C.c_int, C.c_double, _D, _D]
+        L.orc_train_ex.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_double, C.c_double, C.c_int, C.c_int, C.c_double, _D, _D,
+                                   C.c_int]
         L.orc_symm_jvp.argtypes = [C.c_void_p, C.c_int, _L, _D, _I, _D, _D, _D, C.c_int]
         L.orc_lj.restype = C.c_double
         L.orc_lj.argtypes = [C.c_int, _D, _D, C.c_double, C.c_double, C.c_double, _D]
@@ -118,7 +119,8 @@ class Oracle:
             raise ValueError(f"activation {neuron} not supported")
         return float(a[0]), float(d[0]), float(d2[0])
 
-    def neighbors(self, x, R, rc):
+    def neighbors(self, x, R, rc, brute=False):
+        """(i, j, image, r, d) of one structure; brute=True forces the all-pairs search."""
         x = np.ascontiguousarray(x, np.float64)
         Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
         n = len(x)
@@ -126,7 +128,7 @@ class Oracle:
         while True:
             i = np.zeros(cap, np.int32); j = np.zeros(cap, np.int32); img = np.zeros(3 * cap, np.int32)
             r = np.zeros(3 * cap); d = np.zeros(cap)
-            k = self.L.orc_neighbors(n, _d(x), _d(Rc), rc, cap, _i(i), _i(j), _i(img), _d(r), _d(d))
+            k = self.L.orc_neighbors(n, _d(x), _d(Rc), rc, cap, _i(i), _i(j), _i(img), _d(r), _d(d), int(brute))
             if k >= 0:
                 return i[:k], j[:k], img[:3 * k].reshape(-1, 3), r[:3 * k].reshape(-1, 3), d[:k]
             cap = -k
@@ -222,7 +224,7 @@ class Potential:
             raise RuntimeError(self.o.err())
         return E, F, W, G, D
 
-    def train(self, offs, posn, types, cell, e_ref, f_ref, wE=1.0, wF=0.1, loss=1, norm=1, delta=1.0):
+    def train(self, offs, posn, types, cell, e_ref, f_ref, wE=1.0, wF=0.1, loss=1, norm=1, delta=1.0, nthreads=1):
         """Loss (L, L_E, L_F) and dL/dp; loss 1 MSE, 2 MAE, 3 HUBER, 4 ASINH; norm 0 IDENTITY,
         1 LINEAR, 2 SQRT, 3 CBRT, 4 LOG (the energy term)."""
         offs = np.ascontiguousarray(offs, np.int64)
@@ -231,7 +233,7 @@ class Potential:
         rc = self.L.orc_train_ex(self.p, len(offs) - 1, _l(offs), _d(np.ascontiguousarray(posn, np.float64)),
                                  _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
                                  _d(np.ascontiguousarray(e_ref, np.float64)), _d(np.ascontiguousarray(f_ref, np.float64)), wE, wF,
-                                 loss, norm, delta, _d(lossv), _d(g))
+                                 loss, norm, delta, _d(lossv), _d(g), int(nthreads))
         loss = lossv
         if rc != 0:
             raise RuntimeError(self.o.err())

@@ -93,21 +93,44 @@ def test_config1_argon(contexts, tmp_path):
     _compare(tc, simt, text, cases.W.config1())
 
 
-def test_too_wide_for_tensor_core_is_reported(contexts, tmp_path):
-    """128-wide networks do not fit the split BF16 image: mlp_backend=2 refuses them, auto uses SIMT."""
-    tc, _ = contexts
-    text = cases.W.config_potential_text(4)
-    with pytest.raises(AnnError):
-        tc.load_text(text)
-    auto = Context()
+def test_wide_networks_run_on_tensor_cores(contexts, tmp_path):
+    """The 96-128-128-1 tanh networks of the ternary precision study run on the tensor cores with
+    both operands split (one image of W per layer serves the forward GEMM as a K-major operand and
+    the backward GEMM as the MN-major W^T): within 1e-4 of FP64 per atom and the mixed bars."""
+    tc, simt = contexts
+    structs = cases.ternary_box(dims=(8, 8, 6))
+    offs, posn, types, cell = cases.batch(structs)
+    text = cases.config_potential(tc, 4, tmp_path, precondition_batch=(offs, posn, types, cell))
+    assert [tc.network_form(t) for t in range(3)] == [(2, 3)] * 3
+    _compare(tc, simt, text, structs)
+
+
+@pytest.mark.parametrize("split", [1, 2, 3])
+def test_operand_split_forms(gpu_lib, tmp_path, split):
+    """Each operand form (1: BF16 x BF16, 2: activations hi + lo, 3: both split) on the binary
+    networks: structure energies and forces within the mixed bars of FP64, and atom energies /
+    dE/dG within what the form's rounding allows (2^-8 relative per BF16 operand)."""
+    tc = Context(mlp_backend=2, tc_split=split)
     try:
-        auto.load_text(text)
-        offs, posn, types, cell = cases.batch(cases.ternary_box(dims=(6, 6, 4)))
-        E64, F64, _ = auto.compute(offs, posn, types, cell, precision=FP64)
-        E, F, _ = auto.compute(offs, posn, types, cell, precision=MIXED)
+        structs = cases.small_binary(n_struc=6, seed=13)
+        offs, posn, types, cell = cases.batch(structs)
+        cases.config_potential(tc, 2, tmp_path, precondition_batch=(offs, posn, types, cell))
+        assert [tc.network_form(t) for t in range(2)] == [(2, split)] * 2
+        E64, F64, _ = tc.compute(offs, posn, types, cell, precision=FP64)
+        e64, d64 = tc.atom_energies(), tc.dedg()
+        E, F, _ = tc.compute(offs, posn, types, cell, precision=MIXED)
+        e, d = tc.atom_energies(), tc.dedg()
         _mixed_bars(E, F, E64, F64, offs)
+        tol = {1: 2e-2, 2: 1e-2, 3: 1e-4}[split]
+        assert np.max(np.abs(d - d64)) < tol * max(np.max(np.abs(d64)), 1.0), "dE/dG"
+        assert np.max(np.abs(e - e64)) < tol, "atom energies"
     finally:
-        auto.close()
+        tc.close()
+
+
+def test_tc_split_validated(gpu_lib):
+    with pytest.raises(AnnError):
+        Context(tc_split=4)
 
 
 @pytest.mark.parametrize("groups", [1, 2, 4])

@@ -66,7 +66,7 @@ LAYOUT = r'''
 int main() {
     std::printf("ann_options size %zu\n", sizeof(ann_options));
     F(ann_options, device); F(ann_options, precision); F(ann_options, newton); F(ann_options, max_neighbors);
-    F(ann_options, use_graphs); F(ann_options, mlp_backend); F(ann_options, tc_groups);
+    F(ann_options, use_graphs); F(ann_options, mlp_backend); F(ann_options, tc_groups); F(ann_options, tc_split);
     std::printf("ann_tuning size %zu\n", sizeof(ann_tuning));
     F(ann_tuning, tc_groups); F(ann_tuning, bp_blocks_per_sm); F(ann_tuning, nbr_blocks_per_sm);
     F(ann_tuning, ms); F(ann_tuning, ms_default);

@@ -168,6 +168,20 @@ def test_training_gradient_fd(oracle, wE, wF):
         assert abs(fd - g[k]) <= 1e-6 * max(abs(fd), abs(g[k])) + 1e-7 * gscale, (k, fd, g[k])
 
 
+def test_training_gradient_threads(oracle):
+    """structures split over threads (block rule, thread sums added in order) give the one-thread
+    loss and gradient up to the order of the additions"""
+    pot = oracle.load_text(W.config_potential_text(3))
+    structs = cases.small_binary(n_struc=5, seed=12)
+    offs, posn, types, cell = pack_batch(structs)
+    Eref, Fref = W.lennard_jones(structs)
+    Fref = np.concatenate(Fref)
+    l1, g1 = pot.train(offs, posn, types, cell, Eref, Fref, 1.0, 0.1)
+    l3, g3 = pot.train(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, nthreads=3)
+    assert np.allclose(l3, l1, rtol=1e-13, atol=0)
+    assert np.abs(g3 - g1).max() <= 1e-13 * np.abs(g1).max()
+
+
 def test_energy_gradient_matches_error_cost_o1(oracle):
     """the energy term equals the reference trainer's energy gradient (nnptefr2.cpp:1321-1374,
     984-995): MSE loss, LINEAR normalisation, averaged over the batch"""
