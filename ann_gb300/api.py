@@ -64,6 +64,7 @@ _SIGS = {
     "ann_num_inputs": (C.c_int, [_V, C.c_int32, _I32]),
     "ann_num_params": (C.c_int, [_V, _I64]),
     "ann_network_form": (C.c_int, [_V, C.c_int32, _I32, _I32]),
+    "ann_set_wait_limit": (C.c_int, [_V, C.c_int32]),
     "ann_get_params": (C.c_int, [_V, _D, C.c_int64]),
     "ann_set_params": (C.c_int, [_V, _D, C.c_int64]),
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
@@ -253,6 +254,11 @@ class Context:
         v = C.c_double()
         self._ck(self.lib.ann_cutoff(self.h, C.byref(v)))
         return v.value
+
+    def set_wait_limit(self, polls: int = -1):
+        """ann_set_wait_limit: polls >= 0 makes the device waits give up after that many non-blocking
+        polls (0: at once; testing the timeout path); -1 restores the built-in bounds."""
+        self._ck(self.lib.ann_set_wait_limit(self.h, int(polls)))
 
     def network_form(self, t: int):
         """(backend, split) of the MIXED network pass for type t: backend 2 = tensor cores with

@@ -59,6 +59,22 @@ static __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t pha
                  : "=r"(ok) : "r"(smem_u32(bar)), "r"(phase) : "memory");
     return ok != 0;
 }
+static __device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t phase) {   // non-blocking poll
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+// the wait for a staged row: bounded by 2^24 potentially blocking polls, or (testing, polls > 0)
+// by polls - 1 non-blocking ones
+static __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, int polls) {
+    if (polls > 0) {
+        for (int it = 1; it < polls; ++it) if (mbar_test_wait(bar, phase)) return true;
+        return false;
+    }
+    for (int it = 0; it < (1 << 24); ++it) if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
 static __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // ---------------------------------------------------------------- warp reductions
@@ -481,9 +497,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
         nx_b = cb ^ 1;
         nx_issued = stage_row(nx_i, nx_b);
         if (issued) {
-            bool done = false;
-            for (int it = 0; it < (1 << 24) && !done; ++it) done = mbar_try_wait(&w.bar[cb], (phase >> cb) & 1u);
-            if (!__all_sync(0xffffffffu, done)) {  // bounded wait gave up: report, drain (bounded), stop
+            const bool done = mbar_wait_bounded(&w.bar[cb], (phase >> cb) & 1u, a.wait_polls);
+            if (!__all_sync(0xffffffffu, done)) {  // bounded wait gave up: report, drain (full bound), stop
                 if (lane == 0) atomicOr(a.status, (int)ST_TIMEOUT);
                 for (int it = 0; it < (1 << 24); ++it) if (mbar_try_wait(&w.bar[cb], (phase >> cb) & 1u)) break;
                 if (nx_issued)

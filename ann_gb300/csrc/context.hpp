@@ -175,6 +175,7 @@ struct ann_ctx {
     bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
     int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
     int nsm = 1;                    // streaming multiprocessors of the device (persistent grids)
+    int32_t wait_polls = 0;         // kernel argument of ann_set_wait_limit: 0 built-in bounds, k > 0 at most k - 1 polls
     int32_t* status_h = nullptr;    // page-locked copy of the status word
     // launch shapes chosen by ann_autotune / ann_set_tuning (0: the built-in rule)
     int32_t tune_tc[MAXT] = {0, 0, 0, 0};
@@ -214,6 +215,7 @@ inline BpArgs<real> bp_args(ann_ctx* c) {
     b.counter = c->counter.as<uint32_t>(); b.status = c->status.as<int32_t>();
     b.grid_per_sm = c->tune_bp;
     b.nsm = c->nsm;
+    b.wait_polls = c->wait_polls;
     return b;
 }
 
@@ -231,7 +233,7 @@ inline void enqueue_networks(ann_ctx* c, int natoms, DevBuf& G, DevBuf& dEdG, De
             ta.natoms = natoms; ta.imax = pot.imax; ta.type = ty;
             ta.tstart = tstart.as<int32_t>(); ta.tlist = tlist.as<int32_t>();
             ta.G = G.as<float>(); ta.dEdG = dEdG.as<float>(); ta.Eatom = Eatom.as<double>();
-            ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>();
+            ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>(); ta.wait_polls = c->wait_polls;
             launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->nsm, c->stream);
         }
     } else {

@@ -79,6 +79,8 @@ struct BpArgs {
     int32_t* status;
     int32_t grid_per_sm;             // host side: cap on resident blocks per SM (0: as many as fit)
     int32_t nsm;                     // host side: streaming multiprocessors of the device
+    int32_t wait_polls;              // k > 0: a neighbour-row wait gives up after k - 1 non-blocking
+                                     // polls (testing the timeout path); 0: the built-in bound
 };
 template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_force(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);

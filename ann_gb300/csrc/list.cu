@@ -20,7 +20,7 @@ static void enqueue_list(ann_ctx* c, int nrows, int nall, int cap, int nchunks, 
     b.G = c->lG.as<real>(); b.dEdG = c->ldEdG.as<real>(); b.F = c->lF.as<real>(); b.W = c->lW.as<real>();
     b.self = have_ilist ? c->lilist.as<int32_t>() : nullptr;
     b.counter = c->counter.as<uint32_t>(); b.status = c->status.as<int32_t>();
-    b.nsm = c->nsm;
+    b.nsm = c->nsm; b.wait_polls = c->wait_polls;
     b.prm = params_of<real>(c->pf, c->pd);
     launch_symm<real>(pot, b, st);
     enqueue_networks<real>(c, nrows, c->lG, c->ldEdG, c->lEatom, c->ltstart, c->ltlist, b.prm);

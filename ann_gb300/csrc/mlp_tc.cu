@@ -43,7 +43,19 @@ static __device__ __forceinline__ bool tc_try_wait(uint64_t* bar, uint32_t phase
                  : "=r"(ok) : "r"(su32(bar)), "r"(phase) : "memory");
     return ok != 0;
 }
-static __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t phase) {
+static __device__ __forceinline__ bool tc_test_wait(uint64_t* bar, uint32_t phase) {   // non-blocking poll
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(su32(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+// bounded by 2^22 potentially blocking polls, or (polls > 0, testing the timeout path) by
+// polls - 1 non-blocking ones; the drains after a timeout always take the full bound
+static __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t phase, int polls = 0) {
+    if (polls > 0) {
+        for (int it = 1; it < polls; ++it) if (tc_test_wait(bar, phase)) return true;
+        return false;
+    }
     for (int it = 0; it < (1 << 22); ++it) if (tc_try_wait(bar, phase)) return true;
     return false;
 }
@@ -174,7 +186,7 @@ __global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constan
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)), "r"((uint32_t)tt.tmem_cols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    bool good = tc_wait(&bar[0], 0);
+    bool good = tc_wait(&bar[0], 0, a.wait_polls);
     tc_fence_before();
     good = __syncthreads_and(good);
     const bool image_ok = good;
@@ -213,7 +225,7 @@ __global__ void __launch_bounds__(TC_M * G, 4 / G) k_mlp_tc(const __grid_constan
             }
             tc_commit(&bar[1]);
         }
-        const bool ok = __syncthreads_and(tc_wait(&bar[1], mphase));
+        const bool ok = __syncthreads_and(tc_wait(&bar[1], mphase, a.wait_polls));
         tc_fence_after();
         if (ok) mphase ^= 1u;
         else mma_pending = true;

@@ -90,6 +90,8 @@ struct TcArgs {
     double* Eatom;                   // [N]
     const uint8_t* image;            // device copy of TcPlan::image
     int32_t* status;
+    int32_t wait_polls;              // k > 0: image and MMA waits give up after k - 1 non-blocking
+                                     // polls (testing the timeout path); 0: the built-in bound
 };
 // est_atoms: the expected atoms of the type (its count is known on the device only); groups:
 // 1, 2 or 4 to force the split, 0 to choose it (tc_groups)

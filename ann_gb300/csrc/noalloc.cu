@@ -65,7 +65,7 @@ int ann_network_noalloc(ann_ctx* c, int32_t natoms, const int32_t* type_dev, con
                 ta.natoms = natoms; ta.imax = pot.imax; ta.type = ty;
                 ta.tstart = tstart; ta.tlist = tlist;
                 ta.G = static_cast<const float*>(G_dev); ta.dEdG = static_cast<float*>(dEdG_dev); ta.Eatom = Eatom_dev;
-                ta.image = c->tcimg.as<uint8_t>(); ta.status = status;
+                ta.image = c->tcimg.as<uint8_t>(); ta.status = status; ta.wait_polls = c->wait_polls;
                 launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->nsm, st);
             }
         } else if (fp64) {

@@ -67,6 +67,14 @@ static double time_batch(ann_ctx* c, int prec, int reps) {
 
 extern "C" {
 
+int ann_set_wait_limit(ann_ctx* c, int32_t polls) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (polls < -1 || polls > (1 << 24)) return fail(c, ANN_ERR_ARG, "polls must be -1 (built-in bounds) or in [0, 2^24]");
+    c->wait_polls = polls < 0 ? 0 : polls + 1;
+    drop_graphs(c);   // the limit is a kernel argument of the captured launches
+    return ANN_OK;
+}
+
 int ann_set_tuning(ann_ctx* c, const ann_tuning* t) {
     if (!c || !t) return fail(c, ANN_ERR_ARG, "NULL argument");
     ANN_TRY(c, {

@@ -326,6 +326,15 @@ typedef struct ann_tuning {
     double ms_default;             /* ann_autotune: one evaluation with every field 0 (ms)           */
 } ann_tuning;
 int ann_autotune(ann_ctx* ctx, int32_t precision, int32_t reps, ann_tuning* out);
+
+/* ---- bounded device waits (testing aid; no counterpart in the reference) -----------------------
+ * Every device-side wait (a staged neighbour row, a network weight image, a tensor-core MMA) gives
+ * up after a bounded number of polls, reports ANN_ERR_TIMEOUT, lets its copies and MMAs finish
+ * (with the full bound) and returns, so the context stays usable. polls >= 0 makes those waits
+ * give up after that many non-blocking polls (0: at once, every time), which exercises the
+ * timeout path without a fault or a hang; -1 (the default) restores the built-in bounds. The
+ * launch graphs are recaptured on the next call.                                                  */
+int ann_set_wait_limit(ann_ctx* ctx, int32_t polls);
 int ann_set_tuning(ann_ctx* ctx, const ann_tuning* t);
 
 #ifdef __cplusplus

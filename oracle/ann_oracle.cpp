@@ -1154,6 +1154,7 @@ int orc_ntypes(void* p) { return ((NNP*)p)->ntypes(); }
 double orc_rc(void* p) { return ((NNP*)p)->rc; }
 int orc_ninput(void* p, int t) { return ((NNP*)p)->h[t].nInput; }
 int orc_nparams(void* p) { return ((NNP*)p)->nparams(); }
+int orc_nn_size(void* p, int t) { return ((NNP*)p)->h[t].nn.size(); }
 int orc_type_index(void* p, const char* name) { auto& m = ((NNP*)p)->index; auto it = m.find(name); return it == m.end() ? -1 : it->second; }
 void orc_get_params(void* p, double* out) { int c = 0; for (auto& h : ((NNP*)p)->h) { h.nn.pack(out + c); c += h.nn.size(); } }
 void orc_set_params(void* p, const double* in) { int c = 0; for (auto& h : ((NNP*)p)->h) { h.nn.unpack(in + c); c += h.nn.size(); } }
@@ -1161,6 +1162,37 @@ void orc_set_params(void* p, const double* in) { int c = 0; for (auto& h : ((NNP
 int orc_activate(int neuron, double c, double z, double* a, double* d, double* d2) {
     try { activate(neuron, c, z, *a, *d, *d2); return 0; } catch (std::exception& e) { return -1; }
 }
+// One network of a loaded potential on one input, for pinning against the reference's own network
+// code (ANN::fpbp2 + DODZ::grad + Cost::grad + D2ODZDI::grad, nn.cpp:1391-1409, 1712-2100):
+// out = the network output (without the vacuum energy), dodi = dO/dI (nin), grad = dO/dp in the
+// packing order (P), d2odpdi = d2O/(dp dI) (P x nin, row-major; NULL: skipped), the latter by the
+// forward-over-reverse pass with unit tangents.
+int orc_nn_eval(void* pp, int type, const double* inp, double* out, double* dodi, double* grad, double* d2odpdi) {
+    try {
+        NNP& p = *(NNP*)pp;
+        if (type < 0 || type >= p.ntypes()) throw std::invalid_argument("invalid type index");
+        ANN& nn = p.h[type].nn;
+        const int nin = nn.nin, P = nn.size();
+        *out = nn.forward(inp);
+        std::vector<double> d;
+        nn.dodi(d);
+        for (int m = 0; m < nin; ++m) dodi[m] = d[m];
+        for (int k = 0; k < P; ++k) grad[k] = 0;
+        nn.cost_grad(1.0, grad);
+        if (d2odpdi) {
+            std::vector<double> u(nin, 0.0), g(P);
+            for (int m = 0; m < nin; ++m) {
+                u[m] = 1.0;
+                std::fill(g.begin(), g.end(), 0.0);
+                nn.jvp_grad(u.data(), 0.0, 1.0, g.data());
+                for (int k = 0; k < P; ++k) d2odpdi[(size_t)k * nin + m] = g[k];
+                u[m] = 0.0;
+            }
+        }
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
 double orc_fmexp(double x) { return fmexp(x); }
 double orc_coscut(double x) { return coscut(x); }
 double orc_sincut(double x) { return sincut(x); }

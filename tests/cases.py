@@ -123,6 +123,26 @@ def activation_potential_text(neuron: str, c: float = 1.3, seed: int = 5) -> str
     return "\n".join(out) + "\n"
 
 
+def single_network_text(nin, nodes, neuron, c, inpw, inpb, outw, outb):
+    """A one-type potential whose network has nin inputs (nin - 8 radial functions and 8 angular
+    ones), the given hidden / output widths, activation (name) with scale c, and input / output
+    scaling written with 17 significant digits (read back exactly)."""
+    text = W.potential_text(["A"], 6.0, nin - 8, [0.01], list(nodes), neuron)
+    text = text.replace(f"neuron {neuron} 1.000000", f"neuron {neuron} {c:.17g}")
+    out = []
+    for line in text.splitlines():
+        if line.startswith("inpw "):
+            line = "inpw " + " ".join(f"{v:.17g}" for v in inpw)
+        elif line.startswith("inpb "):
+            line = "inpb " + " ".join(f"{v:.17g}" for v in inpb)
+        elif line.startswith("outw "):
+            line = f"outw {outw:.17g}"
+        elif line.startswith("outb "):
+            line = f"outb {outb:.17g}"
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
 def config_potential(ctx, cfg, tmp_path, precondition_batch=None):
     """Initialise the configuration potential in ctx, round-trip it through the 'ann' text format
     (what both sides read) and return that text."""

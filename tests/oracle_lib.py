@@ -17,6 +17,7 @@ ROOT = Path(__file__).resolve().parents[1]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_SO = ORACLE_DIR / "_build" / "libann_oracle.so"
 REF_SO = ORACLE_DIR / "_ref" / "libref_basis.so"
+REF_NN_SO = ORACLE_DIR / "_ref" / "libref_nn.so"
 ORACLE_TIMED_SO = ORACLE_DIR / "_build" / "libann_oracle_timed.so"
 
 
@@ -81,6 +82,8 @@ class Oracle:
             getattr(L, f).argtypes = [C.c_double]
         L.orc_cutoff.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D]
         L.orc_activate.argtypes = [C.c_int, C.c_double, C.c_double, _D, _D, _D]
+        L.orc_nn_eval.argtypes = [C.c_void_p, C.c_int, _D, _D, _D, _D, _D]
+        L.orc_nn_size.argtypes = [C.c_void_p, C.c_int]
         L.orc_basisR.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, C.c_double, _D, _D, _D, _D]
         L.orc_basisA.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, _D, _D, _I, C.c_double, C.c_double, C.c_double, _D, _D, _D, _D, _D]
         L.orc_neighbors.restype = C.c_longlong
@@ -251,6 +254,10 @@ class Potential:
             raise RuntimeError(self.o.err())
         return loss[0], g
 
+    def nn_eval(self, t, inp, d2=True):
+        """(out, dO/dI, dO/dp, d2O/(dp dI)) of type t's network on one input (no vacuum energy)."""
+        return nn_eval(self.L, "orc_nn_eval", self.p, self.ninput(t), self.L.orc_nn_size(self.p, t), inp, d2, t)
+
     def md_step(self, x, v, types, R, masses, dt, F):
         pe, ke = C.c_double(), C.c_double()
         Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
@@ -259,6 +266,49 @@ class Potential:
         if rc != 0:
             raise RuntimeError(self.o.err())
         return pe.value, ke.value
+
+
+def nn_eval(lib, fn, handle, nin, nparams, inp, d2=True, *pre):
+    """(out, dO/dI, dO/dp, d2O/(dp dI) or None) of one network evaluation through the oracle
+    (fn = "orc_nn_eval", pre = (type,)) or the reference build (fn = "ref_nn_eval")."""
+    out = np.zeros(1); dodi = np.zeros(nin); g = np.zeros(nparams)
+    d2o = np.zeros((nparams, nin)) if d2 else None
+    rc = getattr(lib, fn)(handle, *pre, _d(np.ascontiguousarray(inp, np.float64)), _d(out), _d(dodi), _d(g), _d(d2o))
+    if rc != 0:
+        raise RuntimeError(f"{fn} failed")
+    return out[0], dodi, g, d2o
+
+
+class RefNN:
+    """The reference's own network code (ml/nn.cpp compiled with the plain-loop Eigen stand-in)."""
+
+    def __init__(self):
+        if not REF_NN_SO.exists():
+            if not REF_SRC.exists():
+                raise FileNotFoundError("reference sources not available")
+            build_oracle(ref=True)
+        L = self.L = C.CDLL(str(REF_NN_SO))
+        L.ref_nn_create.restype = C.c_void_p
+        L.ref_nn_create.argtypes = [C.c_int, C.c_int, _I, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
+        L.ref_nn_free.argtypes = [C.c_void_p]
+        L.ref_nn_size.argtypes = [C.c_void_p]
+        L.ref_nn_get_params.argtypes = [C.c_void_p, _D]
+        L.ref_nn_set_params.argtypes = [C.c_void_p, _D]
+        L.ref_nn_set_scaling.argtypes = [C.c_void_p, _D, _D, C.c_double, C.c_double]
+        L.ref_nn_eval.argtypes = [C.c_void_p, _D, _D, _D, _D, _D]
+        L.ref_nn_last_error.restype = C.c_char_p
+
+    def create(self, nin, nodes, neuron, c=1.0, init=4, seed=1, sigma_b=0.001, sigma_w=1.0, dist=1):
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        h = self.L.ref_nn_create(nin, len(nodes), _i(nodes), neuron, c, init, seed, sigma_b, sigma_w, dist)
+        if not h:
+            raise RuntimeError(self.L.ref_nn_last_error().decode())
+        return h
+
+    def params(self, h):
+        v = np.zeros(self.L.ref_nn_size(h))
+        self.L.ref_nn_get_params(h, _d(v))
+        return v
 
 
 class RefBasis:
