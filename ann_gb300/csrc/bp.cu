@@ -38,6 +38,13 @@ namespace ann {
 
 enum { PASS_SYMM = 0, PASS_FORCE = 1, PASS_JVP = 2 };
 constexpr int BP_WARPS = 4;
+#ifndef ANN_BP_MIN_BLOCKS
+#define ANN_BP_MIN_BLOCKS 5         // resident blocks per SM the symmetry / tangent passes are bounded for
+#endif
+#ifndef ANN_BP_MIN_BLOCKS_FORCE
+#define ANN_BP_MIN_BLOCKS_FORCE 4   // the force pass (122 registers without spills; at 5: spills)
+#endif
+constexpr int bp_min_blocks(int pass) { return pass == PASS_FORCE ? ANN_BP_MIN_BLOCKS_FORCE : ANN_BP_MIN_BLOCKS; }
 constexpr int CHUNK = 16;   // functions per register chunk (radial and generic angular)
 
 // ---------------------------------------------------------------- PTX helpers (bulk copy + mbarrier)
@@ -157,10 +164,11 @@ struct WarpMem {
     static __host__ __device__ size_t layout(int cap, int imax, WarpMem* w, unsigned char* base) {
         size_t off = 0;
         auto take = [&](size_t bytes, size_t al) { off = align(off, al); const size_t o = off; off += bytes; return o; };
-        const size_t o_geo = take(sizeof(R4) * cap, 32);
-        const size_t o_stage = take(sizeof(R4) * cap, 32);
-        const size_t o_tg = (PASS == PASS_JVP) ? take(sizeof(R4) * cap, 32) : 0;
-        const size_t o_dp = take(sizeof(real) * NDP * cap, 16);
+        // geo / stage / tg / dp hold cap records plus a zero record at index cap (see force_task)
+        const size_t o_geo = take(sizeof(R4) * (cap + 1), 32);
+        const size_t o_stage = take(sizeof(R4) * (cap + 1), 32);
+        const size_t o_tg = (PASS == PASS_JVP) ? take(sizeof(R4) * (cap + 1), 32) : 0;
+        const size_t o_dp = take(sizeof(real) * NDP * (cap + 1), 16);
         const size_t o_d = take(sizeof(real) * cap, 16), o_fc = take(sizeof(real) * cap, 16), o_fcg = take(sizeof(real) * cap, 16);
         size_t o_ax = 0, o_ay = 0, o_az = 0, o_dE = 0;
         if (PASS == PASS_FORCE) {
@@ -315,16 +323,20 @@ __device__ __forceinline__ void angular_poly(const real* dE, const int32_t* slot
 // scalar and bk times the sender's unit vector (read from shared memory) to its vector. Each
 // owner adds its totals to the element's shared-memory accumulator once per task. No atomics;
 // every unordered pair is evaluated once.
+// A slot without a partner (a lane beyond the chunk, a rectangle partner beyond the shorter chunk,
+// the second visit of a pair in the last step of an even triangle) reads the zero record at index
+// `zr`: D = D' = 0 and a zero unit vector make every term of the triplet exactly zero, so the loop
+// carries no per-step masking of its results. Lanes beyond the owning chunk own the zero record.
 template <typename real, int NG, int PASS, bool TRI>
 __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&al)[NG][9], int lane,
-                                           int p0, int np, int q0, int nq) {
+                                           int p0, int np, int q0, int nq, int zr) {
     typedef typename V4<real>::T R4;
     constexpr int NDP = 2 * NG;
     const bool ownP = lane < np, ownQ = !TRI && lane < nq;
-    R4 ga;
+    const int ea = ownP ? p0 + lane : zr;
+    const R4 ga = w.geo[ea];
     DampRec<real, NG> da;
-    if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
-    else { ga.x = ga.y = ga.z = ga.w = real(0); da.zero(); }
+    da.load(w.dp + ea * NDP);
     real ca = real(0), cb = real(0);                                       // along the owned unit vectors
     real sa[3] = {real(0), real(0), real(0)}, sb[3] = {real(0), real(0), real(0)};
     constexpr bool PACKED = std::is_same<real, float>::value && NG == 2;
@@ -340,18 +352,20 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     if (part >= n) part -= n;
     int src = TRI ? lane - 1 : lane;          // sending lane (lane - step) mod n
     if (src < 0) src += n;
+    if (src >= n) src = 0;                    // lanes beyond the chunk: any element of it
+    const int last_half = (TRI && (n & 1) == 0) ? steps : -1;   // even triangle: the last step visits pairs twice
 #pragma unroll 1
     for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
-        const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
-        const int e = qb + (valid ? part : 0);
+        // non-owning lanes always read the zero record (their partner slot may lie outside the chunk)
+        const bool valid = ownP && (TRI ? (st != last_half || lane < steps) : part < nq);
+        const int e = valid ? qb + part : zr;
         const R4 gb = w.geo[e];
         DampRec<real, NG> db;
         db.load(w.dp + e * NDP);
-        const R4 gs = w.geo[p0 + (src < n ? src : 0)];     // the sending lane's own element
+        const R4 gs = w.geo[p0 + src];                     // the sending lane's own element
         real cj, bj, ck, bk;
         if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, cj, bj, ck, bk);
         else triplet_force<real, NG>(ga, da, gb, db, al, cj, bj, ck, bk);
-        if (!valid) { cj = real(0); bj = real(0); ck = real(0); bk = real(0); }
         ca += cj;
         sa[0] += bj * gb.x; sa[1] += bj * gb.y; sa[2] += bj * gb.z;
         const real rc = __shfl_sync(0xffffffffu, ck, src & 31);
@@ -373,19 +387,21 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
 // The same chunk tasks for the symmetry functions of a fast-path block: the lane's own neighbour
 // stays in registers and only the partner's record is read per pair; acc[s] collects slot s.
 template <typename real, int NG, int S, int PASS, bool TRI>
-__device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real (&acc)[S], int lane, int p0, int np, int q0, int nq) {
+__device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real (&acc)[S], int lane, int p0, int np, int q0, int nq,
+                                          int zr) {
     typedef typename V4<real>::T R4;
     constexpr int NDP = 2 * NG;
     const bool ownP = lane < np;
-    R4 ga;
+    const int ea = ownP ? p0 + lane : zr;     // lanes beyond the chunk own the zero record
+    const R4 ga = w.geo[ea];
     DampRec<real, NG> da;
-    if (ownP) { ga = w.geo[p0 + lane]; da.load(w.dp + (p0 + lane) * NDP); }
-    else { ga.x = ga.y = ga.z = ga.w = real(0); da.zero(); }
+    da.load(w.dp + ea * NDP);
     const int n = np;
     const int steps = TRI ? np / 2 : np;
     const int qb = TRI ? p0 : q0;
     int part = TRI ? lane + 1 : lane;
     if (part >= n) part -= n;
+    const int last_half = (TRI && (n & 1) == 0) ? steps : -1;
     if constexpr (std::is_same<real, float>::value && NG <= 2) {
         // FP32: the slot pair (lambda = +1, lambda = -1) of each zeta in one packed register,
         // (|1/2 + cos/2|^zeta, |1/2 - cos/2|^zeta) by packed squaring, accumulated by packed FMA
@@ -394,8 +410,8 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
         for (int k = 0; k < S / 2; ++k) acc2[k] = pk2(acc[2 * k], acc[2 * k + 1]);
 #pragma unroll 2   // two independent triplets per iteration
         for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
-            const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
-            const int e = qb + (valid ? part : 0);
+            const bool valid = ownP && (TRI ? (st != last_half || lane < steps) : part < nq);
+            const int e = valid ? qb + part : zr;
             const R4 gb = w.geo[e];
             DampRec<real, NG> db;
             db.load(w.dp + e * NDP);
@@ -405,7 +421,7 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
             pw[1] = mul2(pw[0], pw[0]); pw[2] = mul2(pw[1], pw[1]); pw[3] = mul2(pw[2], pw[2]);
 #pragma unroll
             for (int g = 0; g < NG; ++g) {
-                const float DD = valid ? da.D(g) * db.D(g) : 0.0f;
+                const float DD = da.D(g) * db.D(g);          // zero for the zero record
                 const uint64_t D2 = pk2(DD, DD);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) acc2[g * 4 + q] = fma2(pw[q], D2, acc2[g * 4 + q]);
@@ -421,8 +437,8 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
     } else {
 #pragma unroll 2   // two independent triplets per iteration
     for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
-        const bool valid = ownP && (TRI ? (2 * st < n || lane < steps) : part < nq);
-        const int e = qb + (valid ? part : 0);
+        const bool valid = ownP && (TRI ? (st != last_half || lane < steps) : part < nq);
+        const int e = valid ? qb + part : zr;
         const R4 gb = w.geo[e];
         DampRec<real, NG> db;
         db.load(w.dp + e * NDP);
@@ -433,7 +449,7 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
         pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
-            const real DD = valid ? da.D(g) * db.D(g) : real(0);
+            const real DD = da.D(g) * db.D(g);
 #pragma unroll
             for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
         }
@@ -442,9 +458,35 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
     }
 }
 
+// per-type neighbour ranges of the current atom (at most MAXT = 4): held in registers and read by
+// selects (symmetry-function and tangent passes), or as a small array (force pass, whose register
+// budget goes to the triplet loop; measured 0.650 vs 0.664 ms on the 74,710-atom batch)
+struct TypeRangesReg {
+    int v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    __device__ __forceinline__ int get(int t) const { return t == 0 ? v0 : t == 1 ? v1 : t == 2 ? v2 : v3; }
+    __device__ __forceinline__ void set(int t, int x) { v0 = t == 0 ? x : v0; v1 = t == 1 ? x : v1; v2 = t == 2 ? x : v2; v3 = t == 3 ? x : v3; }
+};
+struct TypeRangesArr {
+    int v[4];
+    __device__ __forceinline__ int get(int t) const { return v[t]; }
+    __device__ __forceinline__ void set(int t, int x) { v[t] = x; }
+};
+static_assert(MAXT == 4, "the type ranges hold four types");
+
+// Shared table of a fast-path force block: the potential's radial parameters (eta, rs) and the
+// slot map of the angular blocks, copied once per block so that the force pass's radial loop
+// (per neighbour, every function of the block) and coefficient set-up read them from shared
+// memory rather than global memory (0.656 -> 0.650 ms; the symmetry pass, which reads each
+// parameter once per lane, gains nothing and keeps global loads)
+template <typename real>
+__host__ __device__ inline size_t bp_table_bytes(const DevPot& pot) {   // force pass, fast path
+    const size_t r = ((size_t)2 * pot.nrad * sizeof(real) + 15) / 16 * 16;
+    return r + ((size_t)pot.nslot * sizeof(int32_t) + 15) / 16 * 16;
+}
+
 // ---------------------------------------------------------------- the kernel
 template <typename real, int NG, bool FAST, int PASS>
-__global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
+__global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS)) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
     typedef typename V4<real>::T R4;
     extern __shared__ __align__(128) unsigned char bsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -453,7 +495,27 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
     WarpMem<real, NG, PASS> w;
     WarpMem<real, NG, PASS>::layout(cap, imax, &w, bsm + (size_t)wid * wbytes);
     constexpr int NDP = 2 * NG;
+    // force pass, fast path: radial parameters and slot map in shared memory (after the warps' regions)
+    const real* t_reta = a.prm.reta;
+    const real* t_rs = a.prm.rs;
+    const int32_t* t_slot = a.prm.slot2ref;
+    if constexpr (FAST && PASS == PASS_FORCE) {
+        real* s_reta = reinterpret_cast<real*>(bsm + (size_t)BP_WARPS * wbytes);
+        real* s_rs = s_reta + pot.nrad;
+        int32_t* s_slot = reinterpret_cast<int32_t*>(bsm + (size_t)BP_WARPS * wbytes + ((size_t)2 * pot.nrad * sizeof(real) + 15) / 16 * 16);
+        for (int k = threadIdx.x; k < pot.nrad; k += blockDim.x) { s_reta[k] = a.prm.reta[k]; s_rs[k] = a.prm.rs[k]; }
+        for (int k = threadIdx.x; k < pot.nslot; k += blockDim.x) s_slot[k] = a.prm.slot2ref[k];
+        __syncthreads();
+        t_reta = s_reta; t_rs = s_rs; t_slot = s_slot;
+    }
     if (lane == 0) { mbar_init(&w.bar[0], 1); mbar_init(&w.bar[1], 1); }
+    // the zero record (index cap) of both staging buffers and of the damping records: a partner
+    // slot outside a chunk task reads it and contributes exactly zero
+    if (lane < 4) {
+        reinterpret_cast<real*>(&w.geo[cap])[lane] = real(0);
+        reinterpret_cast<real*>(&w.stage[cap])[lane] = real(0);
+    }
+    if (lane < NDP) w.dp[(size_t)cap * NDP + lane] = real(0);
     __syncwarp();
     uint32_t phase = 0;   // bit b: parity of the next phase of barrier b
     const unsigned lt = (1u << lane) - 1u;
@@ -519,11 +581,11 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
         real ie2[NG];
 #pragma unroll
         for (int q = 0; q < NG; ++q) ie2[q] = (real)TT.ietar2[q];
-        int tstart[MAXT], tcnt[MAXT];
+        typename std::conditional<PASS == PASS_FORCE, TypeRangesArr, TypeRangesReg>::type tstart, tcnt;
         int pos = 0, base_in = 0;
         for (int t = 0; t < T; ++t) {
             const int cin = a.ntc[(size_t)i * T + t];
-            tstart[t] = pos;
+            tstart.set(t, pos);
             for (int e0 = 0; e0 < cin; e0 += 32) {
                 const int e = base_in + e0 + lane;
                 bool keep = false;
@@ -563,7 +625,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                 }
                 pos += __popc(msk);
             }
-            tcnt[t] = pos - tstart[t];
+            tcnt.set(t, pos - tstart.get(t));
             base_in += cin;
         }
         if (PASS == PASS_FORCE) {
@@ -583,7 +645,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
             for (int J = 0; J < T; ++J) {
                 const DevRadial& R = TT.R[J];
                 if (R.n == 0) continue;
-                const int e0 = tstart[J], e1 = e0 + tcnt[J];
+                const int e0 = tstart.get(J), e1 = e0 + tcnt.get(J);
                 auto block = [&](auto form) {
                     constexpr int NAME = decltype(form)::value;
                     for (int e = e0 + lane; e < e1; e += 32) {
@@ -592,7 +654,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
 #pragma unroll 4
                         for (int m = 0; m < R.n; ++m) {
                             real val, der;
-                            radial_vd_t<NAME, real>(R.name, __ldg(a.prm.reta + R.pidx + m), __ldg(a.prm.rs + R.pidx + m), dd, f, g, val, der);
+                            radial_vd_t<NAME, real>(R.name, t_reta[R.pidx + m], t_rs[R.pidx + m], dd, f, g, val, der);
                             amp -= w.dE[R.off + m] * der;
                         }
                         const R4 g4 = w.geo[e];
@@ -611,10 +673,9 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                 for (int t = 0; t < MAXT; ++t) {      // the lane's block, with constant indices only
                     if (t < T && J == t && m >= TT.R[t].n) { m -= TT.R[t].n; J = t + 1; }
                 }
-#pragma unroll
-                for (int t = 0; t < MAXT; ++t) if (t == J) { e0 = tstart[t]; ne = tcnt[t]; }
+                e0 = tstart.get(J); ne = tcnt.get(J);
                 const DevRadial& R = TT.R[J];
-                const real eta = a.prm.reta[R.pidx + m], rs = a.prm.rs[R.pidx + m];
+                const real eta = t_reta[R.pidx + m], rs = t_rs[R.pidx + m];
                 real acc = real(0);
                 auto block = [&](auto form) {
                     constexpr int NAME = decltype(form)::value;
@@ -637,7 +698,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                 const int blk = tri_index(J, K);
                 const DevAngular& A = TT.A[blk];
                 if (A.n == 0) continue;
-                const int nJ = tcnt[J], nK = tcnt[K], aJ = tstart[J], aK = tstart[K];
+                const int nJ = tcnt.get(J), nK = tcnt.get(K), aJ = tstart.get(J), aK = tstart.get(K);
                 const int total = (J == K) ? nJ * (nJ - 1) / 2 : nJ * nK;
                 constexpr bool ROWS = (PASS != PASS_FORCE);
                 if (FAST) {
@@ -648,31 +709,44 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                     if (PASS != PASS_JVP) {
                         // chunk tasks: triangles of each chunk, rectangles of chunk pairs (larger first)
                         real al[NG][9];
-                        if (PASS == PASS_FORCE) angular_poly<real, NG>(w.dE + A.off, a.prm.slot2ref, A.sidx, al);
+                        if (PASS == PASS_FORCE) angular_poly<real, NG>(w.dE + A.off, t_slot, A.sidx, al);
                         auto task = [&](int p0, int np, int q0, int nq, bool tri) {
                             if (PASS == PASS_FORCE) {
-                                if (tri) force_task<real, NG, PASS, true>(w, al, lane, p0, np, q0, nq);
-                                else force_task<real, NG, PASS, false>(w, al, lane, p0, np, q0, nq);
+                                if (tri) force_task<real, NG, PASS, true>(w, al, lane, p0, np, q0, nq, cap);
+                                else force_task<real, NG, PASS, false>(w, al, lane, p0, np, q0, nq, cap);
                             } else {
-                                if (tri) symm_task<real, NG, S, PASS, true>(w, acc, lane, p0, np, q0, nq);
-                                else symm_task<real, NG, S, PASS, false>(w, acc, lane, p0, np, q0, nq);
+                                if (tri) symm_task<real, NG, S, PASS, true>(w, acc, lane, p0, np, q0, nq, cap);
+                                else symm_task<real, NG, S, PASS, false>(w, acc, lane, p0, np, q0, nq, cap);
                             }
                         };
+                        // a range of n neighbours in ceil(n / 32) chunks of nearly equal size: a
+                        // rectangle task of chunks P x Q takes max(|P|, |Q|) steps, so an even split
+                        // (35 -> 18 + 17, not 32 + 3) keeps its lanes busy
+                        auto chunk = [](int n, int c, int& c0, int& cn) {
+                            const int k = (n + 31) >> 5, base = n / k, rem = n - base * k;
+                            c0 = c * base + min(c, rem);
+                            cn = base + (c < rem ? 1 : 0);
+                        };
+                        const int kJ = (nJ + 31) >> 5, kK = (nK + 31) >> 5;
                         if (J == K) {
-                            for (int c0 = 0; c0 < nJ; c0 += 32) {
-                                const int n0 = min(32, nJ - c0);
+                            for (int ca = 0; ca < kJ; ++ca) {
+                                int c0, n0;
+                                chunk(nJ, ca, c0, n0);
                                 task(aJ + c0, n0, 0, 0, true);
-                                for (int c1 = c0 + 32; c1 < nJ; c1 += 32) {
-                                    const int n1 = min(32, nJ - c1);
+                                for (int cb = ca + 1; cb < kJ; ++cb) {
+                                    int c1, n1;
+                                    chunk(nJ, cb, c1, n1);
                                     if (n0 >= n1) task(aJ + c0, n0, aJ + c1, n1, false);
                                     else task(aJ + c1, n1, aJ + c0, n0, false);
                                 }
                             }
                         } else {
-                            for (int c0 = 0; c0 < nJ; c0 += 32) {
-                                const int n0 = min(32, nJ - c0);
-                                for (int c1 = 0; c1 < nK; c1 += 32) {
-                                    const int n1 = min(32, nK - c1);
+                            for (int ca = 0; ca < kJ; ++ca) {
+                                int c0, n0;
+                                chunk(nJ, ca, c0, n0);
+                                for (int cb = 0; cb < kK; ++cb) {
+                                    int c1, n1;
+                                    chunk(nK, cb, c1, n1);
                                     if (n0 >= n1) task(aJ + c0, n0, aK + c1, n1, false);
                                     else task(aK + c1, n1, aJ + c0, n0, false);
                                 }
@@ -760,7 +834,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, 5) k_bp(const __grid_constant__
                         constexpr int SH = SlotShift<S>::v;
                         if ((lane & ((1 << SH) - 1)) == 0) {
                             const int s = (lane >> SH) & (S - 1);
-                            const int ref = a.prm.slot2ref[A.sidx + s];
+                            const int ref = t_slot[A.sidx + s];
                             if (ref >= 0) Gout[A.off + ref] = v;
                         }
                     }
@@ -906,8 +980,8 @@ static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t s
         ++::ann::g_launch_counter, k_zero<real><<<1024, 256, 0, st>>>(out, (size_t)a.natoms * pot.imax);
     }
     cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), st);
-    auto go = [&](auto kern, size_t wb) {
-        const size_t smem = wb * BP_WARPS;
+    auto go = [&](auto kern, size_t wb, size_t table) {
+        const size_t smem = wb * BP_WARPS + table;
         int per_sm = (int)std::max<size_t>(1, (size_t)(227 * 1024) / std::max<size_t>(smem, 1));
         per_sm = std::min(per_sm, 16);
         if (a.grid_per_sm > 0) per_sm = std::min(per_sm, (int)a.grid_per_sm);
@@ -915,12 +989,13 @@ static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t s
         grid = std::min(grid, std::max(1, (int)a.nsm) * per_sm);
         ++::ann::g_launch_counter, kern<<<grid, BP_WARPS * 32, smem, st>>>(pot, a);
     };
+    const size_t tb = (PASS == PASS_FORCE) ? bp_table_bytes<real>(pot) : 0;
     if (pot.fast) {
-        if (pot.fastNG == 1) go(k_bp<real, 1, true, PASS>, WarpMem<real, 1, PASS>::bytes(a.cap, pot.imax));
-        else if (pot.fastNG == 2) go(k_bp<real, 2, true, PASS>, WarpMem<real, 2, PASS>::bytes(a.cap, pot.imax));
-        else go(k_bp<real, 4, true, PASS>, WarpMem<real, 4, PASS>::bytes(a.cap, pot.imax));
+        if (pot.fastNG == 1) go(k_bp<real, 1, true, PASS>, WarpMem<real, 1, PASS>::bytes(a.cap, pot.imax), tb);
+        else if (pot.fastNG == 2) go(k_bp<real, 2, true, PASS>, WarpMem<real, 2, PASS>::bytes(a.cap, pot.imax), tb);
+        else go(k_bp<real, 4, true, PASS>, WarpMem<real, 4, PASS>::bytes(a.cap, pot.imax), tb);
     } else {
-        go(k_bp<real, 1, false, PASS>, WarpMem<real, 1, PASS>::bytes(a.cap, pot.imax));
+        go(k_bp<real, 1, false, PASS>, WarpMem<real, 1, PASS>::bytes(a.cap, pot.imax), 0);
     }
 }
 
@@ -944,7 +1019,8 @@ size_t bp_smem_bytes(const DevPot& pot, int cap, bool fp64) {
         if (ng == 2) return std::max({WarpMem<real, 2, PASS_SYMM>::bytes(cap, pot.imax), WarpMem<real, 2, PASS_FORCE>::bytes(cap, pot.imax), WarpMem<real, 2, PASS_JVP>::bytes(cap, pot.imax)});
         return std::max({WarpMem<real, 4, PASS_SYMM>::bytes(cap, pot.imax), WarpMem<real, 4, PASS_FORCE>::bytes(cap, pot.imax), WarpMem<real, 4, PASS_JVP>::bytes(cap, pot.imax)});
     };
-    return (fp64 ? b(double()) : b(float())) * BP_WARPS;
+    const size_t table = pot.fast ? (fp64 ? bp_table_bytes<double>(pot) : bp_table_bytes<float>(pot)) : 0;
+    return (fp64 ? b(double()) : b(float())) * BP_WARPS + table;
 }
 
 template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st) { launch_pass<real, PASS_SYMM>(pot, a, st); }

@@ -126,6 +126,8 @@ void build_plan(const Potential& p, PlanHost& out) {
     auto pad = [](std::vector<double>& v) { if (v.empty()) v.push_back(0.0); };
     pad(out.rs); pad(out.reta); pad(out.aeta); pad(out.zeta); pad(out.alam); pad(out.inpw); pad(out.inpb); pad(out.b); pad(out.w); pad(out.wt);
     if (out.agrp.empty()) out.agrp.push_back(0);
+    out.pot.nrad = (int)out.rs.size();
+    out.pot.nslot = (int)out.slot2ref.size();
 }
 
 }  // namespace ann

@@ -57,6 +57,7 @@ struct DevPot {
     int32_t fast;                      // 1: every angular block is GAUSS with lambda=+-1, zeta=2^k (k<=3)
     int32_t fastNG;                    // damping groups compiled into the fast kernels (1,2,4)
     double rc;                         // neighbour cutoff (NNP::rc)
+    int32_t nrad, nslot;               // lengths of the radial parameter arrays (rs / reta) and of slot2ref
     DevType t[MAXT];
 };
 
