@@ -42,9 +42,17 @@ constexpr int BP_WARPS = 4;
 #define ANN_BP_MIN_BLOCKS 5         // resident blocks per SM the symmetry / tangent passes are bounded for
 #endif
 #ifndef ANN_BP_MIN_BLOCKS_FORCE
-#define ANN_BP_MIN_BLOCKS_FORCE 4   // the force pass (122 registers without spills; at 5: spills)
-#endif
-constexpr int bp_min_blocks(int pass) { return pass == PASS_FORCE ? ANN_BP_MIN_BLOCKS_FORCE : ANN_BP_MIN_BLOCKS; }
+#define ANN_BP_MIN_BLOCKS_FORCE 4   // the force pass with two or more damping groups (114-126 registers
+#endif                              // without spills; bounded for five it spills)
+// With one damping group the atoms have few neighbours (the 262,144-atom argon box) and the passes
+// need the occupancy: the force pass fits five blocks without spills (92 registers), the symmetry
+// and tangent passes six (84 registers; bounded for five they take 89 and lose a block per SM:
+// 0.340 -> 0.395 ms on that box)
+// (fast-path kernels; the generic path keeps five)
+constexpr int bp_min_blocks(int pass, int ng, bool fast) {
+    return pass == PASS_FORCE ? (ng > 1 ? ANN_BP_MIN_BLOCKS_FORCE : ANN_BP_MIN_BLOCKS)
+                              : (ng == 1 && fast ? ANN_BP_MIN_BLOCKS + 1 : ANN_BP_MIN_BLOCKS);
+}
 constexpr int CHUNK = 16;   // functions per register chunk (radial and generic angular)
 
 // ---------------------------------------------------------------- PTX helpers (bulk copy + mbarrier)
@@ -486,7 +494,7 @@ __host__ __device__ inline size_t bp_table_bytes(const DevPot& pot) {   // force
 
 // ---------------------------------------------------------------- the kernel
 template <typename real, int NG, bool FAST, int PASS>
-__global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS)) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
+__global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
     typedef typename V4<real>::T R4;
     extern __shared__ __align__(128) unsigned char bsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

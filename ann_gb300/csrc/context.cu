@@ -437,7 +437,7 @@ int ann_destroy(ann_ctx* c) {
     for (DevBuf* b : {&c->poff, &c->cell, &c->pos, &c->type, &c->sid, &c->geo, &c->pos4, &c->abin, &c->abc, &c->am, &c->aslot,
                       &c->bcount, &c->bstart, &c->bidx, &c->bm, &c->bpos4, &c->bposd, &c->nbins_total, &c->nn, &c->ntc, &c->nj, &c->nimg,
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
-                      &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad,
+                      &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad, &c->gpart,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
                       &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->opt_s0, &c->opt_s1, &c->opt_s2, &c->opt_gold, &c->opt_part,
                       &c->lx, &c->ltype, &c->lilist, &c->lnoff, &c->lneigh, &c->lrtype, &c->lnn, &c->lntc, &c->lnj, &c->lnr, &c->lG,

@@ -143,7 +143,7 @@ struct ann_ctx {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     GraphKey gkey[2] = {{-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}};
     // training
-    DevBuf Eref, Fref, loss3, ce, lam, U, grad;
+    DevBuf Eref, Fref, loss3, ce, lam, U, grad, gpart;   // gpart: per-block gradient sums of the training pass
     bool have_train = false;
     int train_prec = 0;
     double train_wE = 0, train_wF = 0;

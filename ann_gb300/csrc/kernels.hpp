@@ -147,10 +147,15 @@ struct MlpArgs {
     double ct;                       // tangent-loss weight
     double* grad;                    // [P] parameter gradient accumulator (FP64 in both precisions)
     const int32_t* poff;             // [T] parameter offset of each type
+    double* gpart;                   // [blocks * pstride] per-block sums of the training pass (see
+    int32_t pstride;                 //   mlp_train_part_bytes), added into grad in block order
     DevParams<real> prm;
 };
 template <typename real> void launch_mlp_forward_backward(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st);
+// bytes of the training pass's per-block gradient sums for natoms atoms (MlpArgs::gpart) and its row
+// stride (the largest per-type parameter count)
+size_t mlp_train_part_bytes(const DevPot& pot, int natoms, int* pstride);
 
 // ---- small kernels (misc.cu) ---------------------------------------------------------------
 void launch_type_lists(int natoms, int ntypes, const int32_t* type, int32_t* tcount, int32_t* tstart, int32_t* tlist,

@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(MLP_TT) k_mlp_train(const __grid_constant__ De
         adb[a * ld] = (atoms[a] >= 0) ? (real)(A.ct * net.outw) : real(0);
     }
     __syncthreads();
-    const int pbase = A.poff[type];
+    // the block's partial sums of every parameter of its type (each written once)
+    double* gp = A.gpart + (size_t)blockIdx.x * A.pstride;
     // parameter offsets (reference packing): biases of all layers, then weights column-major
     int bias_at[MAXLAYER], wt_at[MAXLAYER];
     {
@@ -275,11 +276,11 @@ __global__ void __launch_bounds__(MLP_TT) k_mlp_train(const __grid_constant__ De
         }
         __syncthreads();
         // bias gradient: sum over the tile's atoms of zbar, in the pass's precision (the products
-        // are formed in it), then added to the FP64 gradient
+        // are formed in it), stored as the block's FP64 partial (k_grad_blocks adds the blocks)
         for (int n = threadIdx.x; n < no; n += blockDim.x) {
             real s = real(0);
             for (int a = 0; a < TAT; ++a) s += zb[a * ld + n];
-            atomicAdd(&A.grad[pbase + bias_at[l] + n], (double)s);
+            gp[bias_at[l] + n] = (double)s;
         }
         // weight gradient: sum_a zbar[a][n] a_{l}[a][m] + zdbar[a][n] ad_{l}[a][m], column-major;
         // each thread a block of RT outputs n x 2 inputs m (every shared value used 2 or RT times)
@@ -305,8 +306,8 @@ __global__ void __launch_bounds__(MLP_TT) k_mlp_train(const __grid_constant__ De
 #pragma unroll
             for (int k = 0; k < RT; ++k) {
                 if (n0 + k >= no) continue;
-                atomicAdd(&A.grad[pbase + wt_at[l] + m0 * no + n0 + k], (double)s[k][0]);
-                if (m0 + 1 < ni) atomicAdd(&A.grad[pbase + wt_at[l] + (m0 + 1) * no + n0 + k], (double)s[k][1]);
+                gp[wt_at[l] + m0 * no + n0 + k] = (double)s[k][0];
+                if (m0 + 1 < ni) gp[wt_at[l] + (m0 + 1) * no + n0 + k] = (double)s[k][1];
             }
         }
         __syncthreads();
@@ -336,6 +337,62 @@ void launch_mlp_forward_backward(const DevPot& pot, const MlpArgs<real>& a, cuda
     const int grid = (a.natoms + TA - 1) / TA + a.ntypes;
     ++::ann::g_launch_counter, k_mlp_fb<real><<<grid, MLP_T, smem, st>>>(pot, a, ld);
 }
+// grad[poff[t] + k] += sum over the blocks b of type t of gpart[b][k]: the training pass's per-tile
+// sums added deterministically (no atomics, the same result on every run). A block of 32 x GB_SEG
+// threads takes 32 consecutive parameters (coalesced rows); thread row y sums segment y of the
+// type's block rows (independent loads, 8 in flight) and the segments are added in order.
+constexpr int GB_SEG = 8;
+__host__ __device__ inline int net_params(const DevNet& net) {
+    int s = 0;
+    for (int l = 0; l < net.nlayer; ++l) s += net.nodes[l] * (1 + ((l == 0) ? net.nin : net.nodes[l - 1]));
+    return s;
+}
+__global__ void __launch_bounds__(32 * GB_SEG) k_grad_blocks(const __grid_constant__ DevPot pot, const int32_t* tstart, const int32_t* poff,
+                                                             const double* gpart, int pstride, double* grad) {
+    __shared__ double seg[GB_SEG][32];
+    const int64_t g = blockIdx.x * (int64_t)32 + threadIdx.x;
+    int b0 = 0, tiles = 0, type = -1, k = 0;
+    int64_t p0 = 0;
+    for (int t = 0; t < pot.ntypes; ++t) {
+        const int nt = (tstart[t + 1] - tstart[t] + TAT - 1) / TAT;
+        const int P = net_params(pot.t[t].net);
+        if (type < 0 && g >= p0 && g < p0 + P) { type = t; k = (int)(g - p0); tiles = nt; }
+        if (type < 0) b0 += nt;
+        p0 += P;
+    }
+    double s = 0.0;
+    if (type >= 0) {
+        const int len = (tiles + GB_SEG - 1) / GB_SEG;
+        const int lo = threadIdx.y * len, hi = min(tiles, lo + len);
+        const double* col = gpart + (size_t)b0 * pstride + k;
+        int b = lo;
+        for (; b + 8 <= hi; b += 8) {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = col[(size_t)(b + q) * pstride];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s += v[q];
+        }
+        for (; b < hi; ++b) s += col[(size_t)b * pstride];
+    }
+    seg[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && type >= 0) {
+        double tsum = 0.0;
+#pragma unroll
+        for (int y = 0; y < GB_SEG; ++y) tsum += seg[y][threadIdx.x];
+        grad[poff[type] + k] += tsum;
+    }
+}
+
+size_t mlp_train_part_bytes(const DevPot& pot, int natoms, int* pstride) {
+    int P = 1;
+    for (int t = 0; t < pot.ntypes; ++t) P = std::max(P, net_params(pot.t[t].net));
+    if (pstride) *pstride = P;
+    const size_t blocks = (size_t)(std::max(natoms, 0) + TAT - 1) / TAT + pot.ntypes;
+    return blocks * P * sizeof(double);
+}
+
 template <typename real>
 void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st) {
     if (a.natoms <= 0) return;
@@ -344,6 +401,9 @@ void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream
     const size_t smem = (size_t)(2 * (L + 1) + 3 * L + 4) * TAT * ld * sizeof(real);
     const int grid = (a.natoms + TAT - 1) / TAT + a.ntypes;
     ++::ann::g_launch_counter, k_mlp_train<real><<<grid, MLP_TT, smem, st>>>(pot, a, ld);
+    int64_t total = 0;
+    for (int t = 0; t < pot.ntypes; ++t) total += net_params(pot.t[t].net);
+    ++::ann::g_launch_counter, k_grad_blocks<<<(unsigned)((total + 31) / 32), dim3(32, GB_SEG), 0, st>>>(pot, a.tstart, a.poff, a.gpart, a.pstride, a.grad);
 }
 void configure_mlp(int maxsmem) {
     set_max_dynamic_smem(k_mlp_fb<float>, maxsmem);

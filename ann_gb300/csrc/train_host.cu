@@ -180,6 +180,8 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
         c->grad.ensure(8 * (size_t)std::max<int64_t>(n, 1));
         ck(cudaMemsetAsync(c->grad.p, 0, 8 * (size_t)std::max<int64_t>(n, 1), c->stream), "memset grad");
         const DevPot& pot = c->plan.pot;
+        int pstride = 1;
+        c->gpart.ensure(mlp_train_part_bytes(pot, c->N, &pstride));
         auto go = [&](auto tag) {
             using real = decltype(tag);
             BpArgs<real> b = bp_args<real>(c);
@@ -189,6 +191,7 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
             m.natoms = c->N; m.ntypes = c->pot.ntypes(); m.imax = pot.imax; m.tstart = c->tstart.as<int32_t>(); m.tlist = c->tlist.as<int32_t>();
             m.G = c->G.as<real>(); m.U = c->U.as<real>(); m.ce = c->ce.as<double>(); m.ct = -1.0; m.grad = c->grad.as<double>();
             m.poff = c->poff.as<int32_t>(); m.prm = b.prm;
+            m.gpart = c->gpart.as<double>(); m.pstride = pstride;
             launch_mlp_train_grad<real>(pot, m, c->stream);
         };
         if (c->train_prec == ANN_FP64) go(double()); else go(float());
