@@ -49,6 +49,8 @@ void drop_graphs(ann_ctx* c) { reset_graph(c); }
 void rebuild_plan(ann_ctx* c) {
     build_plan(c->pot, c->plan);
     build_tc_plan(c->plan.pot, c->plan.w, c->plan.b, c->plan.inpw, c->plan.inpb, c->max_smem, c->opt.tc_split, c->tc);
+    c->tct_ok = c->tc.ok;
+    for (int t = 0; t < c->plan.pot.ntypes && c->tct_ok; ++t) c->tct_ok = plan_tc_train(c->tc.t[t], c->max_smem, c->tct[t]);
     if (c->opt.mlp_backend == 2 && !c->tc.ok)
         throw ann_error(ANN_ERR_UNSUPPORTED, "the networks do not fit the tensor-core kernel (hidden layers 1..5, widths <= 256)");
     c->tcimg.ensure(c->tc.image.size());

@@ -104,6 +104,8 @@ struct ann_ctx {
     Potential pot;
     PlanHost plan;
     TcPlan tc;                      // tensor-core network images (MIXED precision)
+    TcTrainLayout tct[MAXT];        // the training kernel's layout per type
+    bool tct_ok = false;            // every type fits the tensor-core training kernel
     DevBuf tcimg;
     // packed FP64 parameters on the device and where each one is copied to
     DevBuf p64, pmap;

@@ -153,9 +153,13 @@ struct MlpArgs {
 };
 template <typename real> void launch_mlp_forward_backward(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream_t st);
-// bytes of the training pass's per-block gradient sums for natoms atoms (MlpArgs::gpart) and its row
-// stride (the largest per-type parameter count)
-size_t mlp_train_part_bytes(const DevPot& pot, int natoms, int* pstride);
+// bytes of the training pass's per-block gradient sums for natoms atoms in tiles of `tile` atoms
+// (MlpArgs::gpart) and its row stride (the largest per-type parameter count)
+size_t mlp_train_part_bytes(const DevPot& pot, int natoms, int tile, int* pstride);
+int mlp_train_tile();   // atoms per block of the SIMT training pass
+// grad[poff[t] + k] += the per-tile sums of type t's tiles (tiles of `tile` atoms), in tile order
+void launch_grad_blocks(const DevPot& pot, const int32_t* tstart, const int32_t* poff, const double* gpart, int pstride, double* grad,
+                        int tile, cudaStream_t st);
 
 // ---- small kernels (misc.cu) ---------------------------------------------------------------
 void launch_type_lists(int natoms, int ntypes, const int32_t* type, int32_t* tcount, int32_t* tstart, int32_t* tlist,

@@ -348,13 +348,13 @@ __host__ __device__ inline int net_params(const DevNet& net) {
     return s;
 }
 __global__ void __launch_bounds__(32 * GB_SEG) k_grad_blocks(const __grid_constant__ DevPot pot, const int32_t* tstart, const int32_t* poff,
-                                                             const double* gpart, int pstride, double* grad) {
+                                                             const double* gpart, int pstride, double* grad, int tile) {
     __shared__ double seg[GB_SEG][32];
     const int64_t g = blockIdx.x * (int64_t)32 + threadIdx.x;
     int b0 = 0, tiles = 0, type = -1, k = 0;
     int64_t p0 = 0;
     for (int t = 0; t < pot.ntypes; ++t) {
-        const int nt = (tstart[t + 1] - tstart[t] + TAT - 1) / TAT;
+        const int nt = (tstart[t + 1] - tstart[t] + tile - 1) / tile;
         const int P = net_params(pot.t[t].net);
         if (type < 0 && g >= p0 && g < p0 + P) { type = t; k = (int)(g - p0); tiles = nt; }
         if (type < 0) b0 += nt;
@@ -385,11 +385,12 @@ __global__ void __launch_bounds__(32 * GB_SEG) k_grad_blocks(const __grid_consta
     }
 }
 
-size_t mlp_train_part_bytes(const DevPot& pot, int natoms, int* pstride) {
+int mlp_train_tile() { return TAT; }
+size_t mlp_train_part_bytes(const DevPot& pot, int natoms, int tile, int* pstride) {
     int P = 1;
     for (int t = 0; t < pot.ntypes; ++t) P = std::max(P, net_params(pot.t[t].net));
     if (pstride) *pstride = P;
-    const size_t blocks = (size_t)(std::max(natoms, 0) + TAT - 1) / TAT + pot.ntypes;
+    const size_t blocks = (size_t)(std::max(natoms, 0) + tile - 1) / tile + pot.ntypes;
     return blocks * P * sizeof(double);
 }
 
@@ -401,9 +402,14 @@ void launch_mlp_train_grad(const DevPot& pot, const MlpArgs<real>& a, cudaStream
     const size_t smem = (size_t)(2 * (L + 1) + 3 * L + 4) * TAT * ld * sizeof(real);
     const int grid = (a.natoms + TAT - 1) / TAT + a.ntypes;
     ++::ann::g_launch_counter, k_mlp_train<real><<<grid, MLP_TT, smem, st>>>(pot, a, ld);
+    launch_grad_blocks(pot, a.tstart, a.poff, a.gpart, a.pstride, a.grad, TAT, st);
+}
+void launch_grad_blocks(const DevPot& pot, const int32_t* tstart, const int32_t* poff, const double* gpart, int pstride, double* grad,
+                        int tile, cudaStream_t st) {
     int64_t total = 0;
     for (int t = 0; t < pot.ntypes; ++t) total += net_params(pot.t[t].net);
-    ++::ann::g_launch_counter, k_grad_blocks<<<(unsigned)((total + 31) / 32), dim3(32, GB_SEG), 0, st>>>(pot, a.tstart, a.poff, a.gpart, a.pstride, a.grad);
+    if (total <= 0) return;
+    ++::ann::g_launch_counter, k_grad_blocks<<<(unsigned)((total + 31) / 32), dim3(32, GB_SEG), 0, st>>>(pot, tstart, poff, gpart, pstride, grad, tile);
 }
 void configure_mlp(int maxsmem) {
     set_max_dynamic_smem(k_mlp_fb<float>, maxsmem);

@@ -99,4 +99,35 @@ struct TcArgs {
 void launch_mlp_tc(const TcType& tt, const TcArgs& a, long long est_atoms, int groups, size_t smem, int nsm, cudaStream_t st);
 void configure_mlp_tc(int maxsmem);
 
+// ---- the training pass on the tensor cores (mlp_tc_train.cu) --------------------------------
+// layout of a type: widths of the activation tiles H (inputs + a ones column) and of the delta
+// tiles, TMEM columns of the forward accumulators, of the weight-gradient accumulators (per hidden
+// layer and the output layer) and the shared-memory offsets
+struct TcTrainLayout {
+    int32_t WH, WZ;
+    int32_t zc[TC_MAXH], zdc[TC_MAXH], gw[TC_MAXH];
+    int32_t gwl, tmem_cols;
+    uint32_t o_h, o_z, o_tail, smem;
+};
+// false: the type's networks do not fit the training kernel (the SIMT kernel takes them)
+bool plan_tc_train(const TcType& tt, int max_smem, TcTrainLayout& ly);
+struct TcTrainArgs {
+    int32_t natoms, imax, ntypes;
+    const int32_t* tstart;                    // [T+1] start of each type in tlist
+    const int32_t* tlist;                     // [N] atoms grouped by type
+    const float* G;                           // [N*imax]
+    const float* U;                           // [N*imax] tangent of G
+    const double* ce;                         // [N] energy-loss weight per atom
+    float ct;                                 // tangent-loss weight
+    const uint8_t* image;                     // device copy of TcPlan::image
+    double* gpart;                            // [tiles of 128 atoms * pstride] per-tile gradient sums
+    int32_t pstride;
+    int32_t* status;
+    int32_t wait_polls;
+};
+// one CTA per tile of 128 atoms (types one after the other); the per-tile sums go to gpart, to be
+// added by launch_grad_blocks with tile = 128
+void launch_mlp_train_tc(const TcPlan& tc, const TcTrainLayout* lay, const TcTrainArgs& a, cudaStream_t st);
+void configure_mlp_train_tc(int maxsmem);
+
 }  // namespace ann

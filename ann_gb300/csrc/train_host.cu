@@ -180,8 +180,12 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
         c->grad.ensure(8 * (size_t)std::max<int64_t>(n, 1));
         ck(cudaMemsetAsync(c->grad.p, 0, 8 * (size_t)std::max<int64_t>(n, 1), c->stream), "memset grad");
         const DevPot& pot = c->plan.pot;
+        // the MIXED network pass on the tensor cores (tiles of 128 atoms) when every type fits it,
+        // else the SIMT kernel (tiles of 16); either writes per-tile sums added in tile order
+        const bool tc_train = c->train_prec == ANN_MIXED && use_tc(c) && c->tct_ok;
+        const int tile = tc_train ? TC_M : mlp_train_tile();
         int pstride = 1;
-        c->gpart.ensure(mlp_train_part_bytes(pot, c->N, &pstride));
+        c->gpart.ensure(mlp_train_part_bytes(pot, c->N, tile, &pstride));
         auto go = [&](auto tag) {
             using real = decltype(tag);
             BpArgs<real> b = bp_args<real>(c);
@@ -192,6 +196,18 @@ int ann_train_backward(ann_ctx* c, double scale, double* grad, int64_t n) {
             m.G = c->G.as<real>(); m.U = c->U.as<real>(); m.ce = c->ce.as<double>(); m.ct = -1.0; m.grad = c->grad.as<double>();
             m.poff = c->poff.as<int32_t>(); m.prm = b.prm;
             m.gpart = c->gpart.as<double>(); m.pstride = pstride;
+            if constexpr (std::is_same<real, float>::value) {
+                if (tc_train) {
+                    TcTrainArgs ta{};
+                    ta.natoms = c->N; ta.imax = pot.imax; ta.ntypes = c->pot.ntypes();
+                    ta.tstart = m.tstart; ta.tlist = m.tlist; ta.G = m.G; ta.U = m.U; ta.ce = m.ce; ta.ct = (float)m.ct;
+                    ta.image = c->tcimg.as<uint8_t>(); ta.gpart = m.gpart; ta.pstride = pstride;
+                    ta.status = c->status.as<int32_t>(); ta.wait_polls = c->wait_polls;
+                    launch_mlp_train_tc(c->tc, c->tct, ta, c->stream);
+                    launch_grad_blocks(pot, m.tstart, m.poff, m.gpart, pstride, m.grad, TC_M, c->stream);
+                    return;
+                }
+            }
             launch_mlp_train_grad<real>(pot, m, c->stream);
         };
         if (c->train_prec == ANN_FP64) go(double()); else go(float());

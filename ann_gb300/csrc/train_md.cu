@@ -150,6 +150,7 @@ void configure_kernels() {
     configure_mlp(maxs);
     configure_nbr(maxs);
     configure_mlp_tc(maxs);
+    configure_mlp_train_tc(maxs);
     done = true;
 }
 

@@ -154,3 +154,37 @@ def test_forced_warp_split(contexts, tmp_path, groups):
 def test_tc_groups_validated(gpu_lib):
     with pytest.raises(AnnError):
         Context(tc_groups=3)
+
+
+@pytest.mark.parametrize("nstruc", [3, 24])
+def test_training_gradient_on_tensor_cores(gpu_lib, tmp_path, nstruc):
+    """The training pass (energy + force loss, forward-over-reverse through the networks, weight
+    gradient over the atoms) on the tensor cores, tiles of 128 atoms, against the SIMT kernel on the
+    same batch (both mixed precision: within 1e-4 of the gradient's scale) and against the FP64 form
+    (1e-3 of the scale); a second backward call on the same forward state gives the same gradient bit
+    for bit (per-tile sums added in tile order; the forward's force sums use FP32 atomics, so a new
+    forward call may move the last bits)."""
+    from ann_gb300 import workloads as W
+    from ann_gb300.api import pack_batch
+    structs = W.random_binary(nstruc, 32, 256, seed=77)
+    offs, posn, types, cell = pack_batch(structs)
+    Eref, Fref = W.lennard_jones(structs)
+    Fref = np.concatenate(Fref)
+    tc = Context(mlp_backend=2)
+    simt = Context(mlp_backend=1)
+    try:
+        text = cases.config_potential(tc, 3, tmp_path, precondition_batch=(offs, posn, types, cell))
+        simt.load_text(text)
+        tc.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+        g64 = tc.train_backward()
+        tc.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=MIXED)
+        g_tc = tc.train_backward()
+        assert np.array_equal(tc.train_backward(), g_tc)   # the same forward state: bit for bit
+        simt.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=MIXED)
+        g_simt = simt.train_backward()
+        scale = np.abs(g64).max()
+        assert np.abs(g_tc - g_simt).max() <= 1e-4 * scale, np.abs(g_tc - g_simt).max() / scale
+        assert np.abs(g_tc - g64).max() <= 1e-3 * scale, np.abs(g_tc - g64).max() / scale
+    finally:
+        tc.close()
+        simt.close()
