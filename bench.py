@@ -552,15 +552,17 @@ def main():
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count   # cudaDevAttrMultiProcessorCount
     fp32_peak = nsm * 128 * 2 * sm_mhz * 1e6 / 1e12           # TFLOP/s (FMA = 2 flop) at the sampled clock
     mufu_peak = nsm * 16 * sm_mhz * 1e6 / 1e12                 # T ops/s
-    # DRAM bytes of one force-pass launch: the per-atom figure of the committed ncu capture (small
-    # case of the same workload) times the atoms of this launch
+    # DRAM bytes of one force-pass launch (ncu capture of this workload, committed under profiles/)
     traffic, traffic_src = None, None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         tr = json.loads(tf.read_text()).get("k_bp force pass (forces)")
         if tr:
-            traffic = float(tr["dram_bytes_per_atom"]) * N
-            traffic_src = f"{tr['dram_bytes_per_atom']} B/atom x {N} atoms, from {tr['source']}"
+            # the DRAM bytes of one force-pass launch as ncu measured them on this workload; another
+            # batch scales them by its atoms (the traffic grows with the atom count at fixed density)
+            traffic = float(tr["dram_bytes_per_launch"]) * N / float(tr["atoms_in_capture"])
+            traffic_src = (f"{tr['dram_bytes_per_launch']} B per launch measured on {tr['atoms_in_capture']} atoms"
+                           + ("" if N == tr["atoms_in_capture"] else f", scaled to {N} atoms") + f", from {tr['source']}")
     roofline = {"kernel": "k_bp force pass (" + names[4] + ")", "bound": "hbm",
                 "achieved": work["force_bytes"] / t_force / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": work["force_bytes"] / t_force / 1e9 / pk["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
