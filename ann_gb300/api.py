@@ -99,6 +99,7 @@ _SIGS = {
     "ann_num_neighbors": (C.c_int, [_V, _I64]),
     "ann_get_neighbors": (C.c_int, [_V, _I32, _I32, _I32, _D, C.c_int64]),
     "ann_train_forward": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, C.c_double, C.c_double, C.c_int32, _D]),
+    "ann_train_forward_staged": (C.c_int, [_V, C.c_double, C.c_double, C.c_int32, _D]),
     "ann_train_backward": (C.c_int, [_V, C.c_double, _D, C.c_int64]),
     "ann_adam_init": (C.c_int, [_V, C.c_double, C.c_double, C.c_double, C.c_double]),
     "ann_adam_step": (C.c_int, [_V, C.c_double]),
@@ -490,6 +491,15 @@ class Context:
                                             _d(np.ascontiguousarray(posn, np.float64)), _i32(np.ascontiguousarray(types, np.int32)),
                                             _d(np.ascontiguousarray(cell, np.float64)), _d(np.ascontiguousarray(e_ref, np.float64)),
                                             _d(np.ascontiguousarray(f_ref, np.float64)), w_energy, w_force, prec, _d(loss)))
+        return loss
+
+    def train_forward_staged(self, w_energy=1.0, w_force=0.1, precision=None):
+        """The forward pass over the batch and labels of the preceding train_forward, whose neighbour
+        rows and symmetry functions stayed on the device (the reference trainer's loop over its
+        stored structures): networks, forces, sums and loss with the current parameters."""
+        prec = self.precision if precision is None else precision
+        loss = np.zeros(3)
+        self._ck(self.lib.ann_train_forward_staged(self.h, w_energy, w_force, prec, _d(loss)))
         return loss
 
     LOSS = {"MSE": 1, "MAE": 2, "HUBER": 3, "ASINH": 4}

@@ -40,7 +40,7 @@ static void upload_params(ann_ctx* c, ParamSet<real>& P) {
     upload_vec<real>(P.inpw, h.inpw, c->stream); upload_vec<real>(P.inpb, h.inpb, c->stream);
 }
 static void reset_graph(ann_ctx* c) {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
         if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
         c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, -1, 0};
     }
@@ -203,6 +203,7 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
     if (c->S > 0) ck(cudaMemcpyAsync(c->cell.p, cell, sizeof(double) * 9 * (size_t)c->S, k, c->stream), "copy cells");
     c->have_batch = true;
     c->have_results = false;
+    c->train_staged = false;
 }
 
 // ---------------------------------------------------------------- the E+F kernel sequence
@@ -246,10 +247,17 @@ static RedTable red_table(ann_ctx* c) {
 
 
 template <typename real>
-static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
+static void enqueue_ef(ann_ctx* c, bool forces, int mode) {
     cudaStream_t st = c->stream;
     const bool fp64 = std::is_same<real, double>::value;
     const DevPot& pot = c->plan.pot;
+    BpArgs<real> b = bp_args<real>(c);
+    b.prm = params_of<real>(c->pf, c->pd);
+    if (mode == SEQ_STAGED) {
+        // neighbour rows, type lists and symmetry functions of the staged batch are on the device
+        mark(c, 0); mark(c, 1); mark(c, 2); mark(c, 3);
+    } else {
+    const bool build_list = (mode == SEQ_BUILD);
     // the per-type atom lists depend on the types only: outside the phase-timed and debug modes
     // they run on a side stream that forks here and joins before the networks (a parallel branch
     // of the captured graph, beside the neighbour search and the symmetry functions)
@@ -275,12 +283,11 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     if (!side) type_lists(st);
     check_phase(c, "type lists");
     mark(c, 2);
-    BpArgs<real> b = bp_args<real>(c);
-    b.prm = params_of<real>(c->pf, c->pd);
     launch_symm<real>(pot, b, st);
     check_phase(c, "symmetry functions");
     mark(c, 3);
     if (side) ck(cudaStreamWaitEvent(st, c->ev_join, 0), "stream wait");
+    }
     enqueue_networks<real>(c, c->N, c->G, c->dEdG, c->Eatom, c->tstart, c->tlist, b.prm);
     check_phase(c, "networks");
     mark(c, 4);
@@ -296,7 +303,7 @@ static void enqueue_ef(ann_ctx* c, bool forces, bool build_list) {
     mark(c, 6);
 }
 
-void run_batch(ann_ctx* c, int prec, bool forces, bool build_list) {
+static void run_sequence(ann_ctx* c, int prec, bool forces, int mode) {
     if (!c->have_batch) throw ann_error(ANN_ERR_STATE, "no batch staged");
     if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
     ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
@@ -310,14 +317,14 @@ void run_batch(ann_ctx* c, int prec, bool forces, bool build_list) {
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
     const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), c->md_ready ? 1 : 0, g_alloc_gen.load()};
     const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
-    const int gs = build_list ? 0 : 1;
+    const int gs = mode;
     if (graphs) {
         if (!(c->gexec[gs] && c->gkey[gs] == key)) {
             if (c->gexec[gs]) { cudaGraphExecDestroy(c->gexec[gs]); c->gexec[gs] = nullptr; }
             cudaGraph_t g = nullptr;
             const int64_t before = g_launch_counter;
             ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-            if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
+            if (prec == ANN_FP64) enqueue_ef<double>(c, forces, mode); else enqueue_ef<float>(c, forces, mode);
             const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
             if (ce != cudaSuccess) {
                 // locate the failing launch: replay the sequence eagerly with per-phase checks
@@ -326,7 +333,7 @@ void run_batch(ann_ctx* c, int prec, bool forces, bool build_list) {
                 const bool d0 = c->debug;
                 c->debug = true;
                 try {
-                    if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
+                    if (prec == ANN_FP64) enqueue_ef<double>(c, forces, mode); else enqueue_ef<float>(c, forces, mode);
                 } catch (...) { c->debug = d0; throw; }
                 c->debug = d0;
                 throw ann_error(ANN_ERR_CUDA, std::string("graph capture failed (") + cudaGetErrorString(ce) + ") but the eager replay succeeded");
@@ -340,13 +347,25 @@ void run_batch(ann_ctx* c, int prec, bool forces, bool build_list) {
         c->kernels += c->graph_kernels[gs];
     } else {
         const int64_t before = g_launch_counter;
-        if (prec == ANN_FP64) enqueue_ef<double>(c, forces, build_list); else enqueue_ef<float>(c, forces, build_list);
+        if (prec == ANN_FP64) enqueue_ef<double>(c, forces, mode); else enqueue_ef<float>(c, forces, mode);
         c->kernels += g_launch_counter - before;
     }
     ck(cudaGetLastError(), "kernel launch");
     c->last_prec = prec;
     c->have_results = true;
     c->have_forces = forces;
+}
+
+void run_batch(ann_ctx* c, int prec, bool forces, bool build_list) {
+    c->train_staged = false;
+    run_sequence(c, prec, forces, build_list ? SEQ_BUILD : SEQ_REFRESH);
+}
+
+void run_staged(ann_ctx* c, int prec) {
+    if (!c->train_staged) throw ann_error(ANN_ERR_STATE, "no staged training batch");
+    if (prec != c->train_staged_prec)
+        throw ann_error(ANN_ERR_STATE, "the staged symmetry functions were computed in the other precision");
+    run_sequence(c, prec, true, SEQ_STAGED);
 }
 
 // a page-locked copy of the device status word, for reads that ride along with result copies
@@ -406,6 +425,8 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         ck(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream create");
         ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event create");
         ck(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event create");
+        ck(cudaEventCreateWithFlags(&c->ev_net_fork, cudaEventDisableTiming), "event create");
+        ck(cudaEventCreateWithFlags(&c->ev_net_join, cudaEventDisableTiming), "event create");
         configure_kernels();
         cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->opt.device);
         cudaDeviceGetAttribute(&c->tc.smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->opt.device);
@@ -423,6 +444,8 @@ int ann_create(ann_ctx** out, const ann_options* opt) {
         if (c->side) cudaStreamDestroy(c->side);
         if (c->ev_fork) cudaEventDestroy(c->ev_fork);
         if (c->ev_join) cudaEventDestroy(c->ev_join);
+        if (c->ev_net_fork) cudaEventDestroy(c->ev_net_fork);
+        if (c->ev_net_join) cudaEventDestroy(c->ev_net_join);
         delete c;
         return fail(nullptr, e.code, e.what());
     }
@@ -452,6 +475,8 @@ int ann_destroy(ann_ctx* c) {
     if (c->side) cudaStreamDestroy(c->side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_net_fork) cudaEventDestroy(c->ev_net_fork);
+    if (c->ev_net_join) cudaEventDestroy(c->ev_net_join);
     delete c;
     return ANN_OK;
 }
@@ -472,6 +497,7 @@ int ann_load_potential_text(ann_ctx* c, const char* text) {
         c->pot = p;
         c->opt_ready = false;
         c->st_ready = false;   // statistics belong to the previous potential's inputs
+        c->train_staged = false;   // so do the staged training batch's symmetry functions
         rebuild_plan(c);
     })
 }

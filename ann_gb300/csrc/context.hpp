@@ -84,6 +84,9 @@ inline void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw ann_error(ANN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// the three forms of the E+F kernel sequence (graph slots of ann_ctx::gexec)
+enum { SEQ_BUILD = 0, SEQ_REFRESH = 1, SEQ_STAGED = 2 };
+
 struct GraphKey {
     int S, N, cap, prec, forces, nbins, nchunks;
     int md;         // MD mode: list cutoff rc + skin, refreshed between rebuilds
@@ -99,6 +102,7 @@ struct ann_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;                 // fork / join branch of the E+F sequence
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_net_fork = nullptr, ev_net_join = nullptr;   // the per-type network launches on two streams
     std::string err;
     bool have_pot = false;
     Potential pot;
@@ -141,13 +145,19 @@ struct ann_ctx {
     int last_prec = -1;
     bool have_results = false, have_forces = false;
     // graphs
-    // graphs of the E+F sequence: [0] with the list build, [1] with the Verlet-list refresh (MD)
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    GraphKey gkey[2] = {{-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}};
+    // graphs of the E+F sequence: [SEQ_BUILD] with the list build, [SEQ_REFRESH] with the Verlet-list
+    // refresh (MD), [SEQ_STAGED] from the networks on (neighbour rows and G of the staged training batch)
+    cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+    GraphKey gkey[3] = {{-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}};
     // training
     DevBuf Eref, Fref, loss3, ce, lam, U, grad, gpart;   // gpart: per-block gradient sums of the training pass
     bool have_train = false;
     int train_prec = 0;
+    // the batch of the last ann_train_forward with its neighbour rows, type lists and symmetry
+    // functions (in train_staged_prec) still on the device, for ann_train_forward_staged; cleared by
+    // any other batch, E+F sequence or potential load
+    bool train_staged = false;
+    int train_staged_prec = 0;
     double train_wE = 0, train_wF = 0;
     int train_loss = ANN_LOSS_MSE, train_norm = ANN_NORM_LINEAR;   // energy term (ann_train_set_loss)
     double train_delta = 1.0;
@@ -172,7 +182,7 @@ struct ann_ctx {
     int st_T = 0, st_imax = 0;
     // instrumentation
     int64_t kernels = 0;            // kernels launched (graph replays add graph_kernels)
-    int64_t graph_kernels[2] = {0, 0};
+    int64_t graph_kernels[3] = {0, 0, 0};
     bool profile = false;
     bool debug = false;             // synchronise and check after every phase (ANN_DEBUG=1)
     int max_smem = 48 * 1024;       // opt-in shared memory per block of the device
@@ -202,6 +212,9 @@ void sync_params_from_device(ann_ctx* c);
 void leave_md(ann_ctx* c);
 void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell, bool device_src);
 void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true);
+// the E+F sequence from the networks on, over the neighbour rows, type lists and symmetry
+// functions that the last ann_train_forward left on the device (c->train_staged)
+void run_staged(ann_ctx* c, int prec);
 void finish_batch(ann_ctx* c);
 int32_t* status_host(ann_ctx* c);
 // drops the captured graphs (launch shapes changed)
@@ -230,13 +243,33 @@ inline void enqueue_networks(ann_ctx* c, int natoms, DevBuf& G, DevBuf& dEdG, De
                              const DevParams<real>& prm) {
     const DevPot& pot = c->plan.pot;
     if (!std::is_same<real, double>::value && use_tc(c)) {
-        for (int ty = 0; ty < c->pot.ntypes(); ++ty) {
+        // one launch per type; outside the phase-timed and debug modes the odd types run on the side
+        // stream, so that the types' tiles share the SMs (a small batch leaves most SMs idle in each
+        // launch). CTAs of different types may then share an SM: every launch asks for the shared
+        // memory that admits at most 512 / (widest TMEM allocation) CTAs per SM, so that co-resident
+        // CTAs never need more than the SM's 512 tensor-memory columns together.
+        const int T = c->pot.ntypes();
+        const bool fork = T > 1 && !c->profile && !c->debug;
+        int cmax = 32;
+        for (int ty = 0; ty < T; ++ty) cmax = std::max(cmax, (int)c->tc.t[ty].tmem_cols);
+        if (fork) {
+            ck(cudaEventRecord(c->ev_net_fork, c->stream), "event record");
+            ck(cudaStreamWaitEvent(c->side, c->ev_net_fork, 0), "stream wait");
+        }
+        for (int ty = 0; ty < T; ++ty) {
             TcArgs ta{};
             ta.natoms = natoms; ta.imax = pot.imax; ta.type = ty;
             ta.tstart = tstart.as<int32_t>(); ta.tlist = tlist.as<int32_t>();
             ta.G = G.as<float>(); ta.dEdG = dEdG.as<float>(); ta.Eatom = Eatom.as<double>();
             ta.image = c->tcimg.as<uint8_t>(); ta.status = c->status.as<int32_t>(); ta.wait_polls = c->wait_polls;
-            launch_mlp_tc(c->tc.t[ty], ta, natoms / c->pot.ntypes(), c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, c->tc.smem_bytes(ty), c->nsm, c->stream);
+            size_t smem = c->tc.smem_bytes(ty);
+            if (fork) smem = std::max(smem, (size_t)c->tc.smem_per_sm / (size_t)(512 / cmax + 1) + 1);
+            launch_mlp_tc(c->tc.t[ty], ta, natoms / T, c->tune_tc[ty] ? c->tune_tc[ty] : c->opt.tc_groups, smem, c->nsm,
+                          (fork && (ty & 1)) ? c->side : c->stream);
+        }
+        if (fork) {
+            ck(cudaEventRecord(c->ev_net_join, c->side), "event record");
+            ck(cudaStreamWaitEvent(c->stream, c->ev_net_join, 0), "stream wait");
         }
     } else {
         MlpArgs<real> m{};

@@ -34,6 +34,33 @@ static std::vector<double> stats_host(ann_ctx* c, int t, int64_t* count) {
     return out;
 }
 
+// the loss right behind the E+F sequence, read back with the status word in one round trip; a
+// status that is not clean goes through finish_batch (recover or throw) and the loss again. The
+// batch, its neighbour rows and its symmetry functions then stay staged for
+// ann_train_forward_staged.
+static void train_loss(ann_ctx* c, int prec, double wE, double wF, double* loss3) {
+    auto loss = [&]() {
+        ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
+        launch_train_loss(c->S, c->N, c->off_d, c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
+                          c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->train_loss, c->train_norm, c->train_delta,
+                          c->loss3.as<double>(), c->ce.as<double>(), c->lam.p, prec == ANN_FP64, c->stream);
+        ck(cudaGetLastError(), "loss kernel");
+        ck(cudaMemcpyAsync(loss3, c->loss3.p, 8 * 3, cudaMemcpyDeviceToHost, c->stream), "D2H loss");
+    };
+    loss();
+    int32_t* sh = status_host(c);
+    ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
+    ck(cudaStreamSynchronize(c->stream), "synchronize");
+    if (sh[0] != 0) {
+        finish_batch(c);   // a regrown list is rebuilt from the staged positions
+        loss();
+        ck(cudaStreamSynchronize(c->stream), "synchronize");
+    }
+    c->last_loss = loss3[0];
+    c->have_train = true; c->train_prec = prec; c->train_wE = wE; c->train_wF = wF;
+    c->train_staged = true; c->train_staged_prec = prec;
+}
+
 extern "C" {
 int ann_stats_reset(ann_ctx* c) {
     if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
@@ -140,27 +167,19 @@ int ann_train_forward(ann_ctx* c, int32_t nstruc, const int64_t* offs, const dou
         if (c->S > 0) ck(cudaMemcpyAsync(c->Eref.p, Eref, 8 * (size_t)c->S, cudaMemcpyHostToDevice, c->stream), "H2D Eref");
         if (c->N > 0) ck(cudaMemcpyAsync(c->Fref.p, Fref, 8 * 3 * (size_t)c->N, cudaMemcpyHostToDevice, c->stream), "H2D Fref");
         run_batch(c, prec, true);
-        // the loss right behind the E+F sequence, read back with the status word in one round trip;
-        // a status that is not clean goes through finish_batch (recover or throw) and the loss again
-        auto loss = [&]() {
-            ck(cudaMemsetAsync(c->loss3.p, 0, 8 * 4, c->stream), "memset");
-            launch_train_loss(c->S, c->N, c->off_d, c->sid.as<int32_t>(), c->Es.as<double>(), c->Fout.as<double>(),
-                              c->Eref.as<double>(), c->Fref.as<double>(), wE, wF, c->train_loss, c->train_norm, c->train_delta,
-                              c->loss3.as<double>(), c->ce.as<double>(), c->lam.p, prec == ANN_FP64, c->stream);
-            ck(cudaGetLastError(), "loss kernel");
-            ck(cudaMemcpyAsync(loss3, c->loss3.p, 8 * 3, cudaMemcpyDeviceToHost, c->stream), "D2H loss");
-        };
-        loss();
-        int32_t* sh = status_host(c);
-        ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
-        ck(cudaStreamSynchronize(c->stream), "synchronize");
-        if (sh[0] != 0) {
-            finish_batch(c);
-            loss();
-            ck(cudaStreamSynchronize(c->stream), "synchronize");
-        }
-        c->last_loss = loss3[0];
-        c->have_train = true; c->train_prec = prec; c->train_wE = wE; c->train_wF = wF;
+        train_loss(c, prec, wE, wF, loss3);
+    })
+}
+int ann_train_forward_staged(ann_ctx* c, double wE, double wF, int32_t prec, double* loss3) {
+    if (!c) return fail(c, ANN_ERR_ARG, "NULL context");
+    if (!loss3) return fail(c, ANN_ERR_ARG, "NULL argument");
+    ANN_TRY(c, {
+        set_device(c);
+        if (!c->train_staged)
+            throw ann_error(ANN_ERR_STATE, "ann_train_forward_staged needs the batch of a preceding ann_train_forward "
+                                           "(no other batch, E+F call, MD step or potential load since)");
+        run_staged(c, prec);
+        train_loss(c, prec, wE, wF, loss3);
     })
 }
 int ann_train_set_loss(ann_ctx* c, int32_t loss, int32_t norm, double delta) {

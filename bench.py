@@ -1,13 +1,14 @@
 """Benchmark: NNP energy+force atom-evaluations per second on one GB300 (and N replicas).
 
-Workload: 256 binary A/B structures, N ~ U{32..512} atoms each (~69.6k atoms), number density
+Workload: 256 binary A/B structures, N ~ U{32..512} atoms each (74,710 atoms), number density
 0.05 /A^3, rc = 6.5 A, 72 symmetry functions per atom (12 radial per species + 16 angular per
 species pair), 72-64-64-1 softplus networks; one packed batch per step (neighbour list,
 symmetry functions, networks, forces, virials, per-structure energies).
 
   value  : atom-evaluations/s with the batch resident in HBM (device-timed with CUDA events on
            the library's stream, L2 flushed by a 256 MiB write between steps, outside the timed
-           events), mixed precision (FP32 geometry/basis/forces, FP32 networks, FP64 sums).
+           events), mixed precision (FP32 geometry/basis/forces, BF16 hi/lo tensor-core networks
+           with FP32 accumulation, FP64 sums).
   e2e    : the same through ann_compute with the batch in page-locked host memory (H2D of
            positions/types/cells/offsets and D2H of energies/forces/virials inside the timed
            region, every step), wall-clock.
@@ -17,6 +18,10 @@ symmetry functions, networks, forces, virials, per-structure energies).
   training : structures/s of one training step (loss, adjoint, parameter gradient) on the
            64-structure batch with LJ labels, mixed and FP64 (secondary keys).
   md     : atom-steps/s and energy drift of velocity-Verlet MD on the 262,144-atom FCC Ar box.
+  parity / accuracy : the FP64 oracle on the whole batch against the FP64 GPU form (relative
+           errors) and the mixed form (meV/atom, meV/A).
+  precision_study / small_box / lammps / network_forms : the 32,000-atom ternary box (96-128-128-1),
+           the 108-atom argon box, the caller-list path and the three tensor-core operand forms.
 Multi-GPU: structures are independent, so each rank runs its own full batch (weak scaling);
 no collective on the data path, a barrier and a max over ranks around the timed region.
 """
@@ -316,11 +321,59 @@ def precision_study_leg(dev, steps=10, warmup=3):
     return out
 
 
+def small_box_leg(dev, steps=200, warmup=20):
+    """The 108-atom FCC argon box (3 x 3 x 3 cells, a = 5.26 A, 0.1 A jitter), 16 inputs, 16-20-20-1
+    tanh: the FP64 GPU form against the FP64 oracle (relative errors), the mixed form against the
+    oracle (meV/atom, meV/A), E+F throughput of both forms with the box resident (CUDA events, one
+    launch sequence per step: this size is launch-bound) and of the oracle on one host thread."""
+    import tempfile
+    from ann_gb300 import FP64, MIXED, Context
+    from ann_gb300 import workloads as WL
+    from ann_gb300.api import pack_batch
+    structs = WL.config1()
+    offs, posn, types, cell = pack_batch(structs)
+    N = int(offs[-1])
+    ctx = Context(device=dev, use_graphs=True)
+    try:
+        WL.make_potential(ctx, 1)
+        with tempfile.TemporaryDirectory() as td:
+            p = Path(td) / "pot.ann"
+            ctx.write(p)
+            pot_text = p.read_text()
+        ctx.load_text(pot_text)
+        sys.path.insert(0, str(ROOT / "tests"))
+        from oracle_lib import Oracle
+        orc = Oracle(timed=True).load_text(pot_text)
+        Eo, Fo, Wo, _, _ = Oracle().load_text(pot_text).compute(offs, posn, types, cell, nthreads=1)
+        reps, t0 = 0, time.perf_counter()
+        while reps < 3 or time.perf_counter() - t0 < 2.0:
+            orc.compute(offs, posn, types, cell, nthreads=1)
+            reps += 1
+        cpu = N * reps / (time.perf_counter() - t0)
+        out = {"workload": f"FCC Ar {N} atoms, rc 6 A, 16 inputs, 16-20-20-1 tanh",
+               "cpu_oracle_1_thread": cpu, "unit": "atom-evals/s"}
+        run = resident_timer(ctx, dev)
+        for name, prec in (("fp64", FP64), ("mixed", MIXED)):
+            E, F, Wv = ctx.compute(offs, posn, types, cell, precision=prec)
+            ms = float(np.median(run(offs, posn, types, cell, prec, steps, warmup)))
+            r = dict(_errors_vs(E, F, Eo, Fo, offs), ms_per_step=ms, atom_evals_per_s=N / (ms * 1e-3))
+            if prec == FP64:
+                r["e_rel"] = float(abs(E[0] - Eo[0]) / abs(Eo[0]))
+                r["f_rel_max"] = float(np.max(np.abs(F - Fo)) / np.max(np.abs(Fo)))
+                r["w_rel_max"] = float(np.max(np.abs(Wv - Wo)) / np.max(np.abs(Wo)))
+            out[name] = r
+    finally:
+        ctx.close()
+    return out
+
+
 def training_leg(dev, steps=10, warmup=3):
     """Training throughput on the 64-structure binary batch with Lennard-Jones labels: one
     ann_train_forward + ann_train_backward (loss, adjoint, parameter gradient) + ann_adam_step
     (optimiser step on the resident parameters) per step: host arrays and labels in, the loss out,
-    the gradient kept on the device for the optimiser; wall-clock per step."""
+    the gradient kept on the device for the optimiser; wall-clock per step. The staged form is the
+    reference trainer's loop (neighbour lists and symmetry functions of the training set built once,
+    nnptefr2.cpp:2690-2703): ann_train_forward_staged in place of ann_train_forward."""
     from ann_gb300 import FP64, MIXED, Context
     from ann_gb300 import workloads as WL
     from ann_gb300.api import pack_batch
@@ -335,16 +388,27 @@ def training_leg(dev, steps=10, warmup=3):
                        "loss = mean (dE/N)^2 + 0.1 mean |dF|^2/3, Adam step on the device",
            "unit": "structures/s", "nparams": int(ctx.nparams)}
     p0 = ctx.get_params()
-    for name, prec in (("mixed", MIXED), ("fp64", FP64)):
+    # "<prec>": every step sends the batch and its labels and builds lists and symmetry functions;
+    # "<prec>_staged": the reference trainer's loop, lists and symmetry functions built once for the
+    # training set (before the timed steps), each step networks + forces + loss + adjoint + gradient
+    # + optimiser step (ann_train_forward_staged)
+    for name, prec, staged in (("mixed", MIXED, False), ("mixed_staged", MIXED, True), ("fp64", FP64, False),
+                               ("fp64_staged", FP64, True)):
         ctx.set_params(p0)
         ctx.adam_init(1e-4, 0.9, 0.999, 1e-16)
-        for _ in range(warmup):
-            ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
+
+        def fwd(first):
+            if staged and not first:
+                return ctx.train_forward_staged(1.0, 0.1, precision=prec)
+            return ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
+
+        for k in range(warmup):
+            fwd(k == 0)
             ctx.train_backward(download=False)
             ctx.adam_step()
         t0 = time.perf_counter()
         for _ in range(steps):
-            loss = ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec)
+            loss = fwd(False)
             ctx.train_backward(download=False)
             ctx.adam_step()
         ctx.synchronize()
@@ -437,13 +501,14 @@ def main():
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the built-in launch shapes (no autotuner launches before the timed steps, e.g. for "
                          "ncu captures that select launches by position)")
-    ap.add_argument("--only", choices=["training", "md", "lammps", "precision"],
+    ap.add_argument("--only", choices=["training", "md", "lammps", "precision", "small"],
                     help="run one secondary leg alone with --steps / --warmup and print its JSON (for profiling)")
     args = ap.parse_args()
     rank, world, local = _env_rank()
     W_ = max(args.warmup, 3)
     if args.only:
-        leg = {"training": training_leg, "md": md_leg, "lammps": lammps_leg, "precision": precision_study_leg}[args.only]
+        leg = {"training": training_leg, "md": md_leg, "lammps": lammps_leg, "precision": precision_study_leg,
+               "small": small_box_leg}[args.only]
         print(json.dumps({args.only: leg(local if world > 1 else 0, steps=args.steps, warmup=args.warmup)}))
         return
 
@@ -616,6 +681,7 @@ def main():
         line["md"] = md_leg(dev)
         line["lammps"] = lammps_leg(dev)
         line["precision_study"] = precision_study_leg(dev)
+        line["small_box"] = small_box_leg(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(offs, posn, types, cell, pot_text)
     if rank == 0:

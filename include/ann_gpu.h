@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define ANN_GPU_ABI_VERSION 3
+#define ANN_GPU_ABI_VERSION 4
 
 enum ann_status {
     ANN_OK = 0,
@@ -203,6 +203,16 @@ int ann_train_forward(ann_ctx* ctx, int32_t nstruc, const int64_t* atom_offsets,
                       const int32_t* type, const double* cell, const double* energy_ref,
                       const double* forces_ref, double w_energy, double w_force, int32_t precision,
                       double* loss3);
+/* The same forward pass over the structures and labels of the preceding ann_train_forward, whose
+ * neighbour rows, per-type atom lists and symmetry functions stay on the device: the reference
+ * trainer builds each structure's neighbour list and symmetry functions once, before optimising
+ * (nnptefr2.cpp:2690-2703), and every step evaluates the networks on the stored symm
+ * (error_cost_o1, nnptefr2.cpp:1321-1374). Each call runs the networks, the forces, the
+ * per-structure sums and the loss with the current parameters (after optimiser steps,
+ * ann_set_params or new input scaling). ANN_ERR_STATE if no ann_train_forward preceded it, if
+ * another batch, E+F call, MD step or potential load came in between, or if precision differs
+ * from that call's. ann_train_backward follows it as it follows ann_train_forward.             */
+int ann_train_forward_staged(ann_ctx* ctx, double w_energy, double w_force, int32_t precision, double* loss3);
 /* The energy term's loss and normalisation for later ann_train_forward calls (NNPTEFR,
  * nnptefr2.cpp:1339-1368, normalisation 606-612). For structure s with dU = (E_s - Eref_s) normt(N_s):
  * MSE 1/2 dU^2, MAE |dU|, HUBER delta^2 (sqrt(1 + (dU/delta)^2) - 1), ASINH delta^2 (1 - sqrt(1 + a^2)

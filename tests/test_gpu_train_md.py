@@ -258,6 +258,61 @@ def test_adam_steps_on_device(ctx, tmp_path):
         other.close()
 
 
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_staged_training_steps_equal_full_steps(ctx, tmp_path, prec):
+    """ann_train_forward_staged (the neighbour rows and symmetry functions of the preceding
+    ann_train_forward kept on the device, as the reference trainer keeps each structure's symm)
+    gives the losses, gradients and Adam trajectory of full ann_train_forward calls on the same
+    batch: to 1e-12 in FP64, to 1e-5 in the mixed form (FP32 force atomics add in varying order)."""
+    text = cases.config_potential(ctx, 3, tmp_path)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    p0 = ctx.get_params()
+    tol = 1e-12 if prec == FP64 else 1e-5
+
+    def run(staged):
+        ctx.set_params(p0)
+        ctx.adam_init(1e-3, 0.9, 0.999, 1e-16)
+        losses, grads = [], []
+        for k in range(4):
+            if staged and k > 0:
+                losses.append(ctx.train_forward_staged(1.0, 0.1, precision=prec))
+            else:
+                losses.append(ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=prec))
+            grads.append(ctx.train_backward())
+            ctx.adam_step()
+        return np.array(losses), np.array(grads), ctx.get_params()
+
+    La, Ga, Pa = run(False)
+    Lb, Gb, Pb = run(True)
+    assert np.allclose(Lb, La, rtol=tol, atol=1e-15)
+    assert np.abs(Gb - Ga).max() <= tol * np.abs(Ga).max()
+    if prec == FP64:   # (mixed: Adam's first steps are sign steps, so last-bit noise in tiny gradients moves them by lr)
+        assert np.allclose(Pb, Pa, rtol=tol, atol=1e-15)
+    # new parameters set from the host between staged steps are used
+    ctx.set_params(p0)
+    l1 = ctx.train_forward_staged(1.0, 0.1, precision=prec)
+    assert np.allclose(l1, La[0], rtol=tol, atol=1e-15)
+    ctx.load_text(text)
+
+
+def test_staged_training_refused_without_its_batch(ctx, tmp_path):
+    ANN_ERR_STATE = 6
+    cases.config_potential(ctx, 3, tmp_path)
+    offs, posn, types, cell, Eref, Fref = _train_case()
+    with pytest.raises(AnnError) as e:          # a freshly loaded potential: nothing staged
+        ctx.train_forward_staged(1.0, 0.1, precision=FP64)
+    assert e.value.code == ANN_ERR_STATE
+    ctx.train_forward(offs, posn, types, cell, Eref, Fref, 1.0, 0.1, precision=FP64)
+    with pytest.raises(AnnError) as e:          # the other precision
+        ctx.train_forward_staged(1.0, 0.1, precision=MIXED)
+    assert e.value.code == ANN_ERR_STATE
+    ctx.train_forward_staged(1.0, 0.1, precision=FP64)
+    ctx.compute(offs, posn, types, cell, precision=FP64)
+    with pytest.raises(AnnError) as e:          # an E+F call in between replaced the staged state
+        ctx.train_forward_staged(1.0, 0.1, precision=FP64)
+    assert e.value.code == ANN_ERR_STATE
+
+
 def _decay(name, gamma, t, alpha, period):
     """opt::Decay::step (opt/decay.cpp:42-62)."""
     return {"CONST": gamma, "EXP": gamma * (1.0 - alpha), "GAUSS": gamma * (1.0 - 2.0 * alpha * t),

@@ -39,7 +39,7 @@ def test_library_exports_every_declared_symbol(lib):
     for name in declared:
         assert hasattr(lib, name), name
     assert set(declared) == set(ABI_SYMBOLS), set(declared) ^ set(ABI_SYMBOLS)
-    assert lib.ann_abi_version() == 3
+    assert lib.ann_abi_version() == 4
 
 
 def test_no_device_fails_cleanly(lib):
