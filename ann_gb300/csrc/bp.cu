@@ -17,12 +17,14 @@
 //     zeta=2^k) the reference's exp(-(rij^2+rik^2)/eta^2) factorises into D_g(j) D_g(k) and
 //     |1/2 +- cos/2|^zeta comes from a squaring chain (symmetry functions) or from a degree-8
 //     polynomial in cos (force pass), so no transcendental is evaluated per triplet. There the
-//     neighbours of a type range are split into chunks of 32 and lane L owns element L of every
-//     chunk; a chunk's triangle and each pair of chunks are walked along rotations (partner =
-//     own + step mod n), so the lane's own record stays in registers. The generic path and the
-//     tangent pass hand out (j,k) triplets to lanes instead.
+//     neighbours of a type range are split into ceil(n/32) chunks of nearly equal size and lane L
+//     owns element L of every chunk; a chunk's triangle and each pair of chunks are walked along
+//     rotations (partner = own + step mod n), so the lane's own record stays in registers. Lanes
+//     without an element, and partner slots past a chunk's end, read a zero record (index cap),
+//     whose terms vanish, so the walk carries no per-step masks. The generic path and the tangent
+//     pass hand out (j,k) triplets to lanes instead.
 //  4. force pass: per triplet the vectors v_j = -dE_i/dr_ij, v_k = -dE_i/dr_ik are summed per
-//     neighbour. Fast path: lanes own neighbours (chunks of 32 per type range) and visit their
+//     neighbour. Fast path: lanes own neighbours (the chunks above) and visit their
 //     partners along a rotation, keeping their own sums in registers and shuffling the partner's
 //     share to its owner lane (no atomics). Generic path: triplets along diagonals with shared
 //     atomics. F_i = sum_j v_j, F_j -= v_j (Newton's third law, nnp.cpp:491,509-516) and the

@@ -659,7 +659,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps, "warmup": W_,
             "ms_per_step": tmax, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "natoms": N, "nstruc": len(structs), "precision": "mixed (FP32 basis/forces/networks, FP64 energy sums)",
+            "config": {"workload": WORKLOAD, "natoms": N, "nstruc": len(structs), "precision": "mixed (FP32 basis/forces, BF16 hi/lo tensor-core networks with FP32 accumulation, FP64 energy sums)",
                        "l2": "flushed between steps (256 MiB write outside the timed events)", "graphs": True, "sm_count": nsm,
                        "launch_shapes": {"mixed": dict(shapes, ms=tuned["ms"], ms_default=tuned["ms_default"]),
                                          "fp64": {k: tuned64[k] for k in SHAPE_KEYS}},
