@@ -42,7 +42,7 @@ static void upload_params(ann_ctx* c, ParamSet<real>& P) {
 static void reset_graph(ann_ctx* c) {
     for (int k = 0; k < 3; ++k) {
         if (c->gexec[k]) { cudaGraphExecDestroy(c->gexec[k]); c->gexec[k] = nullptr; }
-        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, -1, 0};
+        c->gkey[k] = GraphKey{-1, -1, -1, -1, -1, -1, -1, -1, 0, -1};
     }
 }
 void drop_graphs(ann_ctx* c) { reset_graph(c); }
@@ -120,7 +120,7 @@ static void ensure_batch_buffers(ann_ctx* c) {
     c->pos4.ensure(sizeof(float4) * N); c->abin.ensure(4 * N); c->abc.ensure(4 * N); c->am.ensure(4 * N); c->aslot.ensure(4 * N);
     c->bcount.ensure(4 * (size_t)(c->nbins_cap + 1)); c->bstart.ensure(4 * (size_t)(c->nbins_cap + 1));
     c->bidx.ensure(4 * N); c->bm.ensure(4 * N); c->bpos4.ensure(sizeof(float4) * N); c->bposd.ensure(sizeof(double) * 3 * N);
-    c->nbins_total.ensure(4); c->nn.ensure(4 * N); c->ntc.ensure(4 * (size_t)N * T);
+    c->nn.ensure(4 * N); c->ntc.ensure(4 * (size_t)N * T);
     c->nj.ensure(4 * (size_t)N * c->cap); c->nimg.ensure(4 * (size_t)N * c->cap); c->nr.ensure(sizeof(Vec4d) * (size_t)N * c->cap);
     c->scan_tmp.ensure(4 * scan_tmp_ints(c->nbins_cap + 1)); c->counter.ensure(16); c->status.ensure(4 * 8);
     c->G.ensure(rb * (size_t)N * std::max(imax, 1)); c->dEdG.ensure(rb * (size_t)N * std::max(imax, 1));
@@ -140,6 +140,8 @@ static void stage_offsets(ann_ctx* c, int nstruc, const int64_t* atom_offsets) {
     c->N = (int)atom_offsets[nstruc];
     c->off_h.assign(nstruc + 1, 0);
     for (int s = 0; s <= nstruc; ++s) c->off_h[s] = (int32_t)atom_offsets[s];
+    c->max_nat = 0;
+    for (int s = 0; s < nstruc; ++s) c->max_nat = std::max(c->max_nat, c->off_h[s + 1] - c->off_h[s]);
     // chunks of the per-structure reductions
     c->rchunk_h.clear();
     c->rschunk_h.assign(nstruc + 1, 0);
@@ -162,7 +164,11 @@ void leave_md(ann_ctx* c) {
 
 void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* posn, const int32_t* type, const double* cell, bool device_src) {
     if (!c->have_pot) throw ann_error(ANN_ERR_STATE, "no potential loaded");
-    stage_offsets(c, nstruc, offs);
+    // a batch with the offsets of the staged one (a training or MD-like loop) keeps its offset and
+    // reduction tables and its per-atom structure index on the device, unless a buffer moved since
+    bool same = c->have_batch && offs && nstruc == c->S && c->tables_gen == g_alloc_gen.load() && !c->off_h.empty();
+    for (int s = 0; same && s <= nstruc; ++s) same = (offs[s] == (int64_t)c->off_h[s]);
+    if (!same) stage_offsets(c, nstruc, offs);
     if (c->N > 0 && (!posn || !type)) throw ann_error(ANN_ERR_ARG, "posn/type is NULL");
     if (nstruc > 0 && !cell) throw ann_error(ANN_ERR_ARG, "cell is NULL");
     // types and positions are checked on the device (ST_BAD_TYPE, ST_NONFINITE), cells here
@@ -175,9 +181,11 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
         }
     }
     if (c->cap == 0) c->cap = estimate_cap(c, device_src ? nullptr : cell);
+    const uint64_t gen0 = g_alloc_gen.load();
     ensure_batch_buffers(c);
+    if (g_alloc_gen.load() != gen0) same = false;
     const cudaMemcpyKind k = device_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    {
+    if (!same) {
         // offsets, the reduction chunks and the structures' first chunks in one copy (pageable
         // copies return once the host data is staged). The chunk buffers are sized by the bound
         // S + N / RED_CHUNK + 1, so that a captured graph's pointers stay valid for every batch
@@ -194,9 +202,10 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
         c->off_d = c->tables.as<int32_t>();
         c->rchunk_d = c->off_d + o_ch;
         c->rschunk_d = c->off_d + o_sc;
+        if (c->N > 0) launch_fill_sid(c->S, c->off_d, c->sid.as<int32_t>(), c->stream);
+        c->tables_gen = g_alloc_gen.load();
     }
     if (c->N > 0) {
-        launch_fill_sid(c->S, c->off_d, c->sid.as<int32_t>(), c->stream);
         ck(cudaMemcpyAsync(c->pos.p, posn, sizeof(double) * 3 * (size_t)c->N, k, c->stream), "copy positions");
         ck(cudaMemcpyAsync(c->type.p, type, sizeof(int32_t) * (size_t)c->N, k, c->stream), "copy types");
     }
@@ -213,10 +222,11 @@ static NbrArgs nbr_args(ann_ctx* c, double rc) {
     a.off = c->off_d; a.cell = c->cell.as<double>(); a.pos = c->pos.as<double>(); a.type = c->type.as<int32_t>(); a.sid = c->sid.as<int32_t>();
     a.grid_per_sm = c->tune_nbr;
     a.nsm = c->nsm;
+    a.max_nat = c->max_nat;
     a.geo = c->geo.as<StrucGeo>(); a.pos4 = c->pos4.as<float4>(); a.abin = c->abin.as<int32_t>(); a.abc = c->abc.as<int32_t>(); a.am = c->am.as<int32_t>();
     a.aslot = c->aslot.as<int32_t>(); a.bcount = c->bcount.as<int32_t>(); a.bstart = c->bstart.as<int32_t>(); a.bidx = c->bidx.as<int32_t>();
     a.bm = c->bm.as<int32_t>(); a.bpos4 = c->bpos4.as<float4>(); a.bposd = c->bposd.as<double>(); a.nbins_cap = c->nbins_cap;
-    a.nbins_total = c->nbins_total.as<int32_t>(); a.nn = c->nn.as<int32_t>(); a.ntc = c->ntc.as<int32_t>(); a.nj = c->nj.as<int32_t>();
+    a.nn = c->nn.as<int32_t>(); a.ntc = c->ntc.as<int32_t>(); a.nj = c->nj.as<int32_t>();
     a.nimg = c->nimg.as<int32_t>(); a.nr = c->nr.p; a.scan_tmp = c->scan_tmp.as<int32_t>(); a.counter = c->counter.as<uint32_t>();
     a.status = c->status.as<int32_t>();
     return a;
@@ -310,12 +320,15 @@ static void run_sequence(ann_ctx* c, int prec, bool forces, int mode) {
     // shared-memory needs of this batch (neighbour rows are staged per warp)
     const size_t need_bp = bp_smem_bytes(c->plan.pot, c->cap, prec == ANN_FP64) + 1024;
     const size_t need_mlp = mlp_smem_bytes(c->plan.pot, prec == ANN_FP64, false) + 1024;
+    if (mode == SEQ_BUILD && nbr_smem_bytes(c->cap, prec == ANN_FP64) + 1024 > (size_t)c->max_smem)
+        throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity " + std::to_string(c->cap) + " exceeds the neighbour search's shared memory");
     if (need_bp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_CAPACITY, "neighbour capacity " + std::to_string(c->cap) + " needs " + std::to_string(need_bp) +
                                               " B of shared memory per block (device limit " + std::to_string(c->max_smem) + ")");
     if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
-    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), c->md_ready ? 1 : 0, g_alloc_gen.load()};
+    const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), c->md_ready ? 1 : 0, g_alloc_gen.load(),
+                       nbr_local_binning(c->max_nat) ? 1 : 0};
     const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
     const int gs = mode;
     if (graphs) {
@@ -460,7 +473,7 @@ int ann_destroy(ann_ctx* c) {
     reset_graph(c);
     c->pf.release(); c->pd.release();
     for (DevBuf* b : {&c->poff, &c->cell, &c->pos, &c->type, &c->sid, &c->geo, &c->pos4, &c->abin, &c->abc, &c->am, &c->aslot,
-                      &c->bcount, &c->bstart, &c->bidx, &c->bm, &c->bpos4, &c->bposd, &c->nbins_total, &c->nn, &c->ntc, &c->nj, &c->nimg,
+                      &c->bcount, &c->bstart, &c->bidx, &c->bm, &c->bpos4, &c->bposd, &c->nn, &c->ntc, &c->nj, &c->nimg,
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad, &c->gpart,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,

@@ -91,9 +91,10 @@ struct GraphKey {
     int S, N, cap, prec, forces, nbins, nchunks;
     int md;         // MD mode: list cutoff rc + skin, refreshed between rebuilds
     uint64_t gen;   // g_alloc_gen at capture
+    int local_bins; // structures binned one block each (nbr_local_binning of the largest structure)
     bool operator==(const GraphKey& o) const {
         return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins && nchunks == o.nchunks &&
-               md == o.md && gen == o.gen;
+               md == o.md && gen == o.gen && local_bins == o.local_bins;
     }
 };
 
@@ -131,6 +132,8 @@ struct ann_ctx {
     DevBuf poff;
     // batch
     int S = 0, N = 0;
+    int max_nat = 0;                // atoms of the largest structure of the staged batch
+    uint64_t tables_gen = ~0ull;    // g_alloc_gen when the offset tables and sid were last uploaded
     bool have_batch = false;
     std::vector<int32_t> off_h, rchunk_h, rschunk_h, tables_h;
     DevBuf tables, cell, pos, type, sid, rpartial;
@@ -139,7 +142,7 @@ struct ann_ctx {
     const int32_t* rschunk_d = nullptr;    // first chunk of each structure [S+1] (inside tables)
     // neighbour list
     int cap = 0, nbins_cap = 0;
-    DevBuf geo, pos4, abin, abc, am, aslot, bcount, bstart, bidx, bm, bpos4, bposd, nbins_total, nn, ntc, nj, nimg, nr, scan_tmp, counter, status;
+    DevBuf geo, pos4, abin, abc, am, aslot, bcount, bstart, bidx, bm, bpos4, bposd, nn, ntc, nj, nimg, nr, scan_tmp, counter, status;
     // per atom / structure
     DevBuf G, dEdG, Eatom, F, W, Es, Ws, Fout, tcount, tstart, tlist;
     int last_prec = -1;
@@ -148,7 +151,7 @@ struct ann_ctx {
     // graphs of the E+F sequence: [SEQ_BUILD] with the list build, [SEQ_REFRESH] with the Verlet-list
     // refresh (MD), [SEQ_STAGED] from the networks on (neighbour rows and G of the staged training batch)
     cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
-    GraphKey gkey[3] = {{-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}, {-1, -1, -1, -1, -1, -1, -1, 0}};
+    GraphKey gkey[3] = {{-1, -1, -1, -1, -1, -1, -1, -1, 0, -1}, {-1, -1, -1, -1, -1, -1, -1, -1, 0, -1}, {-1, -1, -1, -1, -1, -1, -1, -1, 0, -1}};
     // training
     DevBuf Eref, Fref, loss3, ce, lam, U, grad, gpart;   // gpart: per-block gradient sums of the training pass
     bool have_train = false;

@@ -16,7 +16,10 @@ struct StrucGeo {          // per structure (FP64), filled on the device by k_st
     int32_t sten[3];       // stencil half-width in bins
     int32_t bin0;          // first global bin of the structure
     int32_t atom0, natoms;
-    int32_t pad;
+    int32_t pad;           // 1: singular or non-finite cell (no search)
+    int32_t ortho;         // 1: lattice vectors along the axes (R diagonal): stencil rows are pruned
+    float labs[3];         // |R_dd| of an orthogonal cell (A)
+    float Rf[9], Rif[9];   // FP32 copies of R and R^-1 (the FP32 candidate test and row pruning)
 };
 
 // ---- neighbour list (neighbor.cu) ----------------------------------------------------------
@@ -41,7 +44,6 @@ struct NbrArgs {
     float4* bpos4;                   // [N] positions in bin order
     double* bposd;                   // [3N] FP64 positions in bin order
     int32_t nbins_cap;
-    int32_t* nbins_total;            // [1]
     int32_t* nn;                     // [N] entries per atom
     int32_t* ntc;                    // [N*T] entries per atom and neighbour type (type-sorted rows)
     int32_t* nj;                     // [N*cap]
@@ -52,7 +54,13 @@ struct NbrArgs {
     int32_t* status;                 // [8]
     int32_t grid_per_sm;             // host side: blocks per SM of the search grid (0: 16)
     int32_t nsm;                     // host side: streaming multiprocessors of the device
+    int32_t max_nat;                 // host side: atoms of the batch's largest structure
 };
+// the batch's structures are binned one block each in shared memory (else by the global chain:
+// atom bins, scan, scatter, sort)
+bool nbr_local_binning(int max_nat);
+// shared memory of a neighbour-search block for row capacity cap
+size_t nbr_smem_bytes(int cap, bool fp64);
 void launch_neighbors(const NbrArgs& a, bool fp64, cudaStream_t st);
 // recompute nr from positions and stored images (Verlet-list refresh between rebuilds)
 void launch_refresh_geometry(const NbrArgs& a, bool fp64, cudaStream_t st);
