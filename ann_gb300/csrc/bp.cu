@@ -156,6 +156,7 @@ struct RectIter {
 };
 
 // ---------------------------------------------------------------- shared-memory layout of one warp
+constexpr int TS_ZERO = 64;   // chunk-task scratch: 2 x 32 slots, then the zero record
 template <typename real, int NG, int PASS>
 struct WarpMem {
     typedef typename V4<real>::T R4;
@@ -169,6 +170,12 @@ struct WarpMem {
     int32_t *stagej, *stagej2;   // staged neighbour indices (two buffers); after compaction the
                                  // current one holds j per record (-1: no Newton-3rd share, FORCE)
     uint64_t* bar;       // two mbarriers, one per staging buffer
+    // chunk-task scratch (symmetry and force passes): the partner chunk twice over, partner slots
+    // without an element as zeros, so that rotation step st reads slot lane + st with no wrap; a
+    // zero record at TS_ZERO. Force pass: the owning chunk twice over (og), for the senders' records
+    R4* sg;
+    real* sd;
+    R4* og;
     static constexpr int NDP = 2 * NG;
     static __host__ __device__ size_t align(size_t x, size_t a) { return (x + a - 1) / a * a; }
     static __host__ __device__ size_t layout(int cap, int imax, WarpMem* w, unsigned char* base) {
@@ -188,6 +195,10 @@ struct WarpMem {
         const size_t o_sj = take(sizeof(int32_t) * cap, 16);
         const size_t o_sj2 = take(sizeof(int32_t) * cap, 16);
         const size_t o_bar = take(16, 16);
+        const bool tasks = (PASS != PASS_JVP);
+        const size_t o_sg = tasks ? take(sizeof(R4) * (TS_ZERO + 1), 32) : 0;
+        const size_t o_sd = tasks ? take(sizeof(real) * NDP * (TS_ZERO + 1), 16) : 0;
+        const size_t o_og = (PASS == PASS_FORCE) ? take(sizeof(R4) * TS_ZERO, 32) : 0;
         if (w) {
             w->geo = reinterpret_cast<R4*>(base + o_geo); w->stage = reinterpret_cast<R4*>(base + o_stage);
             w->tg = reinterpret_cast<R4*>(base + o_tg); w->dp = reinterpret_cast<real*>(base + o_dp);
@@ -197,6 +208,8 @@ struct WarpMem {
             w->stagej = reinterpret_cast<int32_t*>(base + o_sj);
             w->stagej2 = reinterpret_cast<int32_t*>(base + o_sj2);
             w->bar = reinterpret_cast<uint64_t*>(base + o_bar);
+            w->sg = reinterpret_cast<R4*>(base + o_sg); w->sd = reinterpret_cast<real*>(base + o_sd);
+            w->og = reinterpret_cast<R4*>(base + o_og);
         }
         return align(off, 128);
     }
@@ -337,6 +350,58 @@ __device__ __forceinline__ void angular_poly(const real* dE, const int32_t* slot
 // the second visit of a pair in the last step of an even triangle) reads the zero record at index
 // `zr`: D = D' = 0 and a zero unit vector make every term of the triplet exactly zero, so the loop
 // carries no per-step masking of its results. Lanes beyond the owning chunk own the zero record.
+// the task scratch for a partner chunk of n elements at qb, of which the first nv have records:
+// slot k < 2n holds element k mod n (zeros from nv on); og (force pass, rectangles) likewise the
+// owning chunk at p0. Slots at and beyond 2n keep finite older values: only lanes beyond the owning
+// chunk read them, and those lanes own the zero record, so their terms vanish.
+template <typename WM>
+__device__ __forceinline__ void fill_task_scratch(const WM& w, int lane, int qb, int n, int nv, int p0, bool own) {
+    typedef typename WM::R4 R4;
+    constexpr int NDP = WM::NDP;
+    typedef typename std::remove_pointer<decltype(w.sd)>::type real;
+    for (int k = lane; k < 2 * n; k += 32) {
+        const int m = (k < n) ? k : k - n;
+        R4 g;
+        real d[NDP];
+        if (m < nv) {
+            g = w.geo[qb + m];
+#pragma unroll
+            for (int q = 0; q < NDP; ++q) d[q] = w.dp[(qb + m) * NDP + q];
+        } else {
+            g.x = g.y = g.z = g.w = real(0);
+#pragma unroll
+            for (int q = 0; q < NDP; ++q) d[q] = real(0);
+        }
+        w.sg[k] = g;
+#pragma unroll
+        for (int q = 0; q < NDP; ++q) w.sd[k * NDP + q] = d[q];
+        if (own) w.og[k] = w.geo[p0 + m];
+    }
+    __syncwarp();
+}
+
+// one rotation step of a force-pass chunk task: the triplet of the lane's own element with the
+// element at e, and the share sent by lane src (whose element es is the lane's partner's sender)
+template <typename real, int NG, bool PACKED, bool TRI, typename WM, typename R4>
+__device__ __forceinline__ void force_step(const WM& w, const R4& ga, const DampRec<real, NG>& da, const real (&al)[NG][9],
+                                           const uint64_t (&alp)[9], int e, int es, int src, real& ca, real& cb, real (&sa)[3],
+                                           real (&sb)[3]) {
+    constexpr int NDP = 2 * NG;
+    const R4 gb = w.sg[e];                             // partner (task scratch slot)
+    DampRec<real, NG> db;
+    db.load(w.sd + e * NDP);
+    const R4 gs = TRI ? w.sg[es] : w.og[es];           // the sending lane's own element
+    real cj, bj, ck, bk;
+    if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, cj, bj, ck, bk);
+    else triplet_force<real, NG>(ga, da, gb, db, al, cj, bj, ck, bk);
+    ca += cj;
+    sa[0] += bj * gb.x; sa[1] += bj * gb.y; sa[2] += bj * gb.z;
+    const real rc = __shfl_sync(0xffffffffu, ck, src & 31);
+    const real rb = __shfl_sync(0xffffffffu, bk, src & 31);
+    if (TRI) { ca += rc; sa[0] += rb * gs.x; sa[1] += rb * gs.y; sa[2] += rb * gs.z; }
+    else { cb += rc; sb[0] += rb * gs.x; sb[1] += rb * gs.y; sb[2] += rb * gs.z; }
+}
+
 template <typename real, int NG, int PASS, bool TRI>
 __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, const real (&al)[NG][9], int lane,
                                            int p0, int np, int q0, int nq, int zr) {
@@ -357,34 +422,23 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     }
     const int n = np;
     const int steps = TRI ? np / 2 : np;      // triangle: steps 1..n/2, rectangle: 0..n-1
-    const int qb = TRI ? p0 : q0;
-    int part = TRI ? lane + 1 : lane;         // partner slot (lane + step) mod n
-    if (part >= n) part -= n;
+    // the partner chunk (the owning one for a triangle) twice over in the task scratch, so that
+    // step st reads slot lane + st: partner (lane + st) mod n, or zeros where Q has no element; the
+    // sender of step st, lane (lane - st) mod n, owns slot n + lane - st of the owning chunk
+    fill_task_scratch(w, lane, TRI ? p0 : q0, n, TRI ? n : nq, p0, !TRI);
     int src = TRI ? lane - 1 : lane;          // sending lane (lane - step) mod n
     if (src < 0) src += n;
     if (src >= n) src = 0;                    // lanes beyond the chunk: any element of it
-    const int last_half = (TRI && (n & 1) == 0) ? steps : -1;   // even triangle: the last step visits pairs twice
+    // an even triangle's last step (n/2) visits every pair twice: lanes below n/2 take it, apart
+    // from the loop so that the loop body needs no per-lane test
+    const bool peel = TRI && (n & 1) == 0 && steps > 0;
+    int st = TRI ? 1 : 0;
 #pragma unroll 1
-    for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
-        // non-owning lanes always read the zero record (their partner slot may lie outside the chunk)
-        const bool valid = ownP && (TRI ? (st != last_half || lane < steps) : part < nq);
-        const int e = valid ? qb + part : zr;
-        const R4 gb = w.geo[e];
-        DampRec<real, NG> db;
-        db.load(w.dp + e * NDP);
-        const R4 gs = w.geo[p0 + src];                     // the sending lane's own element
-        real cj, bj, ck, bk;
-        if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, cj, bj, ck, bk);
-        else triplet_force<real, NG>(ga, da, gb, db, al, cj, bj, ck, bk);
-        ca += cj;
-        sa[0] += bj * gb.x; sa[1] += bj * gb.y; sa[2] += bj * gb.z;
-        const real rc = __shfl_sync(0xffffffffu, ck, src & 31);
-        const real rb = __shfl_sync(0xffffffffu, bk, src & 31);
-        if (TRI) { ca += rc; sa[0] += rb * gs.x; sa[1] += rb * gs.y; sa[2] += rb * gs.z; }
-        else { cb += rc; sb[0] += rb * gs.x; sb[1] += rb * gs.y; sb[2] += rb * gs.z; }
-        part = (part + 1 == n) ? 0 : part + 1;
+    for (; st < (TRI ? steps + (peel ? 0 : 1) : steps); ++st) {
+        force_step<real, NG, PACKED, TRI>(w, ga, da, al, alp, lane + st, n + lane - st, src, ca, cb, sa, sb);
         src = (src == 0) ? n - 1 : src - 1;
     }
+    if (peel) force_step<real, NG, PACKED, TRI>(w, ga, da, al, alp, lane < steps ? lane + st : TS_ZERO, n + lane - st, src, ca, cb, sa, sb);
     if (ownP) {
         w.ax[p0 + lane] += ca * ga.x + sa[0]; w.ay[p0 + lane] += ca * ga.y + sa[1]; w.az[p0 + lane] += ca * ga.z + sa[2];
     }
@@ -394,8 +448,51 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     }
 }
 
+// one rotation step of a symmetry-function chunk task: the triplet of the lane's own element (ga,
+// da) with the element at e. FP32 with at most two damping groups: the slot pair (lambda = +1,
+// lambda = -1) of each zeta in one packed register, (|1/2 + cos/2|^zeta, |1/2 - cos/2|^zeta) by
+// packed squaring, accumulated by packed FMA
+template <typename real, int NG, int S, typename WM, typename R4>
+__device__ __forceinline__ void symm_step2(const WM& w, const R4& ga, const DampRec<real, NG>& da, int e, uint64_t (&acc2)[S / 2]) {
+    constexpr int NDP = 2 * NG;
+    const R4 gb = w.sg[e];                 // partner (task scratch slot)
+    DampRec<real, NG> db;
+    db.load(w.sd + e * NDP);
+    const float cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
+    uint64_t pw[4];
+    pw[0] = pk2(fabsf(0.5f + 0.5f * cs), fabsf(0.5f - 0.5f * cs));
+    pw[1] = mul2(pw[0], pw[0]); pw[2] = mul2(pw[1], pw[1]); pw[3] = mul2(pw[2], pw[2]);
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+        const float DD = da.D(g) * db.D(g);          // zero for the zero record
+        const uint64_t D2 = pk2(DD, DD);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc2[g * 4 + q] = fma2(pw[q], D2, acc2[g * 4 + q]);
+    }
+}
+template <typename real, int NG, int S, typename WM, typename R4>
+__device__ __forceinline__ void symm_step(const WM& w, const R4& ga, const DampRec<real, NG>& da, int e, real (&acc)[S]) {
+    constexpr int NDP = 2 * NG;
+    const R4 gb = w.sg[e];                 // partner (task scratch slot)
+    DampRec<real, NG> db;
+    db.load(w.sd + e * NDP);
+    const real cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
+    const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
+    real pp[4], pm[4];
+    pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
+    pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+        const real DD = da.D(g) * db.D(g);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
+    }
+}
+
 // The same chunk tasks for the symmetry functions of a fast-path block: the lane's own neighbour
-// stays in registers and only the partner's record is read per pair; acc[s] collects slot s.
+// stays in registers and only the partner's record is read per pair; acc[s] collects slot s. The
+// partner walk is that of force_task (zero record for lanes beyond the chunk, an even triangle's
+// last step apart from the loop).
 template <typename real, int NG, int S, int PASS, bool TRI>
 __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real (&acc)[S], int lane, int p0, int np, int q0, int nq,
                                           int zr) {
@@ -408,36 +505,17 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
     da.load(w.dp + ea * NDP);
     const int n = np;
     const int steps = TRI ? np / 2 : np;
-    const int qb = TRI ? p0 : q0;
-    int part = TRI ? lane + 1 : lane;
-    if (part >= n) part -= n;
-    const int last_half = (TRI && (n & 1) == 0) ? steps : -1;
+    fill_task_scratch(w, lane, TRI ? p0 : q0, n, TRI ? n : nq, p0, false);
+    const bool peel = TRI && (n & 1) == 0 && steps > 0;
+    const int st0 = TRI ? 1 : 0, st_end = TRI ? steps + (peel ? 0 : 1) : steps;
+    const int elast = lane < steps ? lane + st_end : TS_ZERO;   // the peeled step's slot
     if constexpr (std::is_same<real, float>::value && NG <= 2) {
-        // FP32: the slot pair (lambda = +1, lambda = -1) of each zeta in one packed register,
-        // (|1/2 + cos/2|^zeta, |1/2 - cos/2|^zeta) by packed squaring, accumulated by packed FMA
         uint64_t acc2[S / 2];
 #pragma unroll
         for (int k = 0; k < S / 2; ++k) acc2[k] = pk2(acc[2 * k], acc[2 * k + 1]);
 #pragma unroll 2   // two independent triplets per iteration
-        for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
-            const bool valid = ownP && (TRI ? (st != last_half || lane < steps) : part < nq);
-            const int e = valid ? qb + part : zr;
-            const R4 gb = w.geo[e];
-            DampRec<real, NG> db;
-            db.load(w.dp + e * NDP);
-            const float cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
-            uint64_t pw[4];
-            pw[0] = pk2(fabsf(0.5f + 0.5f * cs), fabsf(0.5f - 0.5f * cs));
-            pw[1] = mul2(pw[0], pw[0]); pw[2] = mul2(pw[1], pw[1]); pw[3] = mul2(pw[2], pw[2]);
-#pragma unroll
-            for (int g = 0; g < NG; ++g) {
-                const float DD = da.D(g) * db.D(g);          // zero for the zero record
-                const uint64_t D2 = pk2(DD, DD);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) acc2[g * 4 + q] = fma2(pw[q], D2, acc2[g * 4 + q]);
-            }
-            part = (part + 1 == n) ? 0 : part + 1;
-        }
+        for (int st = st0; st < st_end; ++st) symm_step2<real, NG, S>(w, ga, da, lane + st, acc2);
+        if (peel) symm_step2<real, NG, S>(w, ga, da, elast, acc2);
 #pragma unroll
         for (int k = 0; k < S / 2; ++k) {
             float lo, hi;
@@ -446,25 +524,8 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
         }
     } else {
 #pragma unroll 2   // two independent triplets per iteration
-    for (int st = TRI ? 1 : 0; st < (TRI ? steps + 1 : steps); ++st) {
-        const bool valid = ownP && (TRI ? (st != last_half || lane < steps) : part < nq);
-        const int e = valid ? qb + part : zr;
-        const R4 gb = w.geo[e];
-        DampRec<real, NG> db;
-        db.load(w.dp + e * NDP);
-        const real cs = ga.x * gb.x + ga.y * gb.y + ga.z * gb.z;
-        const real cwp = fabs(real(0.5) + real(0.5) * cs), cwm = fabs(real(0.5) - real(0.5) * cs);
-        real pp[4], pm[4];
-        pp[0] = cwp; pp[1] = cwp * cwp; pp[2] = pp[1] * pp[1]; pp[3] = pp[2] * pp[2];
-        pm[0] = cwm; pm[1] = cwm * cwm; pm[2] = pm[1] * pm[1]; pm[3] = pm[2] * pm[2];
-#pragma unroll
-        for (int g = 0; g < NG; ++g) {
-            const real DD = da.D(g) * db.D(g);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) { acc[g * 8 + 2 * q] += pp[q] * DD; acc[g * 8 + 2 * q + 1] += pm[q] * DD; }
-        }
-        part = (part + 1 == n) ? 0 : part + 1;
-    }
+        for (int st = st0; st < st_end; ++st) symm_step<real, NG, S>(w, ga, da, lane + st, acc);
+        if (peel) symm_step<real, NG, S>(w, ga, da, elast, acc);
     }
 }
 
@@ -526,6 +587,13 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
         reinterpret_cast<real*>(&w.stage[cap])[lane] = real(0);
     }
     if (lane < NDP) w.dp[(size_t)cap * NDP + lane] = real(0);
+    if constexpr (PASS != PASS_JVP) {
+        // the task scratch starts as zeros, so that slots no task wrote hold finite values
+        for (int k = lane; k < 4 * (TS_ZERO + 1); k += 32) reinterpret_cast<real*>(w.sg)[k] = real(0);
+        for (int k = lane; k < NDP * (TS_ZERO + 1); k += 32) w.sd[k] = real(0);
+        if constexpr (PASS == PASS_FORCE)
+            for (int k = lane; k < 4 * TS_ZERO; k += 32) reinterpret_cast<real*>(w.og)[k] = real(0);
+    }
     __syncwarp();
     uint32_t phase = 0;   // bit b: parity of the next phase of barrier b
     const unsigned lt = (1u << lane) - 1u;
@@ -1015,6 +1083,11 @@ static void configure_pass(int maxsmem) {
     set_max_dynamic_smem(k_bp<real, 2, true, PASS>, maxsmem);
     set_max_dynamic_smem(k_bp<real, 4, true, PASS>, maxsmem);
     set_max_dynamic_smem(k_bp<real, 1, false, PASS>, maxsmem);
+    // residency is bounded by shared memory (neighbour records and task scratch per warp)
+    prefer_max_shared(k_bp<real, 1, true, PASS>);
+    prefer_max_shared(k_bp<real, 2, true, PASS>);
+    prefer_max_shared(k_bp<real, 4, true, PASS>);
+    prefer_max_shared(k_bp<real, 1, false, PASS>);
 }
 void configure_bp(int maxsmem) {
     configure_pass<float, PASS_SYMM>(maxsmem); configure_pass<float, PASS_FORCE>(maxsmem); configure_pass<float, PASS_JVP>(maxsmem);

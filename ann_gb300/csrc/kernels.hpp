@@ -197,6 +197,13 @@ inline int set_max_dynamic_smem(K kernel, int maxsmem) {
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) { cudaGetLastError(); return 0; }
     return dyn;
 }
+// ask for the largest shared-memory carveout of the SM for a kernel (a launch preference of this
+// process: L1 takes what shared memory leaves)
+template <typename K>
+inline void prefer_max_shared(K kernel) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        cudaGetLastError();
+}
 // raise the dynamic shared-memory limit of every kernel once (outside any graph capture)
 void configure_bp(int maxsmem);
 void configure_mlp(int maxsmem);
