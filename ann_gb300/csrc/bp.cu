@@ -165,7 +165,7 @@ struct WarpMem {
     real *d, *fc, *fcg;
     real *ax, *ay, *az;  // force accumulators (FORCE)
     R4* tg;              // tangent of the pair vector (drx, dry, drz, dd) (JVP)
-    real* dE;            // dE/dG row (FORCE)
+    real* dE;            // dE/dG row (FORCE); dE + imax: the second staging buffer
     R4* stage;
     int32_t *stagej, *stagej2;   // staged neighbour indices (two buffers); after compaction the
                                  // current one holds j per record (-1: no Newton-3rd share, FORCE)
@@ -190,7 +190,7 @@ struct WarpMem {
         size_t o_ax = 0, o_ay = 0, o_az = 0, o_dE = 0;
         if (PASS == PASS_FORCE) {
             o_ax = take(sizeof(real) * cap, 16); o_ay = take(sizeof(real) * cap, 16); o_az = take(sizeof(real) * cap, 16);
-            o_dE = take(sizeof(real) * imax, 16);
+            o_dE = take(sizeof(real) * imax * 2, 16);   // two rows: the next atom's arrives with its neighbour row
         }
         const size_t o_sj = take(sizeof(int32_t) * cap, 16);
         const size_t o_sj2 = take(sizeof(int32_t) * cap, 16);
@@ -606,36 +606,57 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
     R4* const gbuf1 = w.stage;
     int32_t* const jbuf0 = w.stagej;
     int32_t* const jbuf1 = w.stagej2;
+    real* const ebuf0 = w.dE;
+    real* const ebuf1 = w.dE + imax;
+    // force pass: the dE/dG row travels with the neighbour row when rows are whole 16-byte units
+    const bool dE_bulk = (PASS == PASS_FORCE) && ((size_t)imax * sizeof(real)) % 16 == 0;
     auto next_atom = [&]() {
         int v = 0;
         if (lane == 0) v = (int)atomicAdd(a.counter, 1u);
         return __shfl_sync(0xffffffffu, v, 0);
     };
-    auto stage_row = [&](int i, int b) -> bool {   // false: nothing was issued
+    // the next atom's scalars, loaded a whole atom ahead of their use: type, entries, and the
+    // entries per neighbour type in lanes 0..T-1
+    struct AtomScalars { int type, nn, ntc; };
+    auto load_scalars = [&](int i) {
+        AtomScalars v{0, 0, 0};
+        if (i < a.natoms) {
+            v.type = a.type[i];
+            v.nn = a.nn[i];
+            if (lane < T) v.ntc = a.ntc[(size_t)i * T + lane];
+        }
+        return v;
+    };
+    auto stage_row = [&](int i, int b, int nn) -> bool {   // false: nothing was issued
         if (i >= a.natoms) return false;
-        const int nin = min(a.nn[i], cap);
+        const int nin = min(nn, cap);
         if (nin <= 0) return false;
         if (lane == 0) {
             const size_t row = (size_t)i * cap;
             const uint32_t b1 = (uint32_t)(nin * sizeof(R4));
             const uint32_t b2 = (uint32_t)(((nin + 3) / 4) * 16);
+            const uint32_t b3 = dE_bulk ? (uint32_t)(imax * sizeof(real)) : 0u;
             fence_proxy_async();
-            mbar_expect_tx(&w.bar[b], b1 + b2);
+            mbar_expect_tx(&w.bar[b], b1 + b2 + b3);
             bulk_g2s(b ? gbuf1 : gbuf0, reinterpret_cast<const R4*>(a.nr) + row, b1, &w.bar[b]);
             bulk_g2s(b ? jbuf1 : jbuf0, a.nj + row, b2, &w.bar[b]);
+            if (dE_bulk) bulk_g2s(b ? ebuf1 : ebuf0, a.dEdG + (size_t)i * imax, b3, &w.bar[b]);
         }
         return true;
     };
     int nx_i = next_atom(), nx_b = 0;
-    bool nx_issued = stage_row(nx_i, 0);
+    AtomScalars nx_s = load_scalars(nx_i);
+    bool nx_issued = stage_row(nx_i, 0, nx_s.nn);
 
     for (;;) {
         const int i = nx_i, cb = nx_b;
         const bool issued = nx_issued;
+        const AtomScalars cur = nx_s;
         if (i >= a.natoms) break;
         nx_i = next_atom();
         nx_b = cb ^ 1;
-        nx_issued = stage_row(nx_i, nx_b);
+        nx_s = load_scalars(nx_i);
+        nx_issued = stage_row(nx_i, nx_b, nx_s.nn);
         if (issued) {
             const bool done = mbar_wait_bounded(&w.bar[cb], (phase >> cb) & 1u, a.wait_polls);
             if (!__all_sync(0xffffffffu, done)) {  // bounded wait gave up: report, drain (full bound), stop
@@ -649,10 +670,11 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
         }
         w.geo = cb ? gbuf1 : gbuf0;
         w.stagej = cb ? jbuf1 : jbuf0;
-        const int I = a.type[i];
+        if (PASS == PASS_FORCE) w.dE = cb ? ebuf1 : ebuf0;
+        const int I = cur.type;
         if (I < 0 || I >= T) { if (lane == 0) atomicOr(a.status, (int)ST_BAD_TYPE); continue; }
         const DevType& TT = pot.t[I];
-        const int nin = min(a.nn[i], cap);
+        const int nin = min(cur.nn, cap);
         const size_t row = (size_t)i * cap;
         // ---- compaction to d < rc, per-type active ranges, per-neighbour records ---------------
         const real rc = (real)TT.rc;
@@ -662,7 +684,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
         typename std::conditional<PASS == PASS_FORCE, TypeRangesArr, TypeRangesReg>::type tstart, tcnt;
         int pos = 0, base_in = 0;
         for (int t = 0; t < T; ++t) {
-            const int cin = a.ntc[(size_t)i * T + t];
+            const int cin = __shfl_sync(0xffffffffu, cur.ntc, t);
             tstart.set(t, pos);
             for (int e0 = 0; e0 < cin; e0 += 32) {
                 const int e = base_in + e0 + lane;
@@ -706,7 +728,7 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
             tcnt.set(t, pos - tstart.get(t));
             base_in += cin;
         }
-        if (PASS == PASS_FORCE) {
+        if (PASS == PASS_FORCE && !(dE_bulk && issued)) {
             for (int m = lane; m < TT.nInput; m += 32) w.dE[m] = a.dEdG[(size_t)i * imax + m];
         }
         __syncwarp();
