@@ -69,7 +69,7 @@ _SIGS = {
     "ann_set_params": (C.c_int, [_V, _D, C.c_int64]),
     "ann_set_input_scaling": (C.c_int, [_V, C.c_int32, _D, _D, C.c_int32]),
     "ann_init_network": (C.c_int, [_V, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double]),
-    "ann_compute": (C.c_int, [_V, C.c_int32, _I64, _D, _I32, _D, _D, _D, _D, C.c_int32]),
+    "ann_compute": (C.c_int, [_V, C.c_int32, _V, _V, _V, _V, _V, _V, _V, C.c_int32]),   # addresses (the per-call path)
     "ann_opt_set_schedule": (C.c_int, [_V, C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_double]),
     "ann_opt_init": (C.c_int, [_V, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double]),
     "ann_opt_step": (C.c_int, [_V, C.c_double]),
@@ -326,9 +326,13 @@ class Context:
             e = np.zeros(S)
             f = np.zeros((N, 3)) if forces else None
             w = np.zeros((S, 3, 3)) if virial else None
-        self._ck(self.lib.ann_compute(self.h, S, _i64(np.ascontiguousarray(offs, np.int64)), _d(np.ascontiguousarray(posn, np.float64)),
-                                      _i32(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(cell, np.float64)),
-                                      _d(e), _d(f), _d(w), prec))
+        o, x, t, c = (np.ascontiguousarray(offs, np.int64), np.ascontiguousarray(posn, np.float64),
+                      np.ascontiguousarray(types, np.int32), np.ascontiguousarray(cell, np.float64))
+        for arr in (e, f, w):
+            if arr is not None and not (arr.dtype == np.float64 and arr.flags.c_contiguous):
+                raise ValueError("out arrays must be C-contiguous float64")
+        self._ck(self.lib.ann_compute(self.h, S, o.ctypes.data, x.ctypes.data, t.ctypes.data, c.ctypes.data, e.ctypes.data,
+                                      None if f is None else f.ctypes.data, None if w is None else w.ctypes.data, prec))
         return e, f, w
 
     def compute_list(self, x, types, numneigh, neigh, ilist=None, forces=True, virial=True, eatom=False, precision=None,

@@ -2,6 +2,7 @@
 // capture, batch compute and inspection, page-locked host buffers: the core of the extern "C"
 // entry points of include/ann_gpu.h. No C++ exception crosses the C boundary.
 #include "context.hpp"
+#include "transfer.hpp"
 
 static std::mutex g_err_mu;
 static std::string g_err;
@@ -205,11 +206,19 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
         if (c->N > 0) launch_fill_sid(c->S, c->off_d, c->sid.as<int32_t>(), c->stream);
         c->tables_gen = g_alloc_gen.load();
     }
-    if (c->N > 0) {
-        ck(cudaMemcpyAsync(c->pos.p, posn, sizeof(double) * 3 * (size_t)c->N, k, c->stream), "copy positions");
-        ck(cudaMemcpyAsync(c->type.p, type, sizeof(int32_t) * (size_t)c->N, k, c->stream), "copy types");
-    }
-    if (c->S > 0) ck(cudaMemcpyAsync(c->cell.p, cell, sizeof(double) * 9 * (size_t)c->S, k, c->stream), "copy cells");
+    // inputs in the library's own page-locked buffers move by one copy kernel, the others by the
+    // copy engines
+    CopyPlan cp;
+    auto put = [&](void* dst, const void* src, size_t bytes, const char* what) {
+        if (bytes == 0) return;
+        void* v = device_src ? nullptr : host_device_view(src, bytes);
+        if (v && cp.add(v, dst, bytes)) return;
+        ck(cudaMemcpyAsync(dst, src, bytes, k, c->stream), what);
+    };
+    put(c->pos.p, posn, sizeof(double) * 3 * (size_t)c->N, "copy positions");
+    put(c->type.p, type, sizeof(int32_t) * (size_t)c->N, "copy types");
+    put(c->cell.p, cell, sizeof(double) * 9 * (size_t)c->S, "copy cells");
+    launch_copy_plan(cp, c->nsm, c->stream);
     c->have_batch = true;
     c->have_results = false;
     c->train_staged = false;
@@ -259,6 +268,7 @@ static RedTable red_table(ann_ctx* c) {
 template <typename real>
 static void enqueue_ef(ann_ctx* c, bool forces, int mode) {
     cudaStream_t st = c->stream;
+    ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, st), "memset status");   // part of the captured sequence
     const bool fp64 = std::is_same<real, double>::value;
     const DevPot& pot = c->plan.pot;
     BpArgs<real> b = bp_args<real>(c);
@@ -316,7 +326,6 @@ static void enqueue_ef(ann_ctx* c, bool forces, int mode) {
 static void run_sequence(ann_ctx* c, int prec, bool forces, int mode) {
     if (!c->have_batch) throw ann_error(ANN_ERR_STATE, "no batch staged");
     if (prec != ANN_FP64 && prec != ANN_MIXED) throw ann_error(ANN_ERR_ARG, "invalid precision");
-    ck(cudaMemsetAsync(c->status.p, 0, 4 * 8, c->stream), "memset status");
     // shared-memory needs of this batch (neighbour rows are staged per warp)
     const size_t need_bp = bp_smem_bytes(c->plan.pot, c->cap, prec == ANN_FP64) + 1024;
     const size_t need_mlp = mlp_smem_bytes(c->plan.pot, prec == ANN_FP64, false) + 1024;
@@ -383,7 +392,10 @@ void run_staged(ann_ctx* c, int prec) {
 
 // a page-locked copy of the device status word, for reads that ride along with result copies
 int32_t* status_host(ann_ctx* c) {
-    if (!c->status_h) ck(cudaMallocHost(reinterpret_cast<void**>(&c->status_h), 4 * 8), "cudaMallocHost status");
+    if (!c->status_h) {
+        ck(cudaMallocHost(reinterpret_cast<void**>(&c->status_h), 4 * 8), "cudaMallocHost status");
+        host_register(c->status_h, 4 * 8);
+    }
     return c->status_h;
 }
 
@@ -483,7 +495,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->lEs, &c->lWs, &c->st_acc, &c->st_n, &c->st_part, &c->st_pcount})
         b->release();
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
-    if (c->status_h) cudaFreeHost(c->status_h);
+    if (c->status_h) { host_unregister(c->status_h); cudaFreeHost(c->status_h); }
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->side) cudaStreamDestroy(c->side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -690,18 +702,29 @@ int ann_compute(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* p
         // the results and the status word in one round trip; a status that is not clean (list
         // overflow, bad input) goes through finish_batch, which recovers or throws, and the
         // results are copied again
-        auto copy_out = [&]() {
-            if (c->S > 0) ck(cudaMemcpyAsync(energy, c->Es.p, sizeof(double) * c->S, cudaMemcpyDeviceToHost, c->stream), "D2H energy");
-            if (forces && c->N > 0) ck(cudaMemcpyAsync(forces, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream), "D2H forces");
-            if (virial && c->S > 0) ck(cudaMemcpyAsync(virial, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, cudaMemcpyDeviceToHost, c->stream), "D2H virial");
-        };
-        copy_out();
+        // results into the library's own page-locked buffers move by one copy kernel (with the
+        // status word), the others by the copy engines
         int32_t* sh = status_host(c);
-        ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
+        auto copy_out = [&](bool with_status) {
+            CopyPlan cp;
+            auto get = [&](void* dst, const void* src, size_t bytes, const char* what) {
+                if (bytes == 0) return;
+                void* v = host_device_view(dst, bytes);
+                if (v && cp.add(src, v, bytes)) return;
+                ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream), what);
+            };
+            get(energy, c->Es.p, sizeof(double) * c->S, "D2H energy");
+            if (forces) get(forces, c->Fout.p, sizeof(double) * 3 * (size_t)c->N, "D2H forces");
+            if (virial) get(virial, c->Ws.p, sizeof(double) * 9 * (size_t)c->S, "D2H virial");
+            if (with_status) get(sh, c->status.p, 4 * 8, "D2H status");
+            launch_copy_plan(cp, c->nsm, c->stream);
+            ck(cudaGetLastError(), "copy kernel");
+        };
+        copy_out(true);
         ck(cudaStreamSynchronize(c->stream), "synchronize");
         if (sh[0] != 0) {
             finish_batch(c);
-            copy_out();
+            copy_out(false);
             ck(cudaStreamSynchronize(c->stream), "synchronize");
         }
     })
@@ -731,10 +754,12 @@ int ann_host_alloc(ann_ctx* c, int64_t bytes, void** ptr) {
     ANN_TRY(c, {
         set_device(c);
         ck(cudaMallocHost(ptr, (size_t)bytes), "cudaMallocHost");
+        host_register(*ptr, (size_t)bytes);
     })
 }
 int ann_host_free(ann_ctx* c, void* ptr) {   // ctx may be NULL (a buffer may outlive its context)
     if (!ptr) return ANN_OK;
+    host_unregister(ptr);
     const cudaError_t e = cudaFreeHost(ptr);
     if (e != cudaSuccess) return fail(c, ANN_ERR_CUDA, std::string("cudaFreeHost: ") + cudaGetErrorString(e));
     return ANN_OK;
