@@ -671,6 +671,8 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
         w.geo = cb ? gbuf1 : gbuf0;
         w.stagej = cb ? jbuf1 : jbuf0;
         if (PASS == PASS_FORCE) w.dE = cb ? ebuf1 : ebuf0;
+        // the symmetry pass clears the atom's force accumulator for the force pass that follows
+        if (PASS == PASS_SYMM && lane < 3) a.F[3 * (size_t)i + lane] = real(0);
         const int I = cur.type;
         if (I < 0 || I >= T) { if (lane == 0) atomicOr(a.status, (int)ST_BAD_TYPE); continue; }
         const DevType& TT = pot.t[I];

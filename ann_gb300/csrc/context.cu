@@ -142,7 +142,11 @@ static void stage_offsets(ann_ctx* c, int nstruc, const int64_t* atom_offsets) {
     c->off_h.assign(nstruc + 1, 0);
     for (int s = 0; s <= nstruc; ++s) c->off_h[s] = (int32_t)atom_offsets[s];
     c->max_nat = 0;
-    for (int s = 0; s < nstruc; ++s) c->max_nat = std::max(c->max_nat, c->off_h[s + 1] - c->off_h[s]);
+    c->red_fused = nstruc > 0;
+    for (int s = 0; s < nstruc; ++s) {
+        c->max_nat = std::max(c->max_nat, c->off_h[s + 1] - c->off_h[s]);
+        if (c->off_h[s + 1] == c->off_h[s]) c->red_fused = false;
+    }
     // chunks of the per-structure reductions
     c->rchunk_h.clear();
     c->rschunk_h.assign(nstruc + 1, 0);
@@ -204,6 +208,8 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
         c->rchunk_d = c->off_d + o_ch;
         c->rschunk_d = c->off_d + o_sc;
         if (c->N > 0) launch_fill_sid(c->S, c->off_d, c->sid.as<int32_t>(), c->stream);
+        c->rarrive.ensure(sizeof(int32_t) * (size_t)std::max(c->S, 1));
+        ck(cudaMemsetAsync(c->rarrive.p, 0, sizeof(int32_t) * (size_t)std::max(c->S, 1), c->stream), "memset arrivals");
         c->tables_gen = g_alloc_gen.load();
     }
     // inputs in the library's own page-locked buffers move by one copy kernel, the others by the
@@ -260,6 +266,7 @@ static RedTable red_table(ann_ctx* c) {
     RedTable t;
     t.nchunks = (int32_t)(c->rchunk_h.size() / 3);
     t.chunk = c->rchunk_d; t.schunk = c->rschunk_d; t.partial = c->rpartial.as<double>();
+    t.arrive = c->red_fused ? c->rarrive.as<int32_t>() : nullptr;
     return t;
 }
 
@@ -312,7 +319,8 @@ static void enqueue_ef(ann_ctx* c, bool forces, int mode) {
     check_phase(c, "networks");
     mark(c, 4);
     if (forces) {
-        cudaMemsetAsync(c->F.p, 0, sizeof(real) * 3 * (size_t)std::max(c->N, 1), st);
+        // the symmetry pass clears F atom by atom; the staged sequence runs no symmetry pass
+        if (mode == SEQ_STAGED) cudaMemsetAsync(c->F.p, 0, sizeof(real) * 3 * (size_t)std::max(c->N, 1), st);
         launch_force<real>(pot, b, st);
     }
     check_phase(c, "forces");
@@ -337,7 +345,7 @@ static void run_sequence(ann_ctx* c, int prec, bool forces, int mode) {
     if (!(prec == ANN_MIXED && use_tc(c)) && need_mlp > (size_t)c->max_smem)
         throw ann_error(ANN_ERR_UNSUPPORTED, "networks too wide for the shared-memory network kernel");
     const GraphKey key{c->S, c->N, c->cap, prec, forces ? 1 : 0, c->nbins_cap, (int)(c->rchunk_h.size() / 3), c->md_ready ? 1 : 0, g_alloc_gen.load(),
-                       nbr_local_binning(c->max_nat) ? 1 : 0};
+                       (nbr_local_binning(c->max_nat) ? 1 : 0) | (c->red_fused ? 2 : 0)};
     const bool graphs = c->opt.use_graphs && c->N > 0 && !c->profile;
     const int gs = mode;
     if (graphs) {
@@ -489,7 +497,7 @@ int ann_destroy(ann_ctx* c) {
                       &c->nr, &c->scan_tmp, &c->counter, &c->status, &c->G, &c->dEdG, &c->Eatom, &c->F, &c->W, &c->Es, &c->Ws, &c->Fout,
                       &c->tcount, &c->tstart, &c->tlist, &c->Eref, &c->Fref, &c->loss3, &c->ce, &c->lam, &c->U, &c->grad, &c->gpart,
                       &c->vel, &c->minv, &c->mass, &c->disp_ref, &c->mdflag, &c->ke, &c->md_R_d, &c->md_Ri_d,
-                      &c->tables, &c->rpartial, &c->tcimg, &c->p64, &c->pmap, &c->opt_s0, &c->opt_s1, &c->opt_s2, &c->opt_gold, &c->opt_part,
+                      &c->tables, &c->rpartial, &c->rarrive, &c->tcimg, &c->p64, &c->pmap, &c->opt_s0, &c->opt_s1, &c->opt_s2, &c->opt_gold, &c->opt_part,
                       &c->lx, &c->ltype, &c->lilist, &c->lnoff, &c->lneigh, &c->lrtype, &c->lnn, &c->lntc, &c->lnj, &c->lnr, &c->lG,
                       &c->ldEdG, &c->lEatom, &c->lF, &c->lW, &c->lFout, &c->ltcount, &c->ltstart, &c->ltlist, &c->ltables, &c->lpartial,
                       &c->lEs, &c->lWs, &c->st_acc, &c->st_n, &c->st_part, &c->st_pcount})

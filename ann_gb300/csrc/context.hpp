@@ -91,10 +91,11 @@ struct GraphKey {
     int S, N, cap, prec, forces, nbins, nchunks;
     int md;         // MD mode: list cutoff rc + skin, refreshed between rebuilds
     uint64_t gen;   // g_alloc_gen at capture
-    int local_bins; // structures binned one block each (nbr_local_binning of the largest structure)
+    int flags;      // bit 0: structures binned one block each (nbr_local_binning of the largest
+                    // structure); bit 1: per-structure sums in one launch (no empty structure)
     bool operator==(const GraphKey& o) const {
         return S == o.S && N == o.N && cap == o.cap && prec == o.prec && forces == o.forces && nbins == o.nbins && nchunks == o.nchunks &&
-               md == o.md && gen == o.gen && local_bins == o.local_bins;
+               md == o.md && gen == o.gen && flags == o.flags;
     }
 };
 
@@ -134,6 +135,8 @@ struct ann_ctx {
     int S = 0, N = 0;
     int max_nat = 0;                // atoms of the largest structure of the staged batch
     uint64_t tables_gen = ~0ull;    // g_alloc_gen when the offset tables and sid were last uploaded
+    bool red_fused = false;         // every structure has atoms: per-structure sums in one launch
+    DevBuf rarrive;                 // [S] per-structure chunk arrivals of that launch (zero between launches)
     bool have_batch = false;
     std::vector<int32_t> off_h, rchunk_h, rschunk_h, tables_h;
     DevBuf tables, cell, pos, type, sid, rpartial;

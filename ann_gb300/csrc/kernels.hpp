@@ -179,6 +179,8 @@ struct RedTable {
     const int32_t* chunk;            // [nchunks][3]: structure, first atom, end atom
     const int32_t* schunk;           // [S+1] first chunk of each structure
     double* partial;                 // [nchunks][10]
+    int32_t* arrive = nullptr;       // [S] chunks of each structure done (zero between launches), or
+                                     // nullptr: a second kernel adds the partials per structure
 };
 template <typename real>
 void launch_reduce_structures(int nstruc, const RedTable& t, const double* Eatom, const real* W, const real* F,

@@ -187,10 +187,80 @@ __global__ void k_reduce_partials(int nstruc, const int32_t* schunk, const doubl
         if (with_w && Ws) for (int k = 0; k < 9; ++k) Ws[9 * (size_t)s + k] = red[1 + k][0];
     }
 }
+// The two steps in one launch, when every structure has at least one chunk: the chunk block that
+// completes its structure's last chunk (per-structure arrival count) adds the structure's
+// partials, with the same order and tree as k_reduce_partials, and resets the count.
+template <typename real>
+__global__ void k_reduce_fused(const int32_t* chunk, const int32_t* schunk, const double* Eatom, const real* W, const real* F,
+                               double* partial, double* Fout, int32_t* arrive, bool with_w, double* Es, double* Ws) {
+    const int c = blockIdx.x;
+    const int s = chunk[3 * c], a0 = chunk[3 * c + 1], a1 = chunk[3 * c + 2];
+    __shared__ double red[10][RED_THREADS];
+    __shared__ int last;
+    double acc[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = 0.0;
+    for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+        acc[0] += Eatom[i];
+        if (W) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) acc[1 + k] += (double)W[9 * (size_t)i + k];
+        }
+        if (Fout) {
+            Fout[3 * (size_t)i] = (double)F[3 * (size_t)i];
+            Fout[3 * (size_t)i + 1] = (double)F[3 * (size_t)i + 1];
+            Fout[3 * (size_t)i + 2] = (double)F[3 * (size_t)i + 2];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < 10; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 10) partial[10 * (size_t)c + threadIdx.x] = red[threadIdx.x][0];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(&arrive[s], 1) == schunk[s + 1] - schunk[s] - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = 0.0;
+    for (int cc = schunk[s] + threadIdx.x; cc < schunk[s + 1]; cc += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) acc[k] += __ldcg(partial + 10 * (size_t)cc + k);   // other blocks' rows, from L2
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 10; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < 10; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        Es[s] = red[0][0];
+        if (with_w && Ws) for (int k = 0; k < 9; ++k) Ws[9 * (size_t)s + k] = red[1 + k][0];
+        arrive[s] = 0;
+    }
+}
 template <typename real>
 void launch_reduce_structures(int nstruc, const RedTable& t, const double* Eatom, const real* W, const real* F,
                               double* Es, double* Ws, double* Fout, cudaStream_t st) {
     if (nstruc <= 0) return;
+    if (t.arrive && t.nchunks > 0) {
+        ++::ann::g_launch_counter;
+        k_reduce_fused<real><<<t.nchunks, RED_THREADS, 0, st>>>(t.chunk, t.schunk, Eatom, W, F, t.partial, Fout, t.arrive, W != nullptr, Es, Ws);
+        return;
+    }
     if (t.nchunks > 0) ++::ann::g_launch_counter, k_reduce_chunks<real><<<t.nchunks, RED_THREADS, 0, st>>>(t.chunk, Eatom, W, F, t.partial, Fout);
     ++::ann::g_launch_counter, k_reduce_partials<<<nstruc, RED_THREADS, 0, st>>>(nstruc, t.schunk, t.partial, W != nullptr, Es, Ws);
 }
