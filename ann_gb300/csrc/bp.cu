@@ -51,9 +51,15 @@ constexpr int BP_WARPS = 4;
 // and tangent passes six (84 registers; bounded for five they take 89 and lose a block per SM:
 // 0.340 -> 0.395 ms on that box)
 // (fast-path kernels; the generic path keeps five)
-constexpr int bp_min_blocks(int pass, int ng, bool fast) {
-    return pass == PASS_FORCE ? (ng > 1 ? ANN_BP_MIN_BLOCKS_FORCE : ANN_BP_MIN_BLOCKS)
-                              : (ng == 1 && fast ? ANN_BP_MIN_BLOCKS + 1 : ANN_BP_MIN_BLOCKS);
+// The FP32 force pass with up to two damping groups is bounded for five blocks (96 registers, a
+// 36-byte spill), which its shared memory allows at the row capacities of ~100 that a learned
+// capacity gives on the bench batch (0.621 -> 0.614 ms there; the symmetry pass bounded for six,
+// 80 registers, took 0.334 -> 0.342 ms and keeps five). The FP64 kernels and four damping groups
+// keep the older bounds.
+constexpr int bp_min_blocks(int pass, int ng, bool fast, bool fp64) {
+    return (fp64 || ng > 2) ? (pass == PASS_FORCE ? (ng > 1 ? ANN_BP_MIN_BLOCKS_FORCE : ANN_BP_MIN_BLOCKS)
+                                                  : (ng == 1 && fast ? ANN_BP_MIN_BLOCKS + 1 : ANN_BP_MIN_BLOCKS))
+                : (pass == PASS_FORCE ? ANN_BP_MIN_BLOCKS : (ng == 1 && fast ? ANN_BP_MIN_BLOCKS + 1 : ANN_BP_MIN_BLOCKS));
 }
 constexpr int CHUNK = 16;   // functions per register chunk (radial and generic angular)
 
@@ -172,10 +178,9 @@ struct WarpMem {
     uint64_t* bar;       // two mbarriers, one per staging buffer
     // chunk-task scratch (symmetry and force passes): the partner chunk twice over, partner slots
     // without an element as zeros, so that rotation step st reads slot lane + st with no wrap; a
-    // zero record at TS_ZERO. Force pass: the owning chunk twice over (og), for the senders' records
+    // zero record at TS_ZERO
     R4* sg;
     real* sd;
-    R4* og;
     static constexpr int NDP = 2 * NG;
     static __host__ __device__ size_t align(size_t x, size_t a) { return (x + a - 1) / a * a; }
     static __host__ __device__ size_t layout(int cap, int imax, WarpMem* w, unsigned char* base) {
@@ -198,7 +203,6 @@ struct WarpMem {
         const bool tasks = (PASS != PASS_JVP);
         const size_t o_sg = tasks ? take(sizeof(R4) * (TS_ZERO + 1), 32) : 0;
         const size_t o_sd = tasks ? take(sizeof(real) * NDP * (TS_ZERO + 1), 16) : 0;
-        const size_t o_og = (PASS == PASS_FORCE) ? take(sizeof(R4) * TS_ZERO, 32) : 0;
         if (w) {
             w->geo = reinterpret_cast<R4*>(base + o_geo); w->stage = reinterpret_cast<R4*>(base + o_stage);
             w->tg = reinterpret_cast<R4*>(base + o_tg); w->dp = reinterpret_cast<real*>(base + o_dp);
@@ -209,7 +213,6 @@ struct WarpMem {
             w->stagej2 = reinterpret_cast<int32_t*>(base + o_sj2);
             w->bar = reinterpret_cast<uint64_t*>(base + o_bar);
             w->sg = reinterpret_cast<R4*>(base + o_sg); w->sd = reinterpret_cast<real*>(base + o_sd);
-            w->og = reinterpret_cast<R4*>(base + o_og);
         }
         return align(off, 128);
     }
@@ -351,11 +354,11 @@ __device__ __forceinline__ void angular_poly(const real* dE, const int32_t* slot
 // `zr`: D = D' = 0 and a zero unit vector make every term of the triplet exactly zero, so the loop
 // carries no per-step masking of its results. Lanes beyond the owning chunk own the zero record.
 // the task scratch for a partner chunk of n elements at qb, of which the first nv have records:
-// slot k < 2n holds element k mod n (zeros from nv on); og (force pass, rectangles) likewise the
-// owning chunk at p0. Slots at and beyond 2n keep finite older values: only lanes beyond the owning
-// chunk read them, and those lanes own the zero record, so their terms vanish.
+// slot k < 2n holds element k mod n (zeros from nv on). Slots at and beyond 2n keep finite older
+// values: only lanes beyond the owning chunk read them, and those lanes own the zero record, so
+// their terms vanish.
 template <typename WM>
-__device__ __forceinline__ void fill_task_scratch(const WM& w, int lane, int qb, int n, int nv, int p0, bool own) {
+__device__ __forceinline__ void fill_task_scratch(const WM& w, int lane, int qb, int n, int nv) {
     typedef typename WM::R4 R4;
     constexpr int NDP = WM::NDP;
     typedef typename std::remove_pointer<decltype(w.sd)>::type real;
@@ -375,7 +378,6 @@ __device__ __forceinline__ void fill_task_scratch(const WM& w, int lane, int qb,
         w.sg[k] = g;
 #pragma unroll
         for (int q = 0; q < NDP; ++q) w.sd[k * NDP + q] = d[q];
-        if (own) w.og[k] = w.geo[p0 + m];
     }
     __syncwarp();
 }
@@ -390,7 +392,7 @@ __device__ __forceinline__ void force_step(const WM& w, const R4& ga, const Damp
     const R4 gb = w.sg[e];                             // partner (task scratch slot)
     DampRec<real, NG> db;
     db.load(w.sd + e * NDP);
-    const R4 gs = TRI ? w.sg[es] : w.og[es];           // the sending lane's own element
+    const R4 gs = TRI ? w.sg[es] : w.geo[es];          // the sending lane's own element
     real cj, bj, ck, bk;
     if constexpr (PACKED) triplet_force2(ga, da, gb, db, alp, cj, bj, ck, bk);
     else triplet_force<real, NG>(ga, da, gb, db, al, cj, bj, ck, bk);
@@ -424,8 +426,9 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     const int steps = TRI ? np / 2 : np;      // triangle: steps 1..n/2, rectangle: 0..n-1
     // the partner chunk (the owning one for a triangle) twice over in the task scratch, so that
     // step st reads slot lane + st: partner (lane + st) mod n, or zeros where Q has no element; the
-    // sender of step st, lane (lane - st) mod n, owns slot n + lane - st of the owning chunk
-    fill_task_scratch(w, lane, TRI ? p0 : q0, n, TRI ? n : nq, p0, !TRI);
+    // sender of step st, lane src = (lane - st) mod n, owns slot n + lane - st of a triangle's
+    // scratch, or element p0 + src of a rectangle's owning chunk
+    fill_task_scratch(w, lane, TRI ? p0 : q0, n, TRI ? n : nq);
     int src = TRI ? lane - 1 : lane;          // sending lane (lane - step) mod n
     if (src < 0) src += n;
     if (src >= n) src = 0;                    // lanes beyond the chunk: any element of it
@@ -435,10 +438,10 @@ __device__ __forceinline__ void force_task(const WarpMem<real, NG, PASS>& w, con
     int st = TRI ? 1 : 0;
 #pragma unroll 1
     for (; st < (TRI ? steps + (peel ? 0 : 1) : steps); ++st) {
-        force_step<real, NG, PACKED, TRI>(w, ga, da, al, alp, lane + st, n + lane - st, src, ca, cb, sa, sb);
+        force_step<real, NG, PACKED, TRI>(w, ga, da, al, alp, lane + st, TRI ? n + lane - st : p0 + src, src, ca, cb, sa, sb);
         src = (src == 0) ? n - 1 : src - 1;
     }
-    if (peel) force_step<real, NG, PACKED, TRI>(w, ga, da, al, alp, lane < steps ? lane + st : TS_ZERO, n + lane - st, src, ca, cb, sa, sb);
+    if (peel) force_step<real, NG, PACKED, TRI>(w, ga, da, al, alp, lane < steps ? lane + st : TS_ZERO, n + lane - st, src, ca, cb, sa, sb);   // (triangles only)
     if (ownP) {
         w.ax[p0 + lane] += ca * ga.x + sa[0]; w.ay[p0 + lane] += ca * ga.y + sa[1]; w.az[p0 + lane] += ca * ga.z + sa[2];
     }
@@ -505,7 +508,7 @@ __device__ __forceinline__ void symm_task(const WarpMem<real, NG, PASS>& w, real
     da.load(w.dp + ea * NDP);
     const int n = np;
     const int steps = TRI ? np / 2 : np;
-    fill_task_scratch(w, lane, TRI ? p0 : q0, n, TRI ? n : nq, p0, false);
+    fill_task_scratch(w, lane, TRI ? p0 : q0, n, TRI ? n : nq);
     const bool peel = TRI && (n & 1) == 0 && steps > 0;
     const int st0 = TRI ? 1 : 0, st_end = TRI ? steps + (peel ? 0 : 1) : steps;
     const int elast = lane < steps ? lane + st_end : TS_ZERO;   // the peeled step's slot
@@ -557,7 +560,7 @@ __host__ __device__ inline size_t bp_table_bytes(const DevPot& pot) {   // force
 
 // ---------------------------------------------------------------- the kernel
 template <typename real, int NG, bool FAST, int PASS>
-__global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
+__global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST, std::is_same<real, double>::value)) k_bp(const __grid_constant__ DevPot pot, const BpArgs<real> a) {
     typedef typename V4<real>::T R4;
     extern __shared__ __align__(128) unsigned char bsm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -591,8 +594,6 @@ __global__ void __launch_bounds__(BP_WARPS * 32, bp_min_blocks(PASS, NG, FAST)) 
         // the task scratch starts as zeros, so that slots no task wrote hold finite values
         for (int k = lane; k < 4 * (TS_ZERO + 1); k += 32) reinterpret_cast<real*>(w.sg)[k] = real(0);
         for (int k = lane; k < NDP * (TS_ZERO + 1); k += 32) w.sd[k] = real(0);
-        if constexpr (PASS == PASS_FORCE)
-            for (int k = lane; k < 4 * TS_ZERO; k += 32) reinterpret_cast<real*>(w.og)[k] = real(0);
     }
     __syncwarp();
     uint32_t phase = 0;   // bit b: parity of the next phase of barrier b

@@ -185,7 +185,15 @@ void upload_batch(ann_ctx* c, int nstruc, const int64_t* offs, const double* pos
             if (!(std::fabs(det) > 0)) throw ann_error(ANN_ERR_ARG, "singular cell of structure " + std::to_string(s));
         }
     }
-    if (c->cap == 0) c->cap = estimate_cap(c, device_src ? nullptr : cell);
+    if (c->cap == 0) {
+        c->cap = estimate_cap(c, device_src ? nullptr : cell);
+    } else if (!c->md_ready && c->opt.max_neighbors <= 0 && c->nn_seen > 0) {
+        // rows no longer than 1.25 x the longest seen: the basis and force passes stage rows of
+        // cap entries per warp, and a smaller capacity lets more blocks share an SM (a batch with
+        // longer rows overflows, regrows the capacity and is computed again)
+        const int want = std::max(32, ((int)std::ceil(1.25 * c->nn_seen) + 31) / 32 * 32);
+        if (want < c->cap) c->cap = want;
+    }
     const uint64_t gen0 = g_alloc_gen.load();
     ensure_batch_buffers(c);
     if (g_alloc_gen.load() != gen0) same = false;
@@ -413,6 +421,7 @@ void finish_batch(ann_ctx* c) {
         int32_t st[8];
         ck(cudaMemcpyAsync(st, c->status.p, sizeof(st), cudaMemcpyDeviceToHost, c->stream), "D2H status");
         ck(cudaStreamSynchronize(c->stream), "synchronize");
+        note_rows(c, st);
         if (st[0] == 0) return;
         if (st[0] & ST_BAD_TYPE) throw ann_error(ANN_ERR_ARG, "type index out of range");
         if (st[0] & ST_NONFINITE) throw ann_error(ANN_ERR_NUMERIC, "non-finite position or singular cell");
@@ -531,6 +540,7 @@ int ann_load_potential_text(ann_ctx* c, const char* text) {
         c->opt_ready = false;
         c->st_ready = false;   // statistics belong to the previous potential's inputs
         c->train_staged = false;   // so do the staged training batch's symmetry functions
+        c->nn_seen = 0;            // and the row lengths (the cutoff may differ)
         rebuild_plan(c);
     })
 }
@@ -730,6 +740,7 @@ int ann_compute(ann_ctx* c, int32_t nstruc, const int64_t* offs, const double* p
         };
         copy_out(true);
         ck(cudaStreamSynchronize(c->stream), "synchronize");
+        note_rows(c, sh);
         if (sh[0] != 0) {
             finish_batch(c);
             copy_out(false);

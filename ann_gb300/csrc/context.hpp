@@ -136,6 +136,7 @@ struct ann_ctx {
     int max_nat = 0;                // atoms of the largest structure of the staged batch
     uint64_t tables_gen = ~0ull;    // g_alloc_gen when the offset tables and sid were last uploaded
     bool red_fused = false;         // every structure has atoms: per-structure sums in one launch
+    int nn_seen = 0;                // longest neighbour row of the batches computed so far (list cutoff rc)
     DevBuf rarrive;                 // [S] per-structure chunk arrivals of that launch (zero between launches)
     bool have_batch = false;
     std::vector<int32_t> off_h, rchunk_h, rschunk_h, tables_h;
@@ -222,6 +223,8 @@ void run_batch(ann_ctx* c, int prec, bool forces, bool build_list = true);
 // functions that the last ann_train_forward left on the device (c->train_staged)
 void run_staged(ann_ctx* c, int prec);
 void finish_batch(ann_ctx* c);
+// the longest neighbour row of a finished batch (status word 3), for the capacity of later batches
+inline void note_rows(ann_ctx* c, const int32_t* st) { if (!c->md_ready) c->nn_seen = std::max(c->nn_seen, (int)st[3]); }
 int32_t* status_host(ann_ctx* c);
 // drops the captured graphs (launch shapes changed)
 void drop_graphs(ann_ctx* c);

@@ -302,11 +302,15 @@ __global__ void __launch_bounds__(NBR_WARPS * 32, FP64 ? 5 : 8) k_neighbors(NbrA
     const float rcf = (float)a.rc;
     cd.rc2f = FP64 ? (rcf + 0.05f) * (rcf + 0.05f) : rcf * rcf;
     cd.rc2 = a.rc * a.rc;
+    int wmax = 0;   // the warp's longest row: the host sizes later lists by it (status word 3)
     for (;;) {
         int i = 0;
         if (lane == 0) i = (int)atomicAdd(a.counter, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= a.natoms) break;
+        if (i >= a.natoms) {
+            if (lane == 0 && wmax > 0) atomicMax(a.status + 3, wmax);
+            break;
+        }
         cd.i = i;
         const StrucGeo& g = a.geo[a.sid[i]];
         int b0, b1, b2;
@@ -433,6 +437,7 @@ __global__ void __launch_bounds__(NBR_WARPS * 32, FP64 ? 5 : 8) k_neighbors(NbrA
             }
         }
         int cnt = cursor;
+        wmax = max(wmax, cnt);
         if (cnt > cap) {
             if (lane == 0) { atomicOr(a.status, (int)ST_NBR_OVERFLOW); atomicMax(a.status + 1, cnt); }
             cnt = cap;

@@ -51,6 +51,7 @@ static void train_loss(ann_ctx* c, int prec, double wE, double wF, double* loss3
     int32_t* sh = status_host(c);
     ck(cudaMemcpyAsync(sh, c->status.p, 4 * 8, cudaMemcpyDeviceToHost, c->stream), "D2H status");
     ck(cudaStreamSynchronize(c->stream), "synchronize");
+    note_rows(c, sh);
     if (sh[0] != 0) {
         finish_batch(c);   // a regrown list is rebuilt from the staged positions
         loss();

@@ -199,6 +199,27 @@ def test_capacity_growth(gpu_lib, oracle, tmp_path):
         c.close()
 
 
+def test_learned_capacity_shrinks_and_regrows(gpu_lib, oracle, tmp_path):
+    """The row capacity follows the longest rows seen (1.25 x): after a batch at the bench density it
+    shrinks for the next call, and a batch twice as dense overflows it, regrows it and is computed
+    again; every result matches the oracle."""
+    c = Context()
+    try:
+        text = cases.config_potential(c, 2, tmp_path)
+        pot = oracle.load_text(text)
+        structs = cases.small_binary(n_struc=3, seed=21)
+        dense = [(x * 0.8, t, np.asarray(R) * 0.8) for x, t, R in structs]
+        for batch in (structs, structs, dense, structs, dense):
+            offs, posn, types, cell = cases.batch(batch)
+            E, F, W = c.compute(offs, posn, types, cell, precision=FP64)
+            Eo, Fo, Wo, _, _ = pot.compute(offs, posn, types, cell)
+            assert _rel_err(E, Eo) < REL and _rel_err(F, Fo) < REL and _rel_err(W, Wo) < REL
+            Em, Fm, _ = c.compute(offs, posn, types, cell, precision=MIXED)
+            assert np.abs(Fm - Fo).max() <= 1e-3 * np.abs(Fo).max()
+    finally:
+        c.close()
+
+
 def test_errors_are_reported(ctx, tmp_path):
     from ann_gb300 import AnnError
     cases.config_potential(ctx, 2, tmp_path)
