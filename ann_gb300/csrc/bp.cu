@@ -1075,13 +1075,19 @@ __global__ void k_zero(real* p, size_t n) {
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) p[k] = real(0);
 }
 
+template <typename real>
+void launch_zero_rows(real* p, size_t n, cudaStream_t st) {
+    if (n == 0) return;
+    ++::ann::g_launch_counter, k_zero<real><<<1024, 256, 0, st>>>(p, n);
+}
+template void launch_zero_rows<float>(float*, size_t, cudaStream_t);
+template void launch_zero_rows<double>(double*, size_t, cudaStream_t);
+
 template <typename real, int PASS>
 static void launch_pass(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st) {
     if (a.natoms <= 0) return;
-    if (PASS != PASS_FORCE) {
-        real* out = (PASS == PASS_SYMM) ? a.G : a.U;
-        ++::ann::g_launch_counter, k_zero<real><<<1024, 256, 0, st>>>(out, (size_t)a.natoms * pot.imax);
-    }
+    if (PASS != PASS_FORCE && !a.out_zeroed)
+        launch_zero_rows<real>((PASS == PASS_SYMM) ? a.G : a.U, (size_t)a.natoms * pot.imax, st);
     cudaMemsetAsync(a.counter, 0, sizeof(uint32_t), st);
     auto go = [&](auto kern, size_t wb, size_t table) {
         const size_t smem = wb * BP_WARPS + table;

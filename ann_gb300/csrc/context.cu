@@ -301,11 +301,14 @@ static void enqueue_ef(ann_ctx* c, bool forces, int mode) {
         launch_type_lists(c->N, c->pot.ntypes(), c->type.as<int32_t>(), c->tcount.as<int32_t>(), c->tstart.as<int32_t>(),
                           c->tlist.as<int32_t>(), c->status.as<int32_t>(), s);
     };
+    // the side branch also clears the G rows for the symmetry pass, off the critical path
     if (side) {
         ck(cudaEventRecord(c->ev_fork, st), "event record");
         ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "stream wait");
         type_lists(c->side);
+        if (c->N > 0) launch_zero_rows<real>(c->G.as<real>(), (size_t)c->N * pot.imax, c->side);
         ck(cudaEventRecord(c->ev_join, c->side), "event record");
+        b.out_zeroed = 1;
     }
     mark(c, 0);
     // MD: the list holds rc + skin and is rebuilt only when an atom moved skin/2; between
@@ -318,10 +321,11 @@ static void enqueue_ef(ann_ctx* c, bool forces, int mode) {
     if (!side) type_lists(st);
     check_phase(c, "type lists");
     mark(c, 2);
+    if (side) ck(cudaStreamWaitEvent(st, c->ev_join, 0), "stream wait");
     launch_symm<real>(pot, b, st);
     check_phase(c, "symmetry functions");
     mark(c, 3);
-    if (side) ck(cudaStreamWaitEvent(st, c->ev_join, 0), "stream wait");
+    b.out_zeroed = 0;
     }
     enqueue_networks<real>(c, c->N, c->G, c->dEdG, c->Eatom, c->tstart, c->tlist, b.prm);
     check_phase(c, "networks");

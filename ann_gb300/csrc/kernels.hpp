@@ -89,7 +89,11 @@ struct BpArgs {
     int32_t nsm;                     // host side: streaming multiprocessors of the device
     int32_t wait_polls;              // k > 0: a neighbour-row wait gives up after k - 1 non-blocking
                                      // polls (testing the timeout path); 0: the built-in bound
+    int32_t out_zeroed;              // host side: the caller cleared the G / U rows already
 };
+// clear n reals on stream st (the G / U rows, which the passes do not write for blocks without
+// neighbours or triplets)
+template <typename real> void launch_zero_rows(real* p, size_t n, cudaStream_t st);
 template <typename real> void launch_symm(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_force(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
 template <typename real> void launch_jvp(const DevPot& pot, const BpArgs<real>& a, cudaStream_t st);
