@@ -9,12 +9,16 @@
 // Every routine restates the reference's own source; the file:line of the followed code is given
 // beside each one (paths relative to the reference project's root).
 //
-// Pinning: the special functions, cutoffs and basis functions below are checked bit-for-bit
-// against the reference's own math/special.cpp, nnp/cutoff.cpp, nnp/basis_radial.cpp and
-// nnp/basis_angular.cpp compiled from source (oracle/Makefile -> oracle/_ref/libref_basis.so).
-// The network (src/ml/nn.cpp) and the NNP loops (src/nnp/nnp.cpp) cannot be compiled here (they
-// need Eigen and the missing src/struc/ directory); they are pinned by finite-difference
-// identities and by the structure of the restatement.
+// Pinning, against the reference's own sources compiled unmodified by oracle/Makefile (with the
+// stand-ins of oracle/ref_shim/ for Eigen and for the src/struc/ headers the snapshot lacks):
+//   - special functions, cutoffs and basis functions bit for bit against math/special.cpp,
+//     nnp/cutoff.cpp, nnp/basis_radial.cpp and nnp/basis_angular.cpp (_ref/libref_basis.so);
+//   - the networks against ml/nn.cpp (_ref/libref_nn.so): initialisation bit for bit, values and
+//     gradients within 1e-13;
+//   - the assembly against nnp/nnp.cpp and nnp/nnh.cpp (_ref/libref_nnp.so): NNP::symm's
+//     symmetry functions bit for bit, NNP::energy / NNP::force / NNP::compute within 1e-13.
+// The training loss and the force-term adjoint (nnptef.cpp is stale and does not compile) are
+// pinned by finite-difference identities.
 //
 // Neighbour list: src/struc/ (NeighborList) is missing from the reference snapshot. Its contract
 // is rebuilt from the call sites (src/nnp/nnp.cpp:343-348, 478-486): every periodic image j+R*n

@@ -1,0 +1,127 @@
+// C entry points over the reference's OWN potential code (src/nnp/nnp.cpp, nnh.cpp, type.cpp and
+// the basis, network and helper sources they call), compiled from the reference sources by
+// oracle/Makefile, with the stand-ins of ref_shim/ (Eigen, and the struc/ headers that the
+// reference's sources include but do not contain), into oracle/_ref/libref_nnp.so.
+//
+// TEST INFRASTRUCTURE ONLY: tests/golden/make_golden.py and tests/ load it to pin the oracle's
+// assembly of symmetry functions, energies and forces. Nothing here is reference source; this
+// file fills a Structure and a neighbour list from arrays and calls the reference's NNP::read,
+// NNP::init, NNP::symm, NNP::energy, NNP::force and NNP::compute.
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include "struc/structure.hpp"
+#include "struc/neighbor.hpp"
+#include "struc/verlet.hpp"
+#include "nnp/nnp.hpp"
+
+static std::string g_err;
+
+// std::cout sent to a discarded buffer while in scope: NNP::compute prints its name on every call
+// (nnp.cpp:604)
+struct MuteCout {
+    std::ostringstream sink;
+    std::streambuf* old;
+    MuteCout() : old(std::cout.rdbuf(sink.rdbuf())) {}
+    ~MuteCout() { std::cout.rdbuf(old); }
+};
+
+extern "C" {
+
+const char* ref_nnp_last_error() { return g_err.c_str(); }
+
+// NNP::read of a potential file (nnp.cpp:243-307)
+void* ref_nnp_read(const char* path) {
+    try {
+        NNP* p = new NNP();
+        NNP::read(path, *p);
+        return p;
+    } catch (std::exception& e) { g_err = e.what(); return nullptr; }
+}
+void ref_nnp_free(void* h) { delete (NNP*)h; }
+int ref_nnp_ntypes(void* h) { return ((NNP*)h)->ntypes(); }
+int ref_nnp_ninput(void* h, int t) { return ((NNP*)h)->nnh(t).nInput(); }
+double ref_nnp_rc(void* h) { return ((NNP*)h)->rc(); }
+int ref_nnp_nparams(void* h) { return ((NNP*)h)->size(); }
+
+// One structure: natoms atoms with the potential's type indices `type`, positions `posn` (3 per
+// atom) and lattice vectors as the columns of R (column-major, 9 values). Neighbour entry e
+// belongs to centre atom ei[e] and is atom ej[e] seen through image img[3e..3e+2] (multiples of
+// the lattice vectors); entries are appended to their centre's row in the order given.
+//   form 0: the NeighborList functions; this file forms the pair vectors r = (x_i - x_j) - R n
+//           and their lengths; newton = 1 gives every entry the Newton's-third-law reaction
+//           (min() true), newton = 0 only the entries with a zero image;
+//   form 1: the verlet::List functions, which form the pair vectors themselves and give the
+//           reaction to zero-image entries only (nnp.cpp:550).
+// Outputs: symm (natoms rows of `width`, zero-padded) after NNP::symm; energy = NNP::energy
+// (networks + vacuum energies); force = NNP::force; pe_compute and force_compute = NNP::compute
+// (its energy has no vacuum energies).
+int ref_nnp_structure(void* h, int natoms, const int* type, const double* posn, const double* R, int nent, const int* ei,
+                      const int* ej, const int* img, int newton, int form, int width, double* symm, double* energy,
+                      double* force, double* pe_compute, double* force_compute) {
+    try {
+        NNP& nnp = *(NNP*)h;
+        Structure s;
+        s.resize(natoms);
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) s.R()(r, c) = R[3 * c + r];
+        for (int i = 0; i < natoms; ++i) {
+            if (type[i] < 0 || type[i] >= nnp.ntypes()) throw std::invalid_argument("type index out of range");
+            s.type(i) = type[i];
+            s.name(i) = nnp.nnh(type[i]).type().name();
+            for (int d = 0; d < 3; ++d) s.posn(i)[d] = posn[3 * i + d];
+        }
+        NeighborList nl;
+        verlet::List vl;
+        nl.resize(natoms);
+        vl.resize(natoms);
+        for (int e = 0; e < nent; ++e) {
+            const int i = ei[e], j = ej[e];
+            if (i < 0 || i >= natoms || j < 0 || j >= natoms) throw std::invalid_argument("neighbour index out of range");
+            Eigen::Vector3d n;
+            for (int d = 0; d < 3; ++d) n[d] = (double)img[3 * e + d];
+            const bool zero = img[3 * e] == 0 && img[3 * e + 1] == 0 && img[3 * e + 2] == 0;
+            if (form == 0) {
+                NeighborEntry x;
+                x.type_ = type[j];
+                x.index_ = j;
+                x.min_ = newton ? true : zero;
+                s.diff(s.posn(i), s.posn(j), x.r_);
+                x.r_ -= s.R() * n;
+                x.dr_ = x.r_.norm();
+                nl.add(i, x);
+            } else {
+                verlet::Entry x;
+                x.index_ = j;
+                x.cell_ = n;
+                vl.add(i, x);
+            }
+        }
+        NNP::init(nnp, s);
+        if (form == 0) NNP::symm(nnp, s, nl);
+        else NNP::symm(nnp, s, vl);
+        for (int i = 0; i < natoms; ++i) {
+            const Eigen::VectorXd& g = s.symm(i);
+            if (g.size() > width) throw std::invalid_argument("symm width too small");
+            for (int k = 0; k < width; ++k) symm[(size_t)i * width + k] = k < g.size() ? g[k] : 0.0;
+        }
+        *energy = NNP::energy(nnp, s);
+        if (form == 0) NNP::force(nnp, s, nl);
+        else NNP::force(nnp, s, vl);
+        for (int i = 0; i < natoms; ++i)
+            for (int d = 0; d < 3; ++d) force[3 * i + d] = s.force(i)[d];
+        {
+            MuteCout mute;
+            if (form == 0) NNP::compute(nnp, s, nl);
+            else NNP::compute(nnp, s, vl);
+        }
+        *pe_compute = s.pe();
+        for (int i = 0; i < natoms; ++i)
+            for (int d = 0; d < 3; ++d) force_compute[3 * i + d] = s.force(i)[d];
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+}  // extern "C"

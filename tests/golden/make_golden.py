@@ -13,10 +13,20 @@ ref_nn.npz    : outputs of the reference's OWN network code (src/ml/nn.cpp compi
                 ANN::fpbp2's output, DODZ::grad's dO/dI, Cost::grad's dO/dp and D2ODZDI::grad's
                 d2O/(dp dI), the latter projected on a fixed random input direction u (and in
                 full for two cases).
+ref_nnp.npz   : outputs of the reference's OWN potential code (src/nnp/nnp.cpp, nnh.cpp, type.cpp
+                with the basis and network sources, compiled unmodified against oracle/ref_shim/
+                into oracle/_ref/libref_nnp.so): three potentials read by NNP::read (a binary GAUSS
+                potential with input scaling, the generic-basis potential of tests/cases.py, a
+                ternary potential; all with vacuum energies) on periodic structures (random
+                binary / ternary cells, cells smaller than rc, a triclinic cell, a lone atom,
+                unwrapped coordinates), with the oracle's neighbour entries: NNP::symm's symmetry
+                functions, NNP::energy, NNP::force with the Newton's-third-law reaction on every
+                entry, the verlet::List NNP::force (reaction on untranslated entries only) and
+                NNP::compute's energy.
 The reference keeps no golden vectors of its own (its tests print, seeded from the clock), so
 these are the pins of the oracle's restatement.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--only basis|nn|nnp]
 """
 from __future__ import annotations
 
@@ -28,7 +38,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent))
-from oracle_lib import RefBasis, RefNN, eval_basisA, eval_basisR, nn_eval  # noqa: E402
+sys.path.insert(0, str(HERE.parents[1]))
+from oracle_lib import Oracle, RefBasis, RefNN, RefNNP, eval_basisA, eval_basisR, nn_eval  # noqa: E402
 
 SEED = 20261203
 
@@ -83,7 +94,6 @@ def main():
     out["angular_out"] = np.array(A_out)
     np.savez_compressed(HERE / "ref_basis.npz", **out)
     print("wrote", HERE / "ref_basis.npz", {k: v.shape for k, v in out.items()})
-    main_nn()
 
 
 # activation names in the order of NN::Neuron::Type (nn.hpp:84-103, values 1..19)
@@ -137,5 +147,87 @@ def main_nn():
     print("wrote", HERE / "ref_nn.npz", {k: v.shape for k, v in out.items()})
 
 
+def nnp_potentials():
+    """(name, text) of the three potentials of ref_nnp.npz."""
+    import cases
+    from ann_gb300 import workloads as W
+
+    def with_weights(text, names, nin, nodes, seed, scale_seed):
+        params = [W.xavier_network(seed + 100 * t, nin, nodes) for t in range(len(names))]
+        text = W.set_network_text(text, params, nin, nodes)
+        rng = np.random.default_rng(scale_seed)
+        out = []
+        for line in text.splitlines():
+            if line.startswith("inpw "):
+                line = "inpw " + " ".join(f"{x:.15f}" for x in rng.uniform(0.05, 0.5, nin)) + " "
+            elif line.startswith("inpb "):
+                line = "inpb " + " ".join(f"{x:.15f}" for x in rng.uniform(-1.0, 0.0, nin)) + " "
+            out.append(line)
+        return "\n".join(out) + "\n"
+
+    binary = with_weights(W.potential_text(["A", "B"], 6.5, 4, [0.003, 0.01], [12, 10, 1], "SOFTPLUS",
+                                           energies={"A": -0.31, "B": 0.17}), ["A", "B"], 2 * 4 + 3 * 16, [12, 10, 1], 41, 42)
+    ternary = with_weights(W.potential_text(["A", "B", "C"], 5.5, 3, [0.01], [8, 1], "TANH",
+                                            energies={"A": -0.2, "B": 0.1, "C": 0.07}), ["A", "B", "C"], 3 * 3 + 6 * 8, [8, 1], 51, 52)
+    return [("binary", binary), ("generic", cases.generic_potential_text(7)), ("ternary", ternary)]
+
+
+def nnp_structures(name):
+    """Periodic structures (posn, types, R with lattice vectors as columns) for one potential."""
+    import cases
+    from ann_gb300 import workloads as W
+    rng = np.random.default_rng(SEED + 7)
+    tiny = cases.tiny_cells()
+    if name == "binary":
+        return cases.small_binary(n_struc=2, seed=4) + tiny
+    if name == "generic":
+        return cases.small_binary(n_struc=1, seed=8) + tiny
+    box = W.config4(seed=SEED + 9, dims=(5, 5, 4))
+    R = np.array([[6.0, 1.2, 0.4], [0.0, 5.6, 0.9], [0.0, 0.0, 6.3]])
+    x = rng.uniform(0, 1, (14, 3)) @ R.T
+    return box + [(x, rng.integers(0, 3, 14).astype(np.int32), R)]
+
+
+def main_nnp():
+    import tempfile
+    ref, orc = RefNNP(), Oracle()
+    out = {}
+    names = []
+    k = 0
+    for pi, (name, text) in enumerate(nnp_potentials()):
+        names.append(name)
+        out[f"pot_{name}"] = np.array(text)
+        with tempfile.NamedTemporaryFile("w", suffix=".ann", delete=False) as f:
+            f.write(text)
+            path = f.name
+        h = ref.read(path)
+        Path(path).unlink()
+        rc = ref.L.ref_nnp_rc(h)
+        assert ref.L.ref_nnp_nparams(h) == orc.load_text(text).nparams
+        for x, t, R in nnp_structures(name):
+            x = np.asarray(x, np.float64); t = np.asarray(t, np.int32); R = np.asarray(R, np.float64)
+            i, j, img, _, _ = orc.neighbors(x, R, rc)
+            G, E, F, Ec, Fc = ref.structure(h, t, x, R, i, j, img, newton=1, form=0)
+            assert np.array_equal(F, Fc), "NNP::force and NNP::compute disagree"
+            Gv, Ev, Fu, _, _ = ref.structure(h, t, x, R, i, j, img, newton=0, form=1)
+            Gn, En, Fn, _, _ = ref.structure(h, t, x, R, i, j, img, newton=0, form=0)
+            assert np.array_equal(Gv, G) and Ev == E and np.array_equal(Fn, Fu), "list forms disagree"
+            out.update({f"c{k}_pot": np.array(pi), f"c{k}_posn": x, f"c{k}_types": t, f"c{k}_R": R, f"c{k}_symm": G,
+                        f"c{k}_energy": np.array(E), f"c{k}_force": F, f"c{k}_force_untranslated": Fu,
+                        f"c{k}_energy_compute": np.array(Ec)})
+            k += 1
+        ref.L.ref_nnp_free(h)
+    out["pot_names"] = np.array(names)
+    out["ncases"] = np.array(k)
+    np.savez_compressed(HERE / "ref_nnp.npz", **out)
+    print("wrote", HERE / "ref_nnp.npz", k, "structures")
+
+
 if __name__ == "__main__":
-    main()
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["basis", "nn", "nnp"])
+    a = ap.parse_args()
+    for part, fn in (("basis", main), ("nn", main_nn), ("nnp", main_nnp)):
+        if a.only in (None, part):
+            fn()

@@ -18,6 +18,7 @@ ORACLE_DIR = ROOT / "oracle"
 ORACLE_SO = ORACLE_DIR / "_build" / "libann_oracle.so"
 REF_SO = ORACLE_DIR / "_ref" / "libref_basis.so"
 REF_NN_SO = ORACLE_DIR / "_ref" / "libref_nn.so"
+REF_NNP_SO = ORACLE_DIR / "_ref" / "libref_nnp.so"
 ORACLE_TIMED_SO = ORACLE_DIR / "_build" / "libann_oracle_timed.so"
 
 
@@ -309,6 +310,48 @@ class RefNN:
         v = np.zeros(self.L.ref_nn_size(h))
         self.L.ref_nn_get_params(h, _d(v))
         return v
+
+
+class RefNNP:
+    """The reference's own potential code (nnp/nnp.cpp, nnh.cpp, type.cpp with the basis and
+    network sources) compiled with the stand-ins of oracle/ref_shim/."""
+
+    def __init__(self):
+        if not REF_NNP_SO.exists():
+            if not REF_SRC.exists():
+                raise FileNotFoundError("reference sources not available")
+            build_oracle(ref=True)
+        L = self.L = C.CDLL(str(REF_NNP_SO))
+        L.ref_nnp_last_error.restype = C.c_char_p
+        L.ref_nnp_read.restype = C.c_void_p
+        L.ref_nnp_read.argtypes = [C.c_char_p]
+        for f in ("ref_nnp_free", "ref_nnp_ntypes", "ref_nnp_rc", "ref_nnp_nparams"):
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.ref_nnp_rc.restype = C.c_double
+        L.ref_nnp_ninput.argtypes = [C.c_void_p, C.c_int]
+        L.ref_nnp_structure.argtypes = [C.c_void_p, C.c_int, _I, _D, _D, C.c_int, _I, _I, _I, C.c_int, C.c_int, C.c_int,
+                                        _D, _D, _D, _D, _D]
+
+    def read(self, path):
+        h = self.L.ref_nnp_read(str(path).encode())
+        if not h:
+            raise RuntimeError(self.L.ref_nnp_last_error().decode())
+        return C.c_void_p(h)
+
+    def structure(self, h, types, posn, R, ei, ej, img, newton=1, form=0):
+        """(symm, E, F, E_compute, F_compute) of one structure (R: lattice vectors as columns)."""
+        n = len(types)
+        width = max(self.L.ref_nnp_ninput(h, t) for t in range(self.L.ref_nnp_ntypes(h)))
+        G = np.zeros((n, width)); F = np.zeros((n, 3)); Fc = np.zeros((n, 3))
+        E, Ec = np.zeros(1), np.zeros(1)
+        Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
+        rc = self.L.ref_nnp_structure(h, n, _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(posn, np.float64)),
+                                      _d(Rc), len(ei), _i(np.ascontiguousarray(ei, np.int32)), _i(np.ascontiguousarray(ej, np.int32)),
+                                      _i(np.ascontiguousarray(img, np.int32)), int(newton), int(form), width, _d(G), _d(E), _d(F),
+                                      _d(Ec), _d(Fc))
+        if rc != 0:
+            raise RuntimeError(self.L.ref_nnp_last_error().decode())
+        return G, float(E[0]), F, float(Ec[0]), Fc
 
 
 class RefBasis:

@@ -226,3 +226,87 @@ def test_networks_against_fresh_reference_build(oracle):
                 assert _close(b[3], d2ref, 1e-12), name
         finally:
             ref.L.ref_nn_free(h)
+
+
+# ---- the assembly: the reference's own nnp.cpp / nnh.cpp (NNP::symm, energy, force, compute)
+
+NNP_GOLD = Path(__file__).resolve().parent / "golden" / "ref_nnp.npz"
+
+
+@pytest.fixture(scope="module")
+def nnp_gold():
+    return np.load(NNP_GOLD)
+
+
+def _vacuum_energies(text):
+    """Per-type vacuum energies of a potential text ('name X mass m energy e' lines, type order)."""
+    return np.array([float(ln.split()[5]) for ln in text.splitlines() if ln.startswith("name ")])
+
+
+def _nnp_cases(gold):
+    names = [str(n) for n in gold["pot_names"]]
+    for k in range(int(gold["ncases"])):
+        name = names[int(gold[f"c{k}_pot"])]
+        yield (k, name, str(gold[f"pot_{name}"]), gold[f"c{k}_posn"], gold[f"c{k}_types"], gold[f"c{k}_R"])
+
+
+def _assembly_matches(pot, evac, x, t, R, G_ref, E_ref, F_ref, Fu_ref, Ec_ref, label):
+    from ann_gb300.api import pack_batch
+    offs, posn, types, cell = pack_batch([(x, t, R)])
+    E, F, _, G, _ = pot.compute(offs, posn, types, cell, forces=True, symm=True, newton=1)
+    assert np.array_equal(G[:, :G_ref.shape[1]], G_ref), f"{label}: symmetry functions differ"
+    assert abs(E[0] - E_ref) <= 1e-13 * max(1.0, abs(E_ref)), f"{label}: energy {E[0]} vs {E_ref}"
+    fs = max(1.0, float(np.abs(F_ref).max()))
+    assert np.abs(F - F_ref).max() <= 1e-13 * fs, f"{label}: forces"
+    _, Fu, _, _, _ = pot.compute(offs, posn, types, cell, forces=True, newton=0)
+    assert np.abs(Fu - Fu_ref).max() <= 1e-13 * fs, f"{label}: forces with untranslated reactions"
+    # NNP::compute's energy is the networks' sum alone; NNP::energy adds each atom's vacuum energy
+    assert abs((E_ref - Ec_ref) - evac[t].sum()) <= 1e-12 * max(1.0, abs(E_ref)), label
+
+
+def test_potential_assembly_against_reference(oracle, nnp_gold):
+    """The oracle against the reference's own NNP::symm / energy / force / compute on 13
+    structures of three potentials (tests/golden/ref_nnp.npz): the symmetry functions bit for bit
+    (same neighbour entries in the same order, so the same sums), energies and forces within
+    1e-13 (the force sums run in another order); forces with the Newton's-third-law reaction on
+    every neighbour entry, and with the reaction on untranslated entries only (the verlet::List
+    rule of nnp.cpp:550); NNP::compute's energy without the vacuum energies (nnp.cpp:617)."""
+    pots = {}
+    for k, name, text, x, t, R in _nnp_cases(nnp_gold):
+        if name not in pots:
+            pots[name] = (oracle.load_text(text), _vacuum_energies(text))
+        pot, evac = pots[name]
+        _assembly_matches(pot, evac, x, t, R, nnp_gold[f"c{k}_symm"], float(nnp_gold[f"c{k}_energy"]), nnp_gold[f"c{k}_force"],
+                          nnp_gold[f"c{k}_force_untranslated"], float(nnp_gold[f"c{k}_energy_compute"]), f"case {k} ({name})")
+
+
+@needs_ref
+def test_potential_assembly_against_fresh_reference_build(oracle, tmp_path):
+    """New random structures of each golden potential through a fresh build of the reference's
+    nnp.cpp (NNP::read of the same file), with the oracle's neighbour entries."""
+    import cases
+    from oracle_lib import RefNNP
+    ref = RefNNP()
+    gold = np.load(NNP_GOLD)
+    rng = np.random.default_rng(77)
+    for name in [str(n) for n in gold["pot_names"]]:
+        text = str(gold[f"pot_{name}"])
+        p = tmp_path / f"{name}.ann"
+        p.write_text(text)
+        h = ref.read(p)
+        try:
+            pot, evac = oracle.load_text(text), _vacuum_energies(text)
+            nt = len(evac)
+            assert ref.L.ref_nnp_nparams(h) == pot.nparams and ref.L.ref_nnp_ntypes(h) == nt
+            rc = ref.L.ref_nnp_rc(h)
+            structs = [(x, (t % nt).astype(np.int32), R) for x, t, R in cases.small_binary(n_struc=1, seed=int(rng.integers(1, 999)))]
+            A = np.array([[5.0, 0.8, -0.6], [0.0, 4.6, 1.1], [0.0, 0.0, 5.3]])
+            structs.append((rng.uniform(-0.5, 1.5, (9, 3)) @ A.T, rng.integers(0, nt, 9).astype(np.int32), A))
+            for x, t, R in structs:
+                i, j, img, _, _ = oracle.neighbors(x, R, rc)
+                G, E, F, Ec, Fc = ref.structure(h, t, x, R, i, j, img, newton=1, form=0)
+                _, _, Fu, _, _ = ref.structure(h, t, x, R, i, j, img, newton=0, form=1)
+                assert np.array_equal(F, Fc)
+                _assembly_matches(pot, evac, x, t, R, G, E, F, Fu, Ec, name)
+        finally:
+            ref.L.ref_nnp_free(h)
