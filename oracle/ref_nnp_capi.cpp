@@ -6,7 +6,7 @@
 // TEST INFRASTRUCTURE ONLY: tests/golden/make_golden.py and tests/ load it to pin the oracle's
 // assembly of symmetry functions, energies and forces. Nothing here is reference source; this
 // file fills a Structure and a neighbour list from arrays and calls the reference's NNP::read,
-// NNP::init, NNP::symm, NNP::energy, NNP::force and NNP::compute.
+// NNP::write, NNP::init, NNP::symm, NNP::energy, NNP::force and NNP::compute.
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
@@ -45,6 +45,13 @@ int ref_nnp_ntypes(void* h) { return ((NNP*)h)->ntypes(); }
 int ref_nnp_ninput(void* h, int t) { return ((NNP*)h)->nnh(t).nInput(); }
 double ref_nnp_rc(void* h) { return ((NNP*)h)->rc(); }
 int ref_nnp_nparams(void* h) { return ((NNP*)h)->size(); }
+// NNP::write to a file (nnp.cpp:197-236)
+int ref_nnp_write(void* h, const char* path) {
+    try {
+        NNP::write(path, *(NNP*)h);
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
 
 // One structure: natoms atoms with the potential's type indices `type`, positions `posn` (3 per
 // atom) and lattice vectors as the columns of R (column-major, 9 values). Neighbour entry e

@@ -329,6 +329,7 @@ class RefNNP:
             getattr(L, f).argtypes = [C.c_void_p]
         L.ref_nnp_rc.restype = C.c_double
         L.ref_nnp_ninput.argtypes = [C.c_void_p, C.c_int]
+        L.ref_nnp_write.argtypes = [C.c_void_p, C.c_char_p]
         L.ref_nnp_structure.argtypes = [C.c_void_p, C.c_int, _I, _D, _D, C.c_int, _I, _I, _I, C.c_int, C.c_int, C.c_int,
                                         _D, _D, _D, _D, _D]
 
@@ -337,6 +338,10 @@ class RefNNP:
         if not h:
             raise RuntimeError(self.L.ref_nnp_last_error().decode())
         return C.c_void_p(h)
+
+    def write(self, h, path):
+        if self.L.ref_nnp_write(h, str(path).encode()) != 0:
+            raise RuntimeError(self.L.ref_nnp_last_error().decode())
 
     def structure(self, h, types, posn, R, ei, ej, img, newton=1, form=0):
         """(symm, E, F, E_compute, F_compute) of one structure (R: lattice vectors as columns)."""
