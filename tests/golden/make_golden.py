@@ -22,7 +22,9 @@ ref_nnp.npz   : outputs of the reference's OWN potential code (src/nnp/nnp.cpp, 
                 unwrapped coordinates), with the oracle's neighbour entries: NNP::symm's symmetry
                 functions, NNP::energy, NNP::force with the Newton's-third-law reaction on every
                 entry, the verlet::List NNP::force (reaction on untranslated entries only) and
-                NNP::compute's energy.
+                NNP::compute's energy; and the MD engine's ptnl::PotNNPE::compute
+                (src/torch/pot_nnpe.cpp) on the same entries: its energy, and the largest
+                difference of its forces from NNP::force's.
 The reference keeps no golden vectors of its own (its tests print, seeded from the clock), so
 these are the pins of the oracle's restatement.
 
@@ -201,8 +203,9 @@ def main_nnp():
             f.write(text)
             path = f.name
         h = ref.read(path)
-        Path(path).unlink()
         rc = ref.L.ref_nnp_rc(h)
+        hp = ref.potnnpe_read(path, rc)
+        Path(path).unlink()
         assert ref.L.ref_nnp_nparams(h) == orc.load_text(text).nparams
         for x, t, R in nnp_structures(name):
             x = np.asarray(x, np.float64); t = np.asarray(t, np.int32); R = np.asarray(R, np.float64)
@@ -212,11 +215,14 @@ def main_nnp():
             Gv, Ev, Fu, _, _ = ref.structure(h, t, x, R, i, j, img, newton=0, form=1)
             Gn, En, Fn, _, _ = ref.structure(h, t, x, R, i, j, img, newton=0, form=0)
             assert np.array_equal(Gv, G) and Ev == E and np.array_equal(Fn, Fu), "list forms disagree"
+            Ep, Fp = ref.potnnpe_compute(hp, t, x, R, i, j, img)
             out.update({f"c{k}_pot": np.array(pi), f"c{k}_posn": x, f"c{k}_types": t, f"c{k}_R": R, f"c{k}_symm": G,
                         f"c{k}_energy": np.array(E), f"c{k}_force": F, f"c{k}_force_untranslated": Fu,
-                        f"c{k}_energy_compute": np.array(Ec)})
+                        f"c{k}_energy_compute": np.array(Ec), f"c{k}_energy_potnnpe": np.array(Ep),
+                        f"c{k}_force_potnnpe_vs_force": np.array(np.abs(Fp - F).max())})
             k += 1
         ref.L.ref_nnp_free(h)
+        ref.L.ref_potnnpe_free(hp)
     out["pot_names"] = np.array(names)
     out["ncases"] = np.array(k)
     np.savez_compressed(HERE / "ref_nnp.npz", **out)

@@ -330,6 +330,10 @@ class RefNNP:
         L.ref_nnp_rc.restype = C.c_double
         L.ref_nnp_ninput.argtypes = [C.c_void_p, C.c_int]
         L.ref_nnp_write.argtypes = [C.c_void_p, C.c_char_p]
+        L.ref_potnnpe_read.restype = C.c_void_p
+        L.ref_potnnpe_read.argtypes = [C.c_char_p, C.c_double]
+        L.ref_potnnpe_free.argtypes = [C.c_void_p]
+        L.ref_potnnpe_structure.argtypes = [C.c_void_p, C.c_int, _I, _D, _D, C.c_int, _I, _I, _I, C.c_int, _D, _D]
         L.ref_nnp_structure.argtypes = [C.c_void_p, C.c_int, _I, _D, _D, C.c_int, _I, _I, _I, C.c_int, C.c_int, C.c_int,
                                         _D, _D, _D, _D, _D]
 
@@ -338,6 +342,26 @@ class RefNNP:
         if not h:
             raise RuntimeError(self.L.ref_nnp_last_error().decode())
         return C.c_void_p(h)
+
+    def potnnpe_read(self, path, rc):
+        """The MD engine's ptnl::PotNNPE reading a potential file (its cutoff set first, as the
+        engine's pot line does)."""
+        h = self.L.ref_potnnpe_read(str(path).encode(), float(rc))
+        if not h:
+            raise RuntimeError(self.L.ref_nnp_last_error().decode())
+        return C.c_void_p(h)
+
+    def potnnpe_compute(self, h, types, posn, R, ei, ej, img, newton=1):
+        """(E, F) of PotNNPE::compute on one structure."""
+        n = len(types)
+        E, F = np.zeros(1), np.zeros((n, 3))
+        Rc = np.ascontiguousarray(np.asarray(R, np.float64).T.reshape(9))
+        rc = self.L.ref_potnnpe_structure(h, n, _i(np.ascontiguousarray(types, np.int32)), _d(np.ascontiguousarray(posn, np.float64)),
+                                          _d(Rc), len(ei), _i(np.ascontiguousarray(ei, np.int32)), _i(np.ascontiguousarray(ej, np.int32)),
+                                          _i(np.ascontiguousarray(img, np.int32)), int(newton), _d(E), _d(F))
+        if rc != 0:
+            raise RuntimeError(self.L.ref_nnp_last_error().decode())
+        return float(E[0]), F
 
     def write(self, h, path):
         if self.L.ref_nnp_write(h, str(path).encode()) != 0:

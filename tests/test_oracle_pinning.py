@@ -270,20 +270,25 @@ def test_potential_assembly_against_reference(oracle, nnp_gold):
     (same neighbour entries in the same order, so the same sums), energies and forces within
     1e-13 (the force sums run in another order); forces with the Newton's-third-law reaction on
     every neighbour entry, and with the reaction on untranslated entries only (the verlet::List
-    rule of nnp.cpp:550); NNP::compute's energy without the vacuum energies (nnp.cpp:617)."""
+    rule of nnp.cpp:550); NNP::compute's energy without the vacuum energies (nnp.cpp:617). The
+    MD engine's PotNNPE::compute (torch/pot_nnpe.cpp:169-288), the call the library's ann_compute
+    stands in for, gave NNP::energy's energy and NNP::force's forces bit for bit."""
     pots = {}
     for k, name, text, x, t, R in _nnp_cases(nnp_gold):
         if name not in pots:
             pots[name] = (oracle.load_text(text), _vacuum_energies(text))
         pot, evac = pots[name]
-        _assembly_matches(pot, evac, x, t, R, nnp_gold[f"c{k}_symm"], float(nnp_gold[f"c{k}_energy"]), nnp_gold[f"c{k}_force"],
+        E_ref = float(nnp_gold[f"c{k}_energy"])
+        _assembly_matches(pot, evac, x, t, R, nnp_gold[f"c{k}_symm"], E_ref, nnp_gold[f"c{k}_force"],
                           nnp_gold[f"c{k}_force_untranslated"], float(nnp_gold[f"c{k}_energy_compute"]), f"case {k} ({name})")
+        assert float(nnp_gold[f"c{k}_energy_potnnpe"]) == E_ref and float(nnp_gold[f"c{k}_force_potnnpe_vs_force"]) == 0.0
 
 
 @needs_ref
 def test_potential_assembly_against_fresh_reference_build(oracle, tmp_path):
     """New random structures of each golden potential through a fresh build of the reference's
-    nnp.cpp (NNP::read of the same file), with the oracle's neighbour entries."""
+    nnp.cpp (NNP::read of the same file) and of the MD engine's PotNNPE, with the oracle's
+    neighbour entries."""
     import cases
     from oracle_lib import RefNNP
     ref = RefNNP()
@@ -294,6 +299,7 @@ def test_potential_assembly_against_fresh_reference_build(oracle, tmp_path):
         p = tmp_path / f"{name}.ann"
         p.write_text(text)
         h = ref.read(p)
+        hp = ref.potnnpe_read(p, ref.L.ref_nnp_rc(h))
         try:
             pot, evac = oracle.load_text(text), _vacuum_energies(text)
             nt = len(evac)
@@ -308,5 +314,8 @@ def test_potential_assembly_against_fresh_reference_build(oracle, tmp_path):
                 _, _, Fu, _, _ = ref.structure(h, t, x, R, i, j, img, newton=0, form=1)
                 assert np.array_equal(F, Fc)
                 _assembly_matches(pot, evac, x, t, R, G, E, F, Fu, Ec, name)
+                Ep, Fp = ref.potnnpe_compute(hp, t, x, R, i, j, img)
+                assert abs(Ep - E) <= 1e-13 * max(1.0, abs(E)) and np.abs(Fp - F).max() <= 1e-13 * max(1.0, np.abs(F).max()), name
         finally:
             ref.L.ref_nnp_free(h)
+            ref.L.ref_potnnpe_free(hp)

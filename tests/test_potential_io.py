@@ -84,8 +84,9 @@ def test_library_writer_equals_reference_writer(pio, tmp_path):
 
 @needs_ref
 def test_reference_computes_from_library_file(oracle, pio, tmp_path):
-    """The reference reads a file the library wrote and computes the golden structures' symmetry
-    functions, energies and forces as the oracle does from the original text."""
+    """The reference (NNP::read, and the MD engine's PotNNPE::read) reads a file the library wrote
+    and computes the golden structures' symmetry functions, energies and forces as the oracle does
+    from the original text."""
     from oracle_lib import RefNNP
     from ann_gb300.api import pack_batch
     ref = RefNNP()
@@ -97,14 +98,19 @@ def test_reference_computes_from_library_file(oracle, pio, tmp_path):
         p = tmp_path / f"{name}.lib.ann"
         p.write_text(pio(text))
         h = ref.read(p)
+        hp = ref.potnnpe_read(p, ref.L.ref_nnp_rc(h))
         try:
             x, t, R = gold[f"c{k}_posn"], gold[f"c{k}_types"], gold[f"c{k}_R"]
             i, j, img, _, _ = oracle.neighbors(x, R, ref.L.ref_nnp_rc(h))
             G, E, F, _, _ = ref.structure(h, t, x, R, i, j, img)
+            Ep, Fp = ref.potnnpe_compute(hp, t, x, R, i, j, img)
         finally:
             ref.L.ref_nnp_free(h)
+            ref.L.ref_potnnpe_free(hp)
         offs, posn, types, cell = pack_batch([(x, t, R)])
         E0, F0, _, G0, _ = oracle.load_text(text).compute(offs, posn, types, cell, forces=True, symm=True)
         assert np.array_equal(G, G0[:, :G.shape[1]]), k
         assert abs(E - E0[0]) <= 1e-13 * max(1.0, abs(E0[0])), k
         assert np.abs(F - F0).max() <= 1e-13 * max(1.0, np.abs(F0).max()), k
+        assert abs(Ep - E0[0]) <= 1e-13 * max(1.0, abs(E0[0])), k
+        assert np.abs(Fp - F0).max() <= 1e-13 * max(1.0, np.abs(F0).max()), k
