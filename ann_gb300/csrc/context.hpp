@@ -178,7 +178,7 @@ struct ann_ctx {
     DevBuf md_R_d, md_Ri_d;
     int md_rebuilds = 0;
     // a caller's neighbour list (ann_compute_list): inputs, rows and results, apart from the batch
-    DevBuf lx, ltype, lilist, lnoff, lneigh, lrtype, lnn, lntc, lnj, lnr, lG, ldEdG, lEatom, lF, lW, lFout, ltcount, ltstart, ltlist,
+    DevBuf lx, lxh, lxl, ltype, lilist, lnoff, lneigh, lrtype, lnn, lntc, lnj, lnr, lG, ldEdG, lEatom, lF, lW, lFout, ltcount, ltstart, ltlist,
         ltables, lpartial, lEs, lWs;
     int list_hint = 0;              // longest row within rc seen so far
     bool list_staged = false, list_have_ilist = false;   // a list on the device that ANN_LIST_KEEP may reuse

@@ -5,10 +5,17 @@
 // (src/nnp/nnp.cpp:601-665), where the caller builds the NeighborList.
 //
 // One warp per row (one centre atom). The row's entries are read from the caller's list, the pair
-// vector r = x_centre - x_neighbour is formed in FP64 from the given positions (ghost atoms carry
-// their image shift already), entries with |r| >= rc are dropped (a list built with a skin holds
-// them), and the rest are written type-sorted, as the list builder writes its rows: per neighbour
-// type a contiguous range, ntc[row*T + t] entries long, in list order inside the range.
+// vector r = x_centre - x_neighbour is formed from the given positions (ghost atoms carry their
+// image shift already), entries with |r| >= rc are dropped (a list built with a skin holds them),
+// and the rest are written type-sorted, as the list builder writes its rows: per neighbour type a
+// contiguous range, ntc[row*T + t] entries long, in list order inside the range.
+//
+// The FP64 form forms r in FP64. The mixed form forms it in FP32 from positions split once per
+// call into FP32 hi and lo parts (k_split_positions): r = (hi_i - hi_j) + (lo_i - lo_j). For an
+// entry within the list radius the hi difference is rounded by at most half an FP32 ulp of |r| and
+// the lo difference is near exact, so r is as accurate as an FP64 difference rounded to FP32, the
+// mixed rows' format. No FP64 arithmetic is done per entry: this part issues FP64 at a small
+// fraction of its FP32 rate, and the per-entry FP64 difference, norm and test bounded the kernel.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cmath>
@@ -17,6 +24,20 @@
 namespace ann {
 
 constexpr int LR_WARPS = 8;
+
+// the mixed form's hi / lo parts of every position, and the type bits beside the hi part
+__global__ void __launch_bounds__(256) k_split_positions(int n, const double* x, const int32_t* type, float4* xh, float4* xl) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+        float h[3], l[3];
+        for (int d = 0; d < 3; ++d) {
+            const double v = x[3 * (size_t)a + d];
+            h[d] = __double2float_rn(v);
+            l[d] = __double2float_rn(v - (double)h[d]);
+        }
+        xh[a] = make_float4(h[0], h[1], h[2], __int_as_float(type[a]));
+        xl[a] = make_float4(l[0], l[1], l[2], 0.0f);
+    }
+}
 
 template <bool FP64>
 __global__ void __launch_bounds__(LR_WARPS * 32) k_list_rows(ListArgs a) {
@@ -29,6 +50,8 @@ __global__ void __launch_bounds__(LR_WARPS * 32) k_list_rows(ListArgs a) {
         const int I = bad ? -1 : a.type[i];
         double xi[3] = {0.0, 0.0, 0.0};
         if (!bad) { xi[0] = a.x[3 * (size_t)i]; xi[1] = a.x[3 * (size_t)i + 1]; xi[2] = a.x[3 * (size_t)i + 2]; }
+        float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+        if (!FP64 && !bad) { hi = a.xh[i]; lo = a.xl[i]; }
         if (lane == 0) {
             a.rtype[r] = I;   // an out-of-range type is reported by the symmetry-function kernel
             if (bad) atomicOr(a.status, (int)ST_BAD_INDEX);
@@ -45,20 +68,33 @@ __global__ void __launch_bounds__(LR_WARPS * 32) k_list_rows(ListArgs a) {
                 bool keep = false;
                 int j = -1;
                 double rx = 0.0, ry = 0.0, rz = 0.0, d2 = 0.0;
+                float fx = 0.f, fy = 0.f, fz = 0.f, fd2 = 0.f;
                 if (e < cin) {
                     j = a.neigh[b0 + e];
                     if (j < 0 || j >= a.nall) {
                         if (t == 0) atomicOr(a.status, (int)ST_BAD_INDEX);
                     } else {
-                        const int tj = a.type[j];
+                        float4 hj;
+                        if (!FP64) hj = a.xh[j];
+                        const int tj = FP64 ? a.type[j] : __float_as_int(hj.w);
                         if (t == 0 && (tj < 0 || tj >= T)) atomicOr(a.status, (int)ST_BAD_TYPE);
                         if (tj == t || t == 0) {   // the first pass also checks every neighbour's position
-                            rx = xi[0] - a.x[3 * (size_t)j];
-                            ry = xi[1] - a.x[3 * (size_t)j + 1];
-                            rz = xi[2] - a.x[3 * (size_t)j + 2];
-                            d2 = rx * rx + ry * ry + rz * rz;
-                            if (t == 0 && !isfinite(d2)) atomicOr(a.status, (int)ST_NONFINITE);
-                            keep = tj == t && d2 < a.rc2 && d2 > 0.0;
+                            if (FP64) {
+                                rx = xi[0] - a.x[3 * (size_t)j];
+                                ry = xi[1] - a.x[3 * (size_t)j + 1];
+                                rz = xi[2] - a.x[3 * (size_t)j + 2];
+                                d2 = rx * rx + ry * ry + rz * rz;
+                                if (t == 0 && !isfinite(d2)) atomicOr(a.status, (int)ST_NONFINITE);
+                                keep = tj == t && d2 < a.rc2 && d2 > 0.0;
+                            } else {
+                                const float4 lj = a.xl[j];
+                                fx = (hi.x - hj.x) + (lo.x - lj.x);
+                                fy = (hi.y - hj.y) + (lo.y - lj.y);
+                                fz = (hi.z - hj.z) + (lo.z - lj.z);
+                                fd2 = fx * fx + fy * fy + fz * fz;
+                                if (t == 0 && !isfinite(fd2)) atomicOr(a.status, (int)ST_NONFINITE);
+                                keep = tj == t && fd2 < a.rc2f && fd2 > 0.0f;
+                            }
                         }
                     }
                 }
@@ -66,12 +102,8 @@ __global__ void __launch_bounds__(LR_WARPS * 32) k_list_rows(ListArgs a) {
                 const int o = base + ct + __popc(msk & lt);
                 if (keep && o < cap) {
                     a.nj[row + o] = j;
-                    if (FP64) {
-                        reinterpret_cast<Vec4d*>(a.nr)[row + o] = Vec4d{rx, ry, rz, sqrt(d2)};
-                    } else {
-                        const float fx = (float)rx, fy = (float)ry, fz = (float)rz;
-                        reinterpret_cast<Vec4f*>(a.nr)[row + o] = Vec4f{fx, fy, fz, sqrtf(fx * fx + fy * fy + fz * fz)};
-                    }
+                    if (FP64) reinterpret_cast<Vec4d*>(a.nr)[row + o] = Vec4d{rx, ry, rz, sqrt(d2)};
+                    else reinterpret_cast<Vec4f*>(a.nr)[row + o] = Vec4f{fx, fy, fz, sqrtf(fd2)};
                 }
                 ct += __popc(msk);
             }
@@ -90,6 +122,10 @@ __global__ void __launch_bounds__(LR_WARPS * 32) k_list_rows(ListArgs a) {
 
 void launch_list_rows(const ListArgs& a, bool fp64, cudaStream_t st) {
     if (a.nrows <= 0) return;
+    if (!fp64 && a.nall > 0) {
+        const int g = std::min((a.nall + 255) / 256, std::max(1, (int)a.nsm) * 8);
+        ++::ann::g_launch_counter, k_split_positions<<<g, 256, 0, st>>>(a.nall, a.x, a.type, a.xh, a.xl);
+    }
     const int threads = LR_WARPS * 32;
     int grid = (a.nrows + LR_WARPS - 1) / LR_WARPS;
     grid = std::min(grid, std::max(1, (int)a.nsm) * 8);

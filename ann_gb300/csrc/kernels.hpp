@@ -108,6 +108,9 @@ struct ListArgs {
     const int32_t* neigh;            // [noff[nrows]] neighbour atoms, indices into [0, nall)
     const double* x;                 // [3*nall] positions of local and ghost atoms
     const int32_t* type;             // [nall]
+    float4* xh;                      // mixed form: [nall] FP32 hi parts of the positions + type bits
+    float4* xl;                      // mixed form: [nall] FP32 lo parts (x - hi)
+    float rc2f;                      // rc2 in FP32 (mixed form)
     int32_t* rtype;                  // [nrows] centre type of each row
     int32_t* nn;                     // [nrows]
     int32_t* ntc;                    // [nrows*T]

@@ -85,6 +85,7 @@ int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32
         const size_t rb = fp64 ? sizeof(double) : sizeof(float);
         const int64_t launches0 = g_launch_counter;
         c->lx.ensure(sizeof(double) * 3 * (size_t)std::max(nall, 1));
+        if (!fp64) { c->lxh.ensure(16 * (size_t)std::max(nall, 1)); c->lxl.ensure(16 * (size_t)std::max(nall, 1)); }
         if (nall > 0) ck(cudaMemcpyAsync(c->lx.p, x, sizeof(double) * 3 * (size_t)nall, cudaMemcpyHostToDevice, st), "H2D x");
         // reduction chunks of the rows: {0, nchunks} then (structure 0, first row, end row) per chunk
         const int nch = (inum + RED_CHUNK - 1) / RED_CHUNK;
@@ -121,6 +122,7 @@ int ann_compute_list(ann_ctx* c, int32_t inum, const int32_t* ilist, const int32
             la.ilist = have_ilist ? c->lilist.as<int32_t>() : nullptr; la.noff = c->lnoff.as<int64_t>(); la.neigh = c->lneigh.as<int32_t>();
             la.x = c->lx.as<double>(); la.type = c->ltype.as<int32_t>(); la.rtype = c->lrtype.as<int32_t>(); la.nn = c->lnn.as<int32_t>();
             la.ntc = c->lntc.as<int32_t>(); la.nj = c->lnj.as<int32_t>(); la.nr = c->lnr.p; la.status = c->status.as<int32_t>();
+            la.xh = fp64 ? nullptr : c->lxh.as<float4>(); la.xl = fp64 ? nullptr : c->lxl.as<float4>(); la.rc2f = (float)la.rc2;
             la.nsm = c->nsm;
             launch_list_rows(la, fp64, st);
             if (fp64) enqueue_list<double>(c, inum, nall, cap, nch, want_f, have_ilist);
