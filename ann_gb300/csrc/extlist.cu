@@ -11,10 +11,12 @@
 // contiguous range, ntc[row*T + t] entries long, in list order inside the range.
 //
 // The FP64 form forms r in FP64. The mixed form forms it in FP32 from positions split once per
-// call into FP32 hi and lo parts (k_split_positions): r = (hi_i - hi_j) + (lo_i - lo_j). For an
-// entry within the list radius the hi difference is rounded by at most half an FP32 ulp of |r| and
-// the lo difference is near exact, so r is as accurate as an FP64 difference rounded to FP32, the
-// mixed rows' format. No FP64 arithmetic is done per entry: this part issues FP64 at a small
+// call into FP32 hi and lo parts (k_split_positions): r = (hi_i - hi_j) + (lo_i - lo_j). The hi
+// difference and the final sum each round by at most half an FP32 ulp of |r|, and the lo parts
+// carry the coordinates' own rounding to 24 bits, so for entries within 8 A every component lies
+// within 5e-7 A of the exact difference at coordinates up to 2e7 A, and within one FP32 ulp of
+// |r| at coordinates up to 1000 A (the FP64 difference rounded to FP32, the mixed rows' format, is
+// within half an ulp). No FP64 arithmetic is done per entry: this part issues FP64 at a small
 // fraction of its FP32 rate, and the per-entry FP64 difference, norm and test bounded the kernel.
 #include <cuda_runtime.h>
 #include <cstdint>

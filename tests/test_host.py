@@ -181,3 +181,32 @@ def test_xyz_round_trip_and_wrapping(tmp_path):
     offs, posn, types, cell = batch_from_xyz(Names(), [r, b])
     assert list(offs) == [0, 5, 7] and list(types) == [0, 1, 0, 0, 1, 0, 0]
     assert np.allclose(cell[0].reshape(3, 3).T, R, atol=1e-6)
+
+
+def test_split_position_pair_vectors():
+    """The mixed caller-list rows' pair vectors (csrc/extlist.cu): positions split into FP32 hi and
+    lo parts, r = (hi_i - hi_j) + (lo_i - lo_j) in FP32 arithmetic. For entries within 8 A every
+    component lies within 5e-7 A of the exact difference at coordinates up to 2e7 A (the FP64
+    difference rounded to FP32 is within 2.4e-7 A), and within one FP32 ulp of |r| at coordinates
+    up to 1000 A; FP32 positions alone are off by up to half an ulp of the coordinate."""
+    rng = np.random.default_rng(8)
+
+    def split(x):
+        h = x.astype(np.float32)
+        return h, (x - h.astype(np.float64)).astype(np.float32)
+
+    for L in (10.0, 400.0, 1000.0, 2.0e4, 2.0e7):
+        xi = rng.uniform(-0.2, 1.2, 200_000) * L
+        xj = xi - rng.uniform(-8.0, 8.0, len(xi))
+        exact = xi - xj
+        hi, li = split(xi)
+        hj, lj = split(xj)
+        r = (hi - hj) + (li - lj)                  # FP32 operations, each rounded
+        assert r.dtype == np.float32
+        err = np.abs(r.astype(np.float64) - exact)
+        assert err.max() <= 5e-7, L
+        if L <= 1000.0:
+            assert np.all(err <= np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)), L
+        naive = (xi.astype(np.float32) - xj.astype(np.float32)).astype(np.float64)
+        if L >= 400.0:
+            assert np.abs(naive - exact).max() > 10 * err.max(), L
