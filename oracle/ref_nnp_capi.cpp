@@ -145,6 +145,47 @@ int ref_nnp_structure(void* h, int natoms, const int* type, const double* posn, 
     } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
 
+// NNP::symm, NNP::energy and NNP::force on an MD engine's domain: nlocal atoms (the centres)
+// followed by ghost atoms up to nall, positions already shifted by their images, and the caller's
+// neighbour entries (centre ei[e] < nlocal, neighbour ej[e] < nall), each with the
+// Newton's-third-law reaction. Outputs: the energy (networks + vacuum energies of the local atoms)
+// and the forces of all nall atoms (ghost forces for the engine's reverse communication).
+int ref_nnp_domain(void* h, int nlocal, int nall, const int* type, const double* posn, int nent, const int* ei, const int* ej,
+                   double* energy, double* force) {
+    try {
+        NNP& nnp = *(NNP*)h;
+        if (nlocal < 0 || nall < nlocal) throw std::invalid_argument("need 0 <= nlocal <= nall");
+        Structure s;
+        s.resize(nlocal, nall);
+        for (int a = 0; a < nall; ++a) {
+            if (type[a] < 0 || type[a] >= nnp.ntypes()) throw std::invalid_argument("type index out of range");
+            s.type(a) = type[a];
+            s.name(a) = nnp.nnh(type[a]).type().name();
+            for (int d = 0; d < 3; ++d) s.posn(a)[d] = posn[3 * a + d];
+        }
+        NeighborList nl;
+        nl.resize(nlocal);
+        for (int e = 0; e < nent; ++e) {
+            const int i = ei[e], j = ej[e];
+            if (i < 0 || i >= nlocal || j < 0 || j >= nall) throw std::invalid_argument("neighbour index out of range");
+            NeighborEntry x;
+            x.type_ = type[j];
+            x.index_ = j;
+            x.min_ = true;
+            s.diff(s.posn(i), s.posn(j), x.r_);
+            x.dr_ = x.r_.norm();
+            nl.add(i, x);
+        }
+        NNP::init(nnp, s);
+        NNP::symm(nnp, s, nl);
+        *energy = NNP::energy(nnp, s);
+        NNP::force(nnp, s, nl);
+        for (int a = 0; a < nall; ++a)
+            for (int d = 0; d < 3; ++d) force[3 * a + d] = s.force(a)[d];
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
 // ptnl::PotNNPE::read of a potential file (pot_nnpe.cpp:697-768) with the cutoff that the engine's
 // "pot" line would set first (the reader refuses a file whose rc differs)
 void* ref_potnnpe_read(const char* path, double rc) {

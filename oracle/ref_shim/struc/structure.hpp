@@ -3,7 +3,10 @@
 // (NNP::init / symm / energy / force / compute, nnp.cpp:316-736): per-atom type name, type index,
 // position, force and symmetry-function vector, the lattice vectors R (columns), the energy,
 // and diff(a, b, r) = a - b, the difference that the verlet::List functions correct by the image
-// (nnp.cpp:394-395). The caller fills it from arrays. Test infrastructure for pinning the oracle.
+// (nnp.cpp:394-395). The caller fills it from arrays. resize(n, nall) keeps nall atoms of which
+// the first n are the structure's own (nAtoms, the centres); the others are ghost atoms that only
+// appear as neighbours and receive forces, as in an MD engine's domain. Test infrastructure for
+// pinning the oracle.
 #pragma once
 #include <string>
 #include <vector>
@@ -17,16 +20,19 @@ class Structure {
     std::vector<Eigen::VectorXd> symm_;
     Eigen::Matrix3d R_;
     double pe_ = 0;
+    int n_ = 0;
 
 public:
-    void resize(int n) {
-        name_.assign(n, std::string());
-        type_.assign(n, 0);
-        posn_.assign(n, Eigen::Vector3d());
-        force_.assign(n, Eigen::Vector3d());
-        symm_.assign(n, Eigen::VectorXd());
+    void resize(int n) { resize(n, n); }
+    void resize(int n, int nall) {
+        n_ = n;
+        name_.assign(nall, std::string());
+        type_.assign(nall, 0);
+        posn_.assign(nall, Eigen::Vector3d());
+        force_.assign(nall, Eigen::Vector3d());
+        symm_.assign(nall, Eigen::VectorXd());
     }
-    int nAtoms() const { return (int)type_.size(); }
+    int nAtoms() const { return n_; }
     std::string& name(int i) { return name_[i]; }
     const std::string& name(int i) const { return name_[i]; }
     int& type(int i) { return type_[i]; }

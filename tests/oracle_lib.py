@@ -330,6 +330,7 @@ class RefNNP:
         L.ref_nnp_rc.restype = C.c_double
         L.ref_nnp_ninput.argtypes = [C.c_void_p, C.c_int]
         L.ref_nnp_write.argtypes = [C.c_void_p, C.c_char_p]
+        L.ref_nnp_domain.argtypes = [C.c_void_p, C.c_int, C.c_int, _I, _D, C.c_int, _I, _I, _D, _D]
         L.ref_potnnpe_read.restype = C.c_void_p
         L.ref_potnnpe_read.argtypes = [C.c_char_p, C.c_double]
         L.ref_potnnpe_free.argtypes = [C.c_void_p]
@@ -342,6 +343,18 @@ class RefNNP:
         if not h:
             raise RuntimeError(self.L.ref_nnp_last_error().decode())
         return C.c_void_p(h)
+
+    def domain(self, h, nlocal, types, posn, ei, ej):
+        """(E, F[nall]) of NNP on an MD engine's domain: nlocal centres then ghosts, the caller's
+        neighbour entries (positions already shifted by their images)."""
+        nall = len(types)
+        E, F = np.zeros(1), np.zeros((nall, 3))
+        rc = self.L.ref_nnp_domain(h, int(nlocal), nall, _i(np.ascontiguousarray(types, np.int32)),
+                                   _d(np.ascontiguousarray(posn, np.float64)), len(ei), _i(np.ascontiguousarray(ei, np.int32)),
+                                   _i(np.ascontiguousarray(ej, np.int32)), _d(E), _d(F))
+        if rc != 0:
+            raise RuntimeError(self.L.ref_nnp_last_error().decode())
+        return float(E[0]), F
 
     def potnnpe_read(self, path, rc):
         """The MD engine's ptnl::PotNNPE reading a potential file (its cutoff set first, as the

@@ -53,3 +53,41 @@ def test_fast_ghost_domain_matches(case):
             a = sorted(map(tuple, np.round(X[nb[o1[i]:o1[i + 1]]], 9)))
             b = sorted(map(tuple, np.round(dom.x[dom.neigh[o2[i]:o2[i + 1]]], 9)))
             assert a == b, i
+
+
+@pytest.mark.skipif(not __import__("oracle_lib").REF_SRC.exists(), reason="reference sources not present on this machine")
+def test_reference_on_domain_is_the_periodic_structure(oracle, tmp_path):
+    """The reference's own NNP (nnp.cpp compiled with the struc stand-ins) on an MD engine's
+    domain: local atoms as the centres, ghosts only as neighbours, the full rows cut to rc, the
+    Newton's-third-law reaction on every entry. Its energy is the periodic structure's, and its
+    local + ghost forces, folded onto the owners, are the oracle's periodic forces: the semantics
+    of the caller-list entry point, ann_compute_list, held to the reference's code."""
+    from pathlib import Path
+    from ann_gb300.api import pack_batch
+    from oracle_lib import RefNNP
+    ref = RefNNP()
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "ref_nnp.npz")
+    for name in [str(n) for n in gold["pot_names"]]:
+        text = str(gold[f"pot_{name}"])
+        p = tmp_path / f"{name}.ann"
+        p.write_text(text)
+        h = ref.read(p)
+        try:
+            pot = oracle.load_text(text)
+            nt, rc = pot.ntypes, ref.L.ref_nnp_rc(h)
+            for x, t, R in cases.small_binary(n_struc=1, seed=23) + cases.tiny_cells()[:2]:
+                t = (np.asarray(t) % nt).astype(np.int32)
+                dom = build_domain(x, t, R, rc + 1.0, seed=2)
+                off = np.concatenate([[0], np.cumsum(dom.numneigh)])
+                ei = np.repeat(np.arange(dom.nlocal), dom.numneigh)
+                ej = dom.neigh
+                keep = np.linalg.norm(dom.x[ei] - dom.x[ej], axis=1) < rc
+                assert off[-1] == len(ej)
+                E, F = ref.domain(h, dom.nlocal, dom.type, dom.x, ei[keep], ej[keep])
+                offs, posn, types, cell = pack_batch([(dom.x[:dom.nlocal], dom.type[:dom.nlocal], R)])
+                E0, F0, _, _, _ = pot.compute(offs, posn, types, cell)
+                assert abs(E - E0[0]) <= 1e-12 * max(1.0, abs(E0[0])), name
+                assert np.abs(dom.fold(F) - F0).max() <= 1e-12 * max(1.0, np.abs(F0).max()), name
+                assert np.abs(F[dom.nlocal:]).max() > 0.0      # the ghosts carry force for the owners
+        finally:
+            ref.L.ref_nnp_free(h)
